@@ -1,0 +1,211 @@
+"""GB300-native tiled Gaussian-splatting pass behind a C ABI.
+
+The CUDA library (``csrc/``, built into ``_build/libgs3d.so`` by ``build.py``)
+replaces the data path of the reference's ``TiledGaussianPipeline``
+(src/renderer/pipeline/TiledGaussianPipeline.ts:39-484). This module is the
+host-side mirror of that class for Python callers and tests: the same method
+names, argument meaning and error behaviour (``RangeError``/``TypeError``/
+``Error`` become ``ValueError``/``TypeError``/``RuntimeError``), calling the C
+ABI through ctypes. Device memory, when the caller has none of its own, comes
+from torch; torch is plumbing only, every kernel is in the library.
+
+There is no CPU fallback: if the library cannot be loaded every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+from . import abi
+from .abi import (GS3D_OK, Camera, GaussianData, PipelineDesc, Resources, Stats, Targets)
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libgs3d.so")
+_lib = None
+_lock = threading.Lock()
+
+
+def library_path() -> str:
+    return _LIB_PATH
+
+
+def load(build_if_missing: bool = True):
+    """Load libgs3d.so (building it first when absent or stale)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if build_if_missing:
+                from . import build as _build
+                _build.build()
+            if not os.path.exists(_LIB_PATH):
+                raise RuntimeError(f"CUDA library missing: {_LIB_PATH} (run build.py)")
+            _lib = abi.bind(C.CDLL(_LIB_PATH))
+    return _lib
+
+
+class GaussianPassError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{abi.STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+def _raise(lib, status: int, pipeline=None, context: str = "") -> None:
+    if status == GS3D_OK:
+        return
+    msg = lib.gs3d_pipeline_last_error(pipeline).decode() if pipeline else ""
+    msg = msg or lib.gs3d_status_string(status).decode()
+    if context:
+        msg = f"{context}: {msg}"
+    if status == abi.GS3D_ERROR_RANGE:
+        raise ValueError(msg)
+    if status == abi.GS3D_ERROR_INVALID_ARGUMENT:
+        raise TypeError(msg)
+    raise GaussianPassError(status, msg)
+
+
+def gaussian_data_from_tensors(count: int, active_count: int, sh_degree: int, means, scales_opacity,
+                               rotations, sh_coefficients) -> GaussianData:
+    """Describe resident device buffers (torch tensors or raw pointers) as GaussianData."""
+    def ptr(x):
+        return int(x.data_ptr()) if hasattr(x, "data_ptr") else int(x)
+    d = GaussianData()
+    d.count, d.active_count, d.sh_degree = int(count), int(active_count), int(sh_degree)
+    d.means, d.scales_opacity = ptr(means), ptr(scales_opacity)
+    d.rotations, d.sh_coefficients = ptr(rotations), ptr(sh_coefficients)
+    return d
+
+
+def default_options() -> dict:
+    """The reference's pass defaults (GaussianPass.ts:170-256)."""
+    return {
+        "depth_sort_mode": "float32", "antialias_mode": "compensated",
+        "intersection_capacity": 262_144, "background": (0.0, 0.0, 0.0, 0.0),
+        "max_rasterized_splats_per_tile": None, "raster_chunk_size": 8192,
+        "subpixel_sample_culling": True, "raster_transmittance_threshold": 1e-4,
+        "depth_alpha_threshold": 0.95, "filter_variance": 0.3, "invalid_depth_value": 1.0,
+        "boundary_policy": "clip", "raster_precision": "fp32", "depth_encoding": "device",
+        "device": 0,
+    }
+
+
+def make_desc(options: dict | None = None) -> PipelineDesc:
+    lib = load()
+    o = default_options()
+    o.update(options or {})
+    d = PipelineDesc()
+    lib.gs3d_pipeline_desc_defaults(C.byref(d))
+    d.device = int(o["device"])
+    d.depth_sort_mode = {"float32": 0, "packed16": 1}[o["depth_sort_mode"]]
+    d.antialias_mode = {"compensated": 0, "classic": 1}[o["antialias_mode"]]
+    d.intersection_capacity = int(o["intersection_capacity"])
+    d.background[:] = [float(v) for v in o["background"]]
+    d.max_rasterized_splats_per_tile = int(o["max_rasterized_splats_per_tile"] or 0)
+    d.raster_chunk_size = int(o["raster_chunk_size"] or 0)
+    d.subpixel_sample_culling = 1 if o["subpixel_sample_culling"] else 0
+    d.raster_transmittance_threshold = float(o["raster_transmittance_threshold"])
+    d.depth_alpha_threshold = float(o["depth_alpha_threshold"])
+    d.filter_variance = float(o["filter_variance"])
+    d.invalid_depth_value = float(o["invalid_depth_value"])
+    d.boundary_policy = {"clip": 0, "repeat-x": 1, "repeat-y": 2}[o["boundary_policy"]]
+    d.raster_precision = {"fp32": 0, "exact": 1, "half2": 2}[o["raster_precision"]]
+    d.depth_encoding = {"device": 0, "raw": 1}[o["depth_encoding"]]
+    return d
+
+
+def make_camera(frame: dict) -> Camera:
+    """gs3d_camera from a frame dict (see ``scenes.make_frame``)."""
+    import numpy as np
+    cam = Camera()
+    cam.projection[:] = [float(v) for v in np.asarray(frame["projection"], np.float32).ravel()]
+    view = frame.get("view")
+    if view is not None:
+        cam.view[:] = [float(v) for v in np.asarray(view, np.float32).ravel()]
+    cam.depth_near = float(frame["near"])
+    cam.depth_far = float(frame["far"])
+    table = np.ascontiguousarray(frame["objects"], np.float32)
+    cam._table = table
+    cam.object_table = table.ctypes.data_as(C.POINTER(C.c_float))
+    cam.object_count = table.size // 40
+    return cam
+
+
+class TiledGaussianPipeline:
+    """Mirror of the reference's TiledGaussianPipeline over the C ABI.
+
+    ``data`` is a :class:`GaussianData` describing resident device buffers.
+    Lifecycle: ``prepare_frame(width, height)`` then ``render(camera, ...)``
+    any number of times; ``update_data``, ``resize_intersections``,
+    ``read_stats``, ``get_resources``, ``dispose``.
+    """
+
+    def __init__(self, data: GaussianData, options: dict | None = None):
+        self._lib = load()
+        self._p = C.c_void_p()
+        self._desc = make_desc(options)
+        self._data = data
+        st = self._lib.gs3d_pipeline_create(C.byref(self._desc), C.byref(data), C.byref(self._p))
+        if st != GS3D_OK:
+            _raise(self._lib, st, None, "TiledGaussianPipeline")
+        self.width = self.height = 0
+
+    # -- reference surface -------------------------------------------------
+    def update_data(self, data: GaussianData) -> None:
+        _raise(self._lib, self._lib.gs3d_pipeline_update_data(self._p, C.byref(data)), self._p)
+        self._data = data
+
+    def resize_intersections(self, capacity: int) -> None:
+        _raise(self._lib, self._lib.gs3d_pipeline_resize_intersections(self._p, int(capacity)), self._p)
+
+    def prepare_frame(self, width: int, height: int) -> None:
+        _raise(self._lib, self._lib.gs3d_pipeline_prepare_frame(self._p, int(width), int(height)), self._p)
+        self.width, self.height = int(width), int(height)
+
+    def render(self, camera: Camera, color_ptr: int, depth_ptr: int = 0, attempt: int = 1,
+               reset_valid: bool = False, color_format: str = "rgba32f", stream: int = 0) -> None:
+        t = Targets()
+        t.color = int(color_ptr)
+        t.color_format = {"rgba16f": 0, "rgba32f": 1}[color_format]
+        t.depth = C.cast(C.c_void_p(int(depth_ptr)), C.POINTER(C.c_float)) if depth_ptr else None
+        st = self._lib.gs3d_pipeline_render(self._p, C.byref(camera), int(attempt), 1 if reset_valid else 0,
+                                            C.byref(t), C.c_void_p(int(stream)))
+        _raise(self._lib, st, self._p)
+
+    def read_stats(self) -> dict:
+        s = Stats()
+        st = self._lib.gs3d_pipeline_read_stats(self._p, C.byref(s))
+        out = {"visibleGaussianCount": s.visible_gaussian_count, "intersectionCount": s.intersection_count,
+               "requestedIntersections": s.requested_intersections,
+               "intersectionCapacity": int(s.intersection_capacity), "overflow": bool(s.overflow),
+               "deviceError": int(s.device_error)}
+        _raise(self._lib, st, self._p)
+        return out
+
+    def get_resources(self) -> Resources:
+        r = Resources()
+        _raise(self._lib, self._lib.gs3d_pipeline_get_resources(self._p, C.byref(r)), self._p)
+        return r
+
+    def set_profiling(self, enabled: bool) -> None:
+        _raise(self._lib, self._lib.gs3d_pipeline_set_profiling(self._p, 1 if enabled else 0), self._p)
+
+    def stage_times(self) -> tuple[dict, int]:
+        """Mean per-stage milliseconds over the renders profiled since the last call."""
+        ms = (C.c_float * len(abi.STAGES))()
+        n = C.c_uint32()
+        _raise(self._lib, self._lib.gs3d_pipeline_stage_times(self._p, ms, C.byref(n)), self._p)
+        return {name: float(ms[i]) for i, name in enumerate(abi.STAGES)}, int(n.value)
+
+    def last_launch_count(self) -> int:
+        return int(self._lib.gs3d_pipeline_last_launch_count(self._p))
+
+    def dispose(self) -> None:
+        if self._p:
+            self._lib.gs3d_pipeline_destroy(self._p)
+            self._p = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.dispose()
+        except Exception:
+            pass

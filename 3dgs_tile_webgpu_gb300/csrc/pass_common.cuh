@@ -1,0 +1,174 @@
+// Shared definitions of the CUDA pass: kernel parameter blocks, the per-frame
+// control block, and the decoupled look-back protocol used by the scan,
+// compaction and radix-sort kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gs {
+
+constexpr int kBlock = 256;  // threads per block for the linear kernels
+constexpr uint32_t kTileSize = 16;  // pixels per tile side (src/renderer/pipeline/constants.ts:1)
+
+// Packed scene buffers (GaussianData), device pointers.
+struct SceneView {
+  const float4* means;     // count
+  const uint2* shape;      // count
+  const uint32_t* rot;     // count
+  const uint32_t* sh;      // count * C + count (active tail at count * C)
+  uint32_t count;
+  uint32_t active;
+  uint32_t degree;
+  uint32_t C;
+};
+
+// Frame uniforms (FrameUniforms.ts:18-58) plus pass options.
+struct FrameView {
+  float P[16];             // projection, column-major
+  float vw, vh, vnear, vfar;
+  float filter;
+  uint32_t axis;           // boundary axis 0/1/2
+  uint32_t tiles_x, tiles_y;
+  uint32_t object_count;
+  uint32_t antialias;      // 0 compensated, 1 classic
+  uint32_t subpixel;       // subpixel sample culling
+  uint32_t depth_mode;     // 0 float32, 1 packed16
+  const float* objects;    // object_count * 40, device
+  float background[4];
+  float t_threshold;
+  float depth_alpha_threshold;
+  float invalid_depth;
+  uint32_t chunk;          // raster chunk size, 0 = none
+  uint32_t max_per_tile;   // 0 = uncapped
+  uint32_t depth_encoding; // 0 device depth, 1 raw
+};
+
+// Per-frame control block, zeroed before each render.
+struct Control {
+  uint32_t tickets[16];          // dynamic tile ids of the look-back kernels
+  uint32_t depth_hist[4][256];   // digit histograms of the depth sort
+  uint32_t tile_hist[4][256];    // digit histograms of the tile sort
+  uint32_t visible_state[4];     // visible, visible, radix blocks, 0
+  uint32_t state[4];             // count, total, radix blocks, overflow
+  uint32_t error;                // bit 0: look-back wait expired
+  uint32_t pad[3];
+};
+
+enum Ticket { kTicketCompact = 0, kTicketScan = 1, kTicketSortBase = 2 };
+
+// ---------------------------------------------------------------------------
+// Decoupled look-back status words: [63:34] epoch, [33:32] flag, [31:0] value.
+// A word whose epoch differs from the launch's epoch is "not yet published",
+// so the status array never needs clearing between launches.
+constexpr unsigned long long kFlagAggregate = 1ull;
+constexpr unsigned long long kFlagInclusive = 2ull;
+constexpr uint32_t kSpinLimit = 1u << 22;  // polls before a wait is declared expired
+
+__device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long pack_status(uint32_t epoch, unsigned long long flag, uint32_t value) {
+  return ((unsigned long long)epoch << 34) | (flag << 32) | (unsigned long long)value;
+}
+__device__ __forceinline__ uint32_t sat_add(uint32_t a, uint32_t b) { return a + min(b, 0xffffffffu - a); }
+
+// Walk back from tile-1 summing published values until an inclusive prefix is
+// found. Bounded: after kSpinLimit polls of one word the wait is declared
+// expired, bit 0 of *err is set and the missing value counts as zero, so the
+// kernel always finishes and the host sees the error.
+template <bool SATURATE>
+__device__ __forceinline__ uint32_t lookback(const unsigned long long* status, uint32_t stride, uint32_t tile,
+                                             uint32_t epoch, uint32_t* err) {
+  uint32_t excl = 0;
+  int64_t t = (int64_t)tile - 1;
+  while (t >= 0) {
+    const unsigned long long* p = status + (size_t)t * stride;
+    unsigned long long v = ld_acquire(p);
+    uint32_t polls = 0;
+    uint32_t backoff = 8;
+    while ((uint32_t)(v >> 34) != epoch) {
+      if (++polls >= kSpinLimit) {
+        atomicOr(err, 1u);
+        return excl;
+      }
+      __nanosleep(backoff);
+      backoff = backoff < 256 ? backoff * 2 : 256;
+      v = ld_acquire(p);
+    }
+    uint32_t val = (uint32_t)v;
+    excl = SATURATE ? sat_add(excl, val) : excl + val;
+    if (((v >> 32) & 3ull) == kFlagInclusive) break;
+    --t;
+  }
+  return excl;
+}
+
+// ---------------------------------------------------------------------------
+// Block-wide exclusive scan of one value per thread (256 threads).
+template <bool SATURATE>
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* s_warp, uint32_t* total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x = SATURATE ? sat_add(y, x) : y + x;
+  }
+  if (lane == 31) s_warp[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = lane < (kBlock / 32) ? s_warp[lane] : 0u;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w = SATURATE ? sat_add(y, w) : y + w;
+    }
+    if (lane < (kBlock / 32)) s_warp[lane] = w;
+  }
+  __syncthreads();
+  uint32_t warp_prefix = warp == 0 ? 0u : s_warp[warp - 1];
+  uint32_t incl = SATURATE ? sat_add(warp_prefix, x) : warp_prefix + x;
+  *total = s_warp[kBlock / 32 - 1];
+  // Exclusive value = the previous thread's inclusive value (exact for the
+  // saturating form too, since saturating addition is associative).
+  uint32_t prev = __shfl_up_sync(0xffffffffu, incl, 1);
+  uint32_t excl = lane == 0 ? warp_prefix : prev;
+  __syncthreads();
+  return excl;
+}
+
+// Launch wrappers implemented in the .cu files.
+void launch_project(const SceneView& s, const FrameView& f, float4* mean, float4* conic, float4* color,
+                    uint32_t* counts, uint32_t* keys, cudaStream_t st);
+void launch_compact(const uint32_t* keys, uint32_t n, uint32_t* vis_off, uint32_t* keys_out, uint32_t* vals_out,
+                    Control* ctl, unsigned long long* status, uint32_t epoch, int depth_passes, cudaStream_t st);
+void launch_scan_counts(const uint32_t* sorted_ids, const uint32_t* tile_counts, uint32_t n_max,
+                        uint32_t* ordered, uint32_t* offsets, Control* ctl, unsigned long long* status,
+                        uint32_t epoch, uint32_t capacity, uint32_t attempt, int reset_valid, uint32_t* output_state,
+                        cudaStream_t st);
+void launch_emit(const uint32_t* sorted_ids, uint32_t n_max, const float4* mean, const float4* conic,
+                 const uint32_t* ordered, const uint32_t* offsets, const FrameView& f, Control* ctl,
+                 uint32_t capacity, uint32_t* tile_keys, uint32_t* tile_vals, int tile_passes, int tile_digit_bits,
+                 cudaStream_t st);
+void launch_tile_ranges(const uint32_t* sorted_tiles, Control* ctl, uint32_t ntile, uint32_t* offsets, int sms,
+                        cudaStream_t st);
+// Onesweep LSD pass. n is read from *n_ptr on the device.
+void launch_onesweep(int bits, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
+                     uint32_t* vals_out, const uint32_t* n_ptr, uint32_t n_max, int shift, const uint32_t* hist,
+                     unsigned long long* status, uint32_t* ticket, uint32_t epoch, uint32_t* err, cudaStream_t st);
+constexpr uint32_t kSortTile = 4096;  // items per onesweep block
+// Rasterizer (precision: 0 fp32, 1 exact, 2 half2).
+void launch_raster(int precision, const uint32_t* tile_offsets, const uint32_t* sorted_ids, const float4* mean,
+                   const float4* conic, const float4* color, const FrameView& f, const Control* ctl, void* color_out,
+                   int color_half, float* depth_out, cudaStream_t st);
+void launch_raster_exact(const uint32_t* tile_offsets, const uint32_t* sorted_ids, const float4* mean,
+                         const float4* conic, const float4* color, const FrameView& f, const Control* ctl,
+                         void* color_out, int color_half, float* depth_out, cudaStream_t st);
+
+}  // namespace gs

@@ -1,0 +1,404 @@
+// Kernels whose integer outputs must be bit-identical to the CPU restatement:
+// projection + tile count, visibility compaction, the saturating intersection
+// scan, intersection emission and tile ranges; plus the bit-exact raster form.
+// Built with --fmad=false (see build.py): no multiply-add contraction, so each
+// float expression rounds exactly like the CPU restatement.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "pass_common.cuh"
+#include "raster_impl.cuh"
+#include "splat_math.cuh"
+
+namespace gs {
+
+// ---------------------------------------------------------------------------
+// K1: decode + project + cull + SH + tile count, one thread per active ordinal
+// (ProjectionStage.ts:385-649). Writes the projected mean/conic/colour/count
+// like the reference, plus the depth sort key (or kInvisibleKey), which the
+// compaction kernel consumes instead of re-reading the 16-byte means.
+template <int DEG>
+__device__ __forceinline__ void load_sh(const uint32_t* __restrict__ p, uint32_t* co) {
+  constexpr int C = (DEG + 1) * (DEG + 1);
+  if (DEG == 3) {
+    const uint4* v = reinterpret_cast<const uint4*>(p);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      uint4 w = __ldg(v + i);
+      co[4 * i] = w.x; co[4 * i + 1] = w.y; co[4 * i + 2] = w.z; co[4 * i + 3] = w.w;
+    }
+  } else if (DEG == 1) {
+    uint4 w = __ldg(reinterpret_cast<const uint4*>(p));
+    co[0] = w.x; co[1] = w.y; co[2] = w.z; co[3] = w.w;
+  } else {
+#pragma unroll
+    for (int i = 0; i < C; ++i) co[i] = __ldg(p + i);
+  }
+}
+
+template <int DEG>
+__global__ void __launch_bounds__(kBlock) k_project(SceneView s, FrameView f, float4* __restrict__ mean_out,
+                                                    float4* __restrict__ conic_out, float4* __restrict__ color_out,
+                                                    uint32_t* __restrict__ count_out, uint32_t* __restrict__ key_out) {
+  constexpr int C = (DEG + 1) * (DEG + 1);
+  const uint32_t gid = blockIdx.x * kBlock + threadIdx.x;
+  if (gid >= s.active) return;
+  float4 mo4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  uint32_t cnt = 0, key = kInvisibleKey;
+  do {
+    const uint32_t slot = __ldg(s.sh + (size_t)s.count * C + gid);
+    if (slot >= s.count) break;  // out-of-range tail entries never draw
+    const float4 mo = __ldg(s.means + slot);
+    if (mo.w < 0.0f) break;  // empty slot (ProjectionStage.ts:408-410)
+    const uint32_t obj = (uint32_t)mo.w;
+    if (obj >= f.object_count) break;  // unwritten object rows are zero
+    const float* ot = f.objects + 40 * (size_t)obj;
+    if (!(__ldg(ot + 36) > 0.0f)) break;  // object visibility (:445-450)
+    const float4 so = decode_scale_opacity(__ldg(s.shape + slot));
+    const float4 q = decode_rotation(__ldg(s.rot + slot));
+    float mv[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) mv[i] = __ldg(ot + 16 + i);
+    const float camx = __ldg(ot + 32), camy = __ldg(ot + 33), camz = __ldg(ot + 34);
+    // viewDirection = normalize(positionLocal - cameraLocal) (:469)
+    const float ddx = mo.x - camx, ddy = mo.y - camy, ddz = mo.z - camz;
+    const float dlen = sqrtf((ddx * ddx + ddy * ddy) + ddz * ddz);
+    const f3 vdir = {ddx / dlen, ddy / dlen, ddz / dlen};
+    // view = modelView * (p, 1) (:479-482)
+    const float vx = ((mv[0] * mo.x + mv[4] * mo.y) + mv[8] * mo.z) + mv[12] * 1.0f;
+    const float vy = ((mv[1] * mo.x + mv[5] * mo.y) + mv[9] * mo.z) + mv[13] * 1.0f;
+    const float vz = ((mv[2] * mo.x + mv[6] * mo.y) + mv[10] * mo.z) + mv[14] * 1.0f;
+    m3 l2v;
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+      for (int r = 0; r < 3; ++r) l2v.m[c][r] = mv[4 * c + r];
+    const m3 cv = view_covariance(so, q, l2v);
+    const Projected pr = project({vx, vy, vz}, cv, f.P, f.vw, f.vh, f.vnear, f.vfar, f.filter);
+    if (!pr.ok) break;
+    float op = clampf(so.w, 0.0f, 1.0f);
+    if (f.antialias == 0u) op = op * sqrtf(clampf(pr.orig_det / pr.det, 0.0f, 1.0f));
+    if (op < (float)(1.0 / 255.0) || op != op) break;
+    const float thr = gsdm::logf_(op * 255.0f);
+    const float ex = sqrtf((thr * 2.0f) * clampf(pr.cov_x, 1e-12f, 1e4f));
+    const float ey = sqrtf((thr * 2.0f) * clampf(pr.cov_z, 1e-12f, 1e4f));
+    const float rx = ceilf(ex), ry = ceilf(ey);
+    if (rx <= 0.0f || ry <= 0.0f) break;
+    const float bminx = pr.cx - rx, bminy = pr.cy - ry, bmaxx = pr.cx + rx, bmaxy = pr.cy + ry;
+    if ((f.axis != 1u && (bmaxx < 0.0f || bminx >= f.vw)) || (f.axis != 2u && (bmaxy < 0.0f || bminy >= f.vh)))
+      break;
+    if (f.subpixel != 0u &&
+        !subpixel_has_sample(pr.cx, pr.cy, pr.conic_x, pr.conic_y, pr.conic_z, thr, ex, ey, (uint32_t)f.vw,
+                             (uint32_t)f.vh, f.axis)) {
+      mo4 = make_float4(pr.cx, pr.cy, pr.depth, -1.0f);  // subpixel marker (:572-587)
+      break;
+    }
+    const float mtx = (float)((int)f.tiles_x - 1), mty = (float)((int)f.tiles_y - 1);
+    int tminx = (int)clampf(floorf(bminx / 16.0f), 0.0f, mtx);
+    int tminy = (int)clampf(floorf(bminy / 16.0f), 0.0f, mty);
+    int tmaxx = (int)clampf(floorf(bmaxx / 16.0f), 0.0f, mtx);
+    int tmaxy = (int)clampf(floorf(bmaxy / 16.0f), 0.0f, mty);
+    if (f.axis == 1u) { tminx = 0; tmaxx = (int)f.tiles_x - 1; }
+    if (f.axis == 2u) { tminy = 0; tmaxy = (int)f.tiles_y - 1; }
+    for (int ty = tminy; ty <= tmaxy; ++ty)
+      for (int tx = tminx; tx <= tmaxx; ++tx)
+        if (boundary_tile_hit(pr.cx, pr.cy, pr.conic_x, pr.conic_y, pr.conic_z, thr, rx, ry, tx, ty, f.vw, f.vh,
+                              f.axis))
+          ++cnt;
+    if (cnt == 0) break;
+    uint32_t co[C];
+    load_sh<DEG>(s.sh + (size_t)slot * C, co);
+    const f3 col = eval_sh<DEG>(co, vdir);
+    mo4 = make_float4(pr.cx, pr.cy, pr.depth, op);
+    conic_out[gid] = make_float4(pr.conic_x, pr.conic_y, pr.conic_z, rx + ry * 512.0f);
+    color_out[gid] = make_float4(col.x, col.y, col.z, __uint_as_float(slot ^ kActiveTag));
+    if (f.depth_mode == 0u) {
+      key = __float_as_uint(pr.depth);  // visibility.ts:139
+    } else {
+      float t = clampf((pr.depth - f.vnear) / (f.vfar - f.vnear), 0.0f, 1.0f);
+      key = (uint32_t)gsdm::round_even_small(t * 65535.0f);  // visibility.ts:140-144
+    }
+  } while (false);
+  mean_out[gid] = mo4;
+  count_out[gid] = cnt;
+  key_out[gid] = key;
+}
+
+void launch_project(const SceneView& s, const FrameView& f, float4* mean, float4* conic, float4* color,
+                    uint32_t* counts, uint32_t* keys, cudaStream_t st) {
+  if (s.active == 0) return;
+  const uint32_t grid = (s.active + kBlock - 1) / kBlock;
+  switch (s.degree) {
+    case 0: k_project<0><<<grid, kBlock, 0, st>>>(s, f, mean, conic, color, counts, keys); break;
+    case 1: k_project<1><<<grid, kBlock, 0, st>>>(s, f, mean, conic, color, counts, keys); break;
+    case 2: k_project<2><<<grid, kBlock, 0, st>>>(s, f, mean, conic, color, counts, keys); break;
+    default: k_project<3><<<grid, kBlock, 0, st>>>(s, f, mean, conic, color, counts, keys); break;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Visibility compaction (scan.ts:9-83 + visibility.ts:9-61): one pass with
+// decoupled look-back. Writes visibleOffsets, the (depthKey, ordinal) records
+// in ordinal order, the visible state, and the depth sort's digit histograms.
+constexpr uint32_t kItems = 4;
+constexpr uint32_t kScanTile = kBlock * kItems;  // 1024 items per tile
+
+__global__ void __launch_bounds__(kBlock) k_compact(const uint32_t* __restrict__ keys, uint32_t n,
+                                                    uint32_t* __restrict__ vis_off, uint32_t* __restrict__ keys_out,
+                                                    uint32_t* __restrict__ vals_out, Control* __restrict__ ctl,
+                                                    unsigned long long* __restrict__ status, uint32_t epoch,
+                                                    int passes) {
+  __shared__ uint32_t s_tile, s_prefix;
+  __shared__ uint32_t s_warp[kBlock / 32];
+  __shared__ uint32_t s_hist[4][256];
+  const uint32_t tid = threadIdx.x;
+  if (tid == 0) s_tile = atomicAdd(&ctl->tickets[kTicketCompact], 1u);
+  for (uint32_t i = tid; i < 4 * 256; i += kBlock) (&s_hist[0][0])[i] = 0u;
+  __syncthreads();
+  const uint32_t tile = s_tile;
+  const uint32_t ntiles = n == 0 ? 1u : (n + kScanTile - 1) / kScanTile;
+  if (tile >= ntiles) return;
+  const uint32_t base = tile * kScanTile + tid * kItems;
+  uint32_t k[kItems];
+  if (base + kItems <= n) {
+    uint4 w = *reinterpret_cast<const uint4*>(keys + base);
+    k[0] = w.x; k[1] = w.y; k[2] = w.z; k[3] = w.w;
+  } else {
+#pragma unroll
+    for (uint32_t i = 0; i < kItems; ++i) k[i] = base + i < n ? keys[base + i] : kInvisibleKey;
+  }
+  uint32_t c = 0;
+#pragma unroll
+  for (uint32_t i = 0; i < kItems; ++i) c += k[i] != kInvisibleKey ? 1u : 0u;
+  uint32_t total;
+  const uint32_t excl = block_exclusive_scan<false>(c, s_warp, &total);
+  if (tid == 0) {
+    unsigned long long* mine = status + tile;
+    uint32_t prefix = 0;
+    if (tile == 0) {
+      st_release(mine, pack_status(epoch, kFlagInclusive, total));
+    } else {
+      st_release(mine, pack_status(epoch, kFlagAggregate, total));
+      prefix = lookback<false>(status, 1, tile, epoch, &ctl->error);
+      st_release(mine, pack_status(epoch, kFlagInclusive, prefix + total));
+    }
+    s_prefix = prefix;
+    if (tile == ntiles - 1) {
+      const uint32_t v = prefix + total;
+      ctl->visible_state[0] = v;
+      ctl->visible_state[1] = v;
+      ctl->visible_state[2] = (v + 1023u) / 1024u;
+      ctl->visible_state[3] = 0u;
+    }
+  }
+  __syncthreads();
+  uint32_t off = s_prefix + excl;
+#pragma unroll
+  for (uint32_t i = 0; i < kItems; ++i) {
+    const uint32_t idx = base + i;
+    if (idx >= n) break;
+    vis_off[idx] = off;
+    if (k[i] != kInvisibleKey) {
+      keys_out[off] = k[i];
+      vals_out[off] = idx;
+      for (int p = 0; p < passes; ++p) atomicAdd(&s_hist[p][(k[i] >> (8 * p)) & 255u], 1u);
+      ++off;
+    }
+  }
+  __syncthreads();
+  for (uint32_t d = tid; d < 256; d += kBlock)
+    for (int p = 0; p < passes; ++p)
+      if (s_hist[p][d]) atomicAdd(&ctl->depth_hist[p][d], s_hist[p][d]);
+}
+
+void launch_compact(const uint32_t* keys, uint32_t n, uint32_t* vis_off, uint32_t* keys_out, uint32_t* vals_out,
+                    Control* ctl, unsigned long long* status, uint32_t epoch, int passes, cudaStream_t st) {
+  const uint32_t grid = n == 0 ? 1u : (n + kScanTile - 1) / kScanTile;
+  k_compact<<<grid, kBlock, 0, st>>>(keys, n, vis_off, keys_out, vals_out, ctl, status, epoch, passes);
+}
+
+// ---------------------------------------------------------------------------
+// Depth-ordered tile counts + saturating exclusive scan + prepare_dispatch +
+// prepare_intersection_output (visibility.ts:63-76, scan.ts:9-99,
+// intersections.ts:10-41,114-133) in one look-back pass over visible ranks.
+__global__ void __launch_bounds__(kBlock) k_scan_counts(const uint32_t* __restrict__ ids,
+                                                        const uint32_t* __restrict__ tile_counts,
+                                                        uint32_t* __restrict__ ordered,
+                                                        uint32_t* __restrict__ offsets, Control* __restrict__ ctl,
+                                                        unsigned long long* __restrict__ status, uint32_t epoch,
+                                                        uint32_t capacity, uint32_t attempt, int reset_valid,
+                                                        uint32_t* __restrict__ output_state) {
+  __shared__ uint32_t s_tile, s_prefix;
+  __shared__ uint32_t s_warp[kBlock / 32];
+  const uint32_t tid = threadIdx.x;
+  if (tid == 0) s_tile = atomicAdd(&ctl->tickets[kTicketScan], 1u);
+  __syncthreads();
+  const uint32_t n = ctl->visible_state[0];
+  const uint32_t tile = s_tile;
+  const uint32_t ntiles = n == 0 ? 1u : (n + kScanTile - 1) / kScanTile;
+  if (tile >= ntiles) return;
+  const uint32_t base = tile * kScanTile + tid * kItems;
+  uint32_t c[kItems];
+#pragma unroll
+  for (uint32_t i = 0; i < kItems; ++i) c[i] = base + i < n ? __ldg(tile_counts + ids[base + i]) : 0u;
+  uint32_t sum = 0;
+#pragma unroll
+  for (uint32_t i = 0; i < kItems; ++i) sum = sat_add(sum, c[i]);
+  uint32_t total;
+  const uint32_t excl = block_exclusive_scan<true>(sum, s_warp, &total);
+  if (tid == 0) {
+    unsigned long long* mine = status + tile;
+    uint32_t prefix = 0;
+    if (tile == 0) {
+      st_release(mine, pack_status(epoch, kFlagInclusive, total));
+    } else {
+      st_release(mine, pack_status(epoch, kFlagAggregate, total));
+      prefix = lookback<true>(status, 1, tile, epoch, &ctl->error);
+      st_release(mine, pack_status(epoch, kFlagInclusive, sat_add(prefix, total)));
+    }
+    s_prefix = prefix;
+    if (tile == ntiles - 1) {
+      const uint32_t all = sat_add(prefix, total);
+      const bool overflow = all > capacity;
+      const uint32_t count = overflow ? 0u : all;
+      ctl->state[0] = count;
+      ctl->state[1] = all;
+      ctl->state[2] = (uint32_t)(((uint64_t)count + 1023u) / 1024u);
+      ctl->state[3] = overflow ? 1u : 0u;
+      const uint32_t last_version = reset_valid ? 0u : output_state[1];
+      output_state[0] = attempt;
+      output_state[1] = overflow ? last_version : attempt;
+      output_state[2] = all;
+      output_state[3] = overflow ? 1u : 0u;
+    }
+  }
+  __syncthreads();
+  uint32_t run = sat_add(s_prefix, excl);
+#pragma unroll
+  for (uint32_t i = 0; i < kItems; ++i) {
+    const uint32_t idx = base + i;
+    if (idx < n) {
+      ordered[idx] = c[i];
+      offsets[idx] = run;
+    }
+    run = sat_add(run, c[i]);
+  }
+}
+
+void launch_scan_counts(const uint32_t* ids, const uint32_t* tile_counts, uint32_t n_max, uint32_t* ordered,
+                        uint32_t* offsets, Control* ctl, unsigned long long* status, uint32_t epoch,
+                        uint32_t capacity, uint32_t attempt, int reset_valid, uint32_t* output_state,
+                        cudaStream_t st) {
+  const uint32_t grid = n_max == 0 ? 1u : (n_max + kScanTile - 1) / kScanTile;
+  k_scan_counts<<<grid, kBlock, 0, st>>>(ids, tile_counts, ordered, offsets, ctl, status, epoch, capacity, attempt,
+                                         reset_valid, output_state);
+}
+
+// ---------------------------------------------------------------------------
+// Intersection emission (intersections.ts:43-111): per depth rank, one
+// (tile, ordinal) record for every tile the splat contributes to, written at
+// the rank's scanned offset; sentinel padding if fewer hits than reserved.
+// Also accumulates the tile sort's digit histograms.
+__global__ void __launch_bounds__(kBlock) k_emit(const uint32_t* __restrict__ ids, const float4* __restrict__ mean,
+                                                 const float4* __restrict__ conic,
+                                                 const uint32_t* __restrict__ ordered,
+                                                 const uint32_t* __restrict__ offsets, FrameView f,
+                                                 Control* __restrict__ ctl, uint32_t capacity,
+                                                 uint32_t* __restrict__ tile_keys, uint32_t* __restrict__ tile_vals,
+                                                 int passes, int digit_bits) {
+  if (ctl->state[3] != 0u) return;  // overflow: emission dispatch is zero
+  __shared__ uint32_t s_hist[4][256];
+  const uint32_t tid = threadIdx.x;
+  for (uint32_t i = tid; i < 4 * 256; i += kBlock) (&s_hist[0][0])[i] = 0u;
+  __syncthreads();
+  const uint32_t n = ctl->visible_state[0];
+  const uint32_t r = blockIdx.x * kBlock + tid;
+  const uint32_t mask = (1u << digit_bits) - 1u;
+  const uint32_t ntile = f.tiles_x * f.tiles_y;
+  if (r < n) {
+    const uint32_t g = ids[r];
+    const float4 m = __ldg(mean + g);
+    const float4 c = __ldg(conic + g);
+    const uint32_t packed = (uint32_t)c.w;
+    const float rx = (float)(packed % 512u), ry = (float)(packed / 512u);
+    const float thr = gsdm::logf_(m.w * 255.0f);
+    const float mtx = (float)((int)f.tiles_x - 1), mty = (float)((int)f.tiles_y - 1);
+    int tminx = (int)clampf(floorf((m.x - rx) / 16.0f), 0.0f, mtx);
+    int tminy = (int)clampf(floorf((m.y - ry) / 16.0f), 0.0f, mty);
+    int tmaxx = (int)clampf(floorf((m.x + rx) / 16.0f), 0.0f, mtx);
+    int tmaxy = (int)clampf(floorf((m.y + ry) / 16.0f), 0.0f, mty);
+    if (f.axis == 1u) { tminx = 0; tmaxx = (int)f.tiles_x - 1; }
+    if (f.axis == 2u) { tminy = 0; tmaxy = (int)f.tiles_y - 1; }
+    const uint32_t reserved = ordered[r];
+    const uint32_t base = offsets[r];
+    uint32_t local = 0;
+    for (int ty = tminy; ty <= tmaxy; ++ty)
+      for (int tx = tminx; tx <= tmaxx; ++tx)
+        if (boundary_tile_hit(m.x, m.y, c.x, c.y, c.z, thr, rx, ry, tx, ty, f.vw, f.vh, f.axis)) {
+          if (local < reserved && base + local < capacity) {
+            const uint32_t t = (uint32_t)ty * f.tiles_x + (uint32_t)tx;
+            tile_keys[base + local] = t;
+            tile_vals[base + local] = g;
+            for (int p = 0; p < passes; ++p) atomicAdd(&s_hist[p][(t >> (p * digit_bits)) & mask], 1u);
+          }
+          ++local;
+        }
+    for (uint32_t pad = local; pad < reserved; ++pad)
+      if (base + pad < capacity) {
+        tile_keys[base + pad] = ntile;
+        tile_vals[base + pad] = g;
+        for (int p = 0; p < passes; ++p) atomicAdd(&s_hist[p][(ntile >> (p * digit_bits)) & mask], 1u);
+      }
+  }
+  __syncthreads();
+  const uint32_t radix = 1u << digit_bits;
+  for (uint32_t d = tid; d < radix; d += kBlock)
+    for (int p = 0; p < passes; ++p)
+      if (s_hist[p][d]) atomicAdd(&ctl->tile_hist[p][d], s_hist[p][d]);
+}
+
+void launch_emit(const uint32_t* ids, uint32_t n_max, const float4* mean, const float4* conic,
+                 const uint32_t* ordered, const uint32_t* offsets, const FrameView& f, Control* ctl,
+                 uint32_t capacity, uint32_t* tile_keys, uint32_t* tile_vals, int passes, int digit_bits,
+                 cudaStream_t st) {
+  if (n_max == 0) return;
+  const uint32_t grid = (n_max + kBlock - 1) / kBlock;
+  k_emit<<<grid, kBlock, 0, st>>>(ids, mean, conic, ordered, offsets, f, ctl, capacity, tile_keys, tile_vals, passes,
+                                  digit_bits);
+}
+
+// ---------------------------------------------------------------------------
+// Tile ranges (tileOffsets.ts:4-128): offsets[t] = first sorted index with
+// tile >= t, i.e. the reference's boundary detection followed by its
+// suffix-min fill, written directly (offsets[T] = first sentinel or count).
+__global__ void k_tile_ranges(const uint32_t* __restrict__ keys, const Control* __restrict__ ctl, uint32_t ntile,
+                              uint32_t* __restrict__ off) {
+  const uint32_t n = ctl->state[0];
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i <= n; i += stride) {
+    const uint32_t lo = i == 0 ? 0u : keys[i - 1] + 1u;
+    const uint32_t hi = i == n ? ntile : min(keys[i], ntile);
+    for (uint32_t t = lo; t <= hi; ++t) off[t] = i;
+    if (i == n) break;
+  }
+}
+
+void launch_tile_ranges(const uint32_t* keys, Control* ctl, uint32_t ntile, uint32_t* offsets, int sms,
+                        cudaStream_t st) {
+  k_tile_ranges<<<sms * 4, kBlock, 0, st>>>(keys, ctl, ntile, offsets);
+}
+
+// ---------------------------------------------------------------------------
+void launch_raster_exact(const uint32_t* tile_offsets, const uint32_t* ids, const float4* mean, const float4* conic,
+                         const float4* color, const FrameView& f, const Control* ctl, void* color_out,
+                         int color_half, float* depth_out, cudaStream_t st) {
+  const uint32_t grid = f.tiles_x * f.tiles_y;
+  if (color_half)
+    k_raster<ExactMath, true><<<grid, kBlock, 0, st>>>(tile_offsets, ids, mean, conic, color, f, ctl, color_out,
+                                                       depth_out);
+  else
+    k_raster<ExactMath, false><<<grid, kBlock, 0, st>>>(tile_offsets, ids, mean, conic, color, f, ctl, color_out,
+                                                        depth_out);
+}
+
+}  // namespace gs

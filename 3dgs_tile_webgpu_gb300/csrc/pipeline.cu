@@ -1,0 +1,618 @@
+// Host side of the C ABI (include/gs3d.h): workspace ownership, validation
+// with the reference's error semantics, and the per-frame launch sequence of
+// TiledGaussianPipeline.render (src/renderer/pipeline/TiledGaussianPipeline.ts:324-341).
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <algorithm>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/gs3d.h"
+#include "pass_common.cuh"
+
+using namespace gs;
+
+namespace {
+
+constexpr uint32_t kObjectRing = 4;  // pinned object-table staging slots
+constexpr uint32_t kEpochMask = (1u << 30) - 1u;
+constexpr uint32_t kStageEvents = GS3D_STAGE_COUNT + 1;
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+}  // namespace
+
+struct gs3d_pipeline {
+  gs3d_pipeline_desc desc{};
+  gs3d_gaussian_data data{};
+  int device = 0;
+  int sms = 148;
+  std::string error;
+  // Per-slot workspaces (sized by data.count).
+  uint32_t slot_cap = 0;
+  float4* mean = nullptr;
+  float4* conic = nullptr;
+  float4* color = nullptr;
+  uint32_t* counts = nullptr;
+  uint32_t* keys = nullptr;
+  uint32_t* vis_off = nullptr;
+  uint32_t* dk[2] = {nullptr, nullptr};
+  uint32_t* dv[2] = {nullptr, nullptr};
+  uint32_t* ordered = nullptr;
+  uint32_t* ioff = nullptr;
+  // Intersection workspaces (sized by capacity).
+  uint64_t capacity = 0;
+  uint32_t* tk[2] = {nullptr, nullptr};
+  uint32_t* tv[2] = {nullptr, nullptr};
+  // Tiles.
+  uint32_t tile_cap = 0;
+  uint32_t* tile_offsets = nullptr;
+  // Control, output state, look-back status.
+  Control* ctl = nullptr;
+  uint32_t* output_state = nullptr;
+  unsigned long long* status = nullptr;
+  size_t status_words = 0;
+  uint32_t epoch = 0;
+  // Object table staging.
+  uint32_t object_cap = 0;
+  float* objects_dev[kObjectRing] = {};
+  float* objects_pinned[kObjectRing] = {};
+  cudaEvent_t object_ev[kObjectRing] = {};
+  bool object_ev_used[kObjectRing] = {};
+  uint32_t frame_index = 0;
+  // Frame.
+  bool prepared = false;
+  uint32_t width = 0, height = 0, tiles_x = 0, tiles_y = 0;
+  cudaStream_t last_stream = nullptr;
+  uint32_t last_launches = 0;
+  // Final buffers of the two sorts (after ping-pong).
+  int depth_final = 0;
+  int tile_final = 0;
+  // Kernel timing: one set of GS3D_STAGE_COUNT + 1 events per profiled render.
+  bool profiling = false;
+  std::vector<cudaEvent_t> events;  // pool, in sets of kStageEvents
+  uint32_t profiled = 0;            // sets recorded since the last read
+};
+
+namespace {
+
+gs3d_status fail(gs3d_pipeline* p, gs3d_status s, const std::string& msg) {
+  if (p) p->error = msg;
+  return s;
+}
+
+gs3d_status cuda_fail(gs3d_pipeline* p, cudaError_t e, const char* what) {
+  cudaGetLastError();
+  gs3d_status s = e == cudaErrorMemoryAllocation ? GS3D_ERROR_OUT_OF_MEMORY : GS3D_ERROR_CUDA;
+  return fail(p, s, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+template <typename T>
+void dfree(T*& ptr) {
+  if (ptr) cudaFree((void*)ptr);
+  ptr = nullptr;
+}
+
+template <typename T>
+cudaError_t dalloc(T*& ptr, size_t count) {
+  dfree(ptr);
+  if (count == 0) count = 1;
+  return cudaMalloc((void**)&ptr, count * sizeof(T));
+}
+
+uint32_t tiles_for(uint32_t px) { return (px + 15u) / 16u; }
+
+uint32_t ceil_log2(uint64_t v) {
+  uint32_t b = 0;
+  while ((1ull << b) < v) ++b;
+  return b;
+}
+
+gs3d_status validate_desc(gs3d_pipeline* p, const gs3d_pipeline_desc& d) {
+  if (d.abi_version != GS3D_ABI_VERSION) return fail(p, GS3D_ERROR_INVALID_ARGUMENT, "abi_version mismatch");
+  if (d.depth_sort_mode > 1) return fail(p, GS3D_ERROR_INVALID_ARGUMENT, "depthSortMode must be float32 or packed16");
+  if (d.antialias_mode > 1) return fail(p, GS3D_ERROR_INVALID_ARGUMENT, "antialiasMode must be compensated or classic");
+  if (d.boundary_policy > 2) return fail(p, GS3D_ERROR_INVALID_ARGUMENT, "boundaryPolicy must be clip, repeat-x or repeat-y");
+  if (d.raster_precision > 2) return fail(p, GS3D_ERROR_INVALID_ARGUMENT, "unknown raster precision");
+  if (d.depth_encoding > 1) return fail(p, GS3D_ERROR_INVALID_ARGUMENT, "unknown depth encoding");
+  // GaussianPass.ts:178-192,231-255
+  if (d.intersection_capacity == 0 || d.intersection_capacity > 0x7fffffffull)
+    return fail(p, GS3D_ERROR_RANGE, "intersectionCapacity must be a positive integer below 2^31");
+  if (!(d.raster_transmittance_threshold > 0.0f && d.raster_transmittance_threshold < 1.0f))
+    return fail(p, GS3D_ERROR_RANGE, "rasterTransmittanceThreshold must be finite and in (0, 1)");
+  if (!(d.depth_alpha_threshold >= 0.0f && d.depth_alpha_threshold <= 1.0f))
+    return fail(p, GS3D_ERROR_RANGE, "depthAlphaThreshold must be finite and in [0, 1]");
+  // rasterChunks.ts:208-227 (the 65,535-task bound is a WebGPU dispatch limit
+  // and does not apply to this implementation).
+  if (d.raster_chunk_size != 0 && (d.raster_chunk_size < 256 || d.raster_chunk_size % 256 != 0))
+    return fail(p, GS3D_ERROR_RANGE, "rasterChunkSize must be a multiple of 256 and at least 256");
+  if (!isfinite(d.filter_variance) || d.filter_variance < 0.0f)
+    return fail(p, GS3D_ERROR_RANGE, "filterVariance must be finite and non-negative");
+  return GS3D_OK;
+}
+
+gs3d_status validate_data(gs3d_pipeline* p, const gs3d_gaussian_data* d) {
+  if (!d) return fail(p, GS3D_ERROR_INVALID_ARGUMENT, "GaussianData is null");
+  // GaussianData.ts:76-167
+  if (d->count == 0) return fail(p, GS3D_ERROR_RANGE, "GaussianData count must be a positive integer");
+  if (d->sh_degree > 3) return fail(p, GS3D_ERROR_RANGE, "GaussianData shDegree must be 0, 1, 2, or 3");
+  if (d->active_count > d->count) return fail(p, GS3D_ERROR_RANGE, "active count exceeds slot count");
+  if (!d->means || !d->scales_opacity || !d->rotations || !d->sh_coefficients)
+    return fail(p, GS3D_ERROR_INVALID_ARGUMENT, "Invalid compact Gaussian shape attribute");
+  if (((uintptr_t)d->means & 15u) || ((uintptr_t)d->scales_opacity & 7u) || ((uintptr_t)d->rotations & 3u) ||
+      ((uintptr_t)d->sh_coefficients & 15u))
+    return fail(p, GS3D_ERROR_INVALID_ARGUMENT, "packed buffers must be naturally aligned (SH to 16 bytes)");
+  return GS3D_OK;
+}
+
+size_t status_words_needed(uint32_t slots, uint64_t capacity) {
+  const size_t scan = (slots + 1023u) / 1024u + 1;
+  const size_t sort_slots = ((size_t)slots + kSortTile - 1) / kSortTile * 256 + 256;
+  const size_t sort_caps = (size_t)((capacity + kSortTile - 1) / kSortTile) * 256 + 256;
+  return std::max(scan, std::max(sort_slots, sort_caps));
+}
+
+gs3d_status ensure_status(gs3d_pipeline* p) {
+  const size_t need = status_words_needed(p->slot_cap, p->capacity);
+  if (need <= p->status_words) return GS3D_OK;
+  cudaError_t e = dalloc(p->status, need);
+  if (e != cudaSuccess) return cuda_fail(p, e, "allocating look-back status");
+  e = cudaMemset(p->status, 0, need * sizeof(unsigned long long));
+  if (e != cudaSuccess) return cuda_fail(p, e, "clearing look-back status");
+  p->status_words = need;
+  p->epoch = 0;
+  return GS3D_OK;
+}
+
+gs3d_status ensure_slots(gs3d_pipeline* p, uint32_t count) {
+  if (count <= p->slot_cap) return GS3D_OK;
+  // AttributePool.grow semantics: at least double.
+  const uint32_t cap = std::max(count, p->slot_cap * 2u);
+  cudaError_t e = cudaSuccess;
+  if ((e = dalloc(p->mean, cap)) || (e = dalloc(p->conic, cap)) || (e = dalloc(p->color, cap)) ||
+      (e = dalloc(p->counts, cap)) || (e = dalloc(p->keys, cap)) || (e = dalloc(p->vis_off, cap)) ||
+      (e = dalloc(p->dk[0], cap)) || (e = dalloc(p->dk[1], cap)) || (e = dalloc(p->dv[0], cap)) ||
+      (e = dalloc(p->dv[1], cap)) || (e = dalloc(p->ordered, cap)) || (e = dalloc(p->ioff, cap))) {
+    p->slot_cap = 0;
+    return cuda_fail(p, e, "allocating per-Gaussian workspaces");
+  }
+  cudaMemset(p->conic, 0, (size_t)cap * sizeof(float4));
+  cudaMemset(p->color, 0, (size_t)cap * sizeof(float4));
+  p->slot_cap = cap;
+  return ensure_status(p);
+}
+
+gs3d_status ensure_capacity(gs3d_pipeline* p, uint64_t capacity) {
+  cudaError_t e = cudaSuccess;
+  if ((e = dalloc(p->tk[0], capacity)) || (e = dalloc(p->tk[1], capacity)) || (e = dalloc(p->tv[0], capacity)) ||
+      (e = dalloc(p->tv[1], capacity))) {
+    p->capacity = 0;
+    return cuda_fail(p, e, "allocating intersection workspaces");
+  }
+  p->capacity = capacity;
+  return ensure_status(p);
+}
+
+gs3d_status ensure_objects(gs3d_pipeline* p, uint32_t objects) {
+  if (objects <= p->object_cap) return GS3D_OK;
+  const uint32_t cap = std::max(objects, std::max(8u, p->object_cap * 2u));
+  for (uint32_t i = 0; i < kObjectRing; ++i) {
+    if (p->object_ev_used[i]) cudaEventSynchronize(p->object_ev[i]);
+    dfree(p->objects_dev[i]);
+    if (p->objects_pinned[i]) cudaFreeHost(p->objects_pinned[i]);
+    p->objects_pinned[i] = nullptr;
+    cudaError_t e = dalloc(p->objects_dev[i], (size_t)cap * 40);
+    if (e != cudaSuccess) return cuda_fail(p, e, "allocating object table");
+    e = cudaMallocHost((void**)&p->objects_pinned[i], (size_t)cap * 40 * sizeof(float));
+    if (e != cudaSuccess) return cuda_fail(p, e, "allocating pinned object table");
+  }
+  p->object_cap = cap;
+  return GS3D_OK;
+}
+
+uint32_t next_epoch(gs3d_pipeline* p, cudaStream_t st) {
+  p->epoch = (p->epoch + 1u) & kEpochMask;
+  if (p->epoch == 0) {
+    // Wrapped: clear the status words so no stale word can match.
+    cudaMemsetAsync(p->status, 0, p->status_words * sizeof(unsigned long long), st);
+    p->epoch = 1;
+  }
+  return p->epoch;
+}
+
+// Event marking the start of `stage` (stage == GS3D_STAGE_COUNT: end) of the
+// current profiled render.
+void mark(gs3d_pipeline* p, uint32_t stage, cudaStream_t st) {
+  if (!p->profiling) return;
+  const size_t idx = (size_t)p->profiled * kStageEvents + stage;
+  while (p->events.size() <= idx) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) return;
+    p->events.push_back(e);
+  }
+  cudaEventRecord(p->events[idx], st);
+}
+
+void release_all(gs3d_pipeline* p) {
+  for (cudaEvent_t e : p->events) cudaEventDestroy(e);
+  p->events.clear();
+  for (uint32_t i = 0; i < kObjectRing; ++i) {
+    if (p->object_ev_used[i]) cudaEventSynchronize(p->object_ev[i]);
+    if (p->object_ev[i]) cudaEventDestroy(p->object_ev[i]);
+    dfree(p->objects_dev[i]);
+    if (p->objects_pinned[i]) cudaFreeHost(p->objects_pinned[i]);
+  }
+  dfree(p->mean); dfree(p->conic); dfree(p->color); dfree(p->counts); dfree(p->keys); dfree(p->vis_off);
+  dfree(p->dk[0]); dfree(p->dk[1]); dfree(p->dv[0]); dfree(p->dv[1]); dfree(p->ordered); dfree(p->ioff);
+  dfree(p->tk[0]); dfree(p->tk[1]); dfree(p->tv[0]); dfree(p->tv[1]);
+  dfree(p->tile_offsets); dfree(p->ctl); dfree(p->output_state); dfree(p->status);
+}
+
+}  // namespace
+
+extern "C" {
+
+uint32_t gs3d_abi_version(void) { return GS3D_ABI_VERSION; }
+
+const char* gs3d_status_string(gs3d_status s) {
+  switch (s) {
+    case GS3D_OK: return "ok";
+    case GS3D_ERROR_INVALID_ARGUMENT: return "invalid argument";
+    case GS3D_ERROR_RANGE: return "out of range";
+    case GS3D_ERROR_NOT_PREPARED: return "pipeline must be prepared before rendering";
+    case GS3D_ERROR_OUT_OF_MEMORY: return "allocation failed";
+    case GS3D_ERROR_CUDA: return "CUDA error";
+    case GS3D_ERROR_DEVICE_TIMEOUT: return "device wait expired";
+    case GS3D_ERROR_UNSUPPORTED: return "unsupported option";
+  }
+  return "unknown status";
+}
+
+void gs3d_pipeline_desc_defaults(gs3d_pipeline_desc* d) {
+  if (!d) return;
+  memset(d, 0, sizeof(*d));
+  d->abi_version = GS3D_ABI_VERSION;
+  d->device = 0;
+  d->depth_sort_mode = GS3D_DEPTH_FLOAT32;
+  d->antialias_mode = GS3D_ANTIALIAS_COMPENSATED;
+  d->intersection_capacity = 262144;  // IntersectionCapacityPolicy.ts:71-74
+  d->max_rasterized_splats_per_tile = 0;
+  d->raster_chunk_size = 8192;        // constants.ts:3
+  d->subpixel_sample_culling = 1;
+  d->raster_transmittance_threshold = 1e-4f;
+  d->depth_alpha_threshold = 0.95f;
+  d->filter_variance = 0.3f;
+  d->invalid_depth_value = 1.0f;
+  d->boundary_policy = GS3D_BOUNDARY_CLIP;
+  d->raster_precision = GS3D_RASTER_FP32;
+  d->depth_encoding = 0;
+}
+
+gs3d_status gs3d_pipeline_create(const gs3d_pipeline_desc* desc, const gs3d_gaussian_data* data,
+                                 gs3d_pipeline** out) {
+  if (!desc || !out) return GS3D_ERROR_INVALID_ARGUMENT;
+  *out = nullptr;
+  gs3d_pipeline* p = new (std::nothrow) gs3d_pipeline();
+  if (!p) return GS3D_ERROR_OUT_OF_MEMORY;
+  gs3d_status s;
+  if ((s = validate_desc(p, *desc)) != GS3D_OK || (s = validate_data(p, data)) != GS3D_OK) {
+    delete p;
+    return s;
+  }
+  if (desc->raster_precision == GS3D_RASTER_HALF2) {
+    delete p;
+    return GS3D_ERROR_UNSUPPORTED;
+  }
+  p->desc = *desc;
+  p->data = *data;
+  p->device = desc->device;
+  cudaError_t e = cudaSetDevice(p->device);
+  if (e != cudaSuccess) {
+    delete p;
+    return GS3D_ERROR_CUDA;
+  }
+  cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, p->device);
+  for (uint32_t i = 0; i < kObjectRing; ++i) cudaEventCreateWithFlags(&p->object_ev[i], cudaEventDisableTiming);
+  if ((e = dalloc(p->ctl, 1)) || (e = dalloc(p->output_state, 4))) {
+    s = cuda_fail(p, e, "allocating control block");
+    release_all(p);
+    delete p;
+    return s;
+  }
+  cudaMemset(p->output_state, 0, 4 * sizeof(uint32_t));
+  cudaMemset(p->ctl, 0, sizeof(Control));
+  if ((s = ensure_slots(p, data->count)) != GS3D_OK || (s = ensure_capacity(p, desc->intersection_capacity)) != GS3D_OK ||
+      (s = ensure_objects(p, 8)) != GS3D_OK) {
+    release_all(p);
+    delete p;
+    return s;
+  }
+  *out = p;
+  return GS3D_OK;
+}
+
+void gs3d_pipeline_destroy(gs3d_pipeline* p) {
+  if (!p) return;
+  cudaSetDevice(p->device);
+  if (p->last_stream) cudaStreamSynchronize(p->last_stream);
+  release_all(p);
+  delete p;
+}
+
+gs3d_status gs3d_pipeline_update_data(gs3d_pipeline* p, const gs3d_gaussian_data* data) {
+  if (!p) return GS3D_ERROR_INVALID_ARGUMENT;
+  gs3d_status s = validate_data(p, data);
+  if (s != GS3D_OK) return s;
+  cudaSetDevice(p->device);
+  if (p->last_stream) cudaStreamSynchronize(p->last_stream);
+  if ((s = ensure_slots(p, data->count)) != GS3D_OK) return s;
+  p->data = *data;
+  return GS3D_OK;
+}
+
+gs3d_status gs3d_pipeline_resize_intersections(gs3d_pipeline* p, uint64_t capacity) {
+  if (!p) return GS3D_ERROR_INVALID_ARGUMENT;
+  if (capacity == 0 || capacity > 0x7fffffffull)
+    return fail(p, GS3D_ERROR_RANGE, "intersection capacity must be a positive integer below 2^31");
+  cudaSetDevice(p->device);
+  if (p->last_stream) cudaStreamSynchronize(p->last_stream);
+  return ensure_capacity(p, capacity);
+}
+
+gs3d_status gs3d_pipeline_prepare_frame(gs3d_pipeline* p, uint32_t width, uint32_t height) {
+  if (!p) return GS3D_ERROR_INVALID_ARGUMENT;
+  if (width == 0 || height == 0) return fail(p, GS3D_ERROR_RANGE, "render size must be positive");
+  const uint32_t tx = tiles_for(width), ty = tiles_for(height);
+  // TiledGaussianPipeline.ts:294-296
+  if (tx > 65535u || ty > 65535u) return fail(p, GS3D_ERROR_RANGE, "Render size exceeds WebGPU's tile dispatch limit");
+  cudaSetDevice(p->device);
+  const uint32_t ntile = tx * ty;
+  if (ntile + 1 > p->tile_cap) {
+    if (p->last_stream) cudaStreamSynchronize(p->last_stream);
+    // tile capacity grows to the next power of two (TiledGaussianPipeline.ts:306-318)
+    uint32_t cap = 1;
+    while (cap < ntile + 1) cap <<= 1;
+    cudaError_t e = dalloc(p->tile_offsets, cap);
+    if (e != cudaSuccess) return cuda_fail(p, e, "allocating tile offsets");
+    cudaMemset(p->tile_offsets, 0, (size_t)cap * sizeof(uint32_t));
+    p->tile_cap = cap;
+  }
+  p->width = width;
+  p->height = height;
+  p->tiles_x = tx;
+  p->tiles_y = ty;
+  p->prepared = true;
+  return GS3D_OK;
+}
+
+gs3d_status gs3d_pipeline_render(gs3d_pipeline* p, const gs3d_camera* cam, uint32_t attempt, int reset_valid,
+                                 const gs3d_targets* targets, void* stream) {
+  if (!p) return GS3D_ERROR_INVALID_ARGUMENT;
+  // TiledGaussianPipeline.ts:324-329
+  if (!p->prepared) return fail(p, GS3D_ERROR_NOT_PREPARED, "TiledGaussianPipeline must be prepared before rendering");
+  if (!cam || !targets || !targets->color) return fail(p, GS3D_ERROR_INVALID_ARGUMENT, "camera and color target required");
+  if (targets->color_format > 1) return fail(p, GS3D_ERROR_INVALID_ARGUMENT, "unknown color format");
+  if (cam->object_count > 0 && !cam->object_table) return fail(p, GS3D_ERROR_INVALID_ARGUMENT, "object table is null");
+  if (!(cam->depth_near >= 0.0f) || !(cam->depth_far > cam->depth_near))
+    return fail(p, GS3D_ERROR_RANGE, "depth range must satisfy 0 <= near < far");
+  cudaSetDevice(p->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  gs3d_status s = ensure_objects(p, std::max(1u, cam->object_count));
+  if (s != GS3D_OK) return s;
+  uint32_t launches = 0;
+
+  // Object table: pinned staging ring -> device (ObjectFrameState.update).
+  const uint32_t slot = p->frame_index++ % kObjectRing;
+  if (p->object_ev_used[slot]) cudaEventSynchronize(p->object_ev[slot]);
+  const size_t obj_bytes = (size_t)cam->object_count * 40 * sizeof(float);
+  if (obj_bytes) {
+    memcpy(p->objects_pinned[slot], cam->object_table, obj_bytes);
+    cudaMemcpyAsync(p->objects_dev[slot], p->objects_pinned[slot], obj_bytes, cudaMemcpyHostToDevice, st);
+  }
+
+  const gs3d_gaussian_data& d = p->data;
+  SceneView sv;
+  sv.means = (const float4*)d.means;
+  sv.shape = (const uint2*)d.scales_opacity;
+  sv.rot = (const uint32_t*)d.rotations;
+  sv.sh = (const uint32_t*)d.sh_coefficients;
+  sv.count = d.count;
+  sv.active = d.active_count;
+  sv.degree = d.sh_degree;
+  sv.C = (d.sh_degree + 1) * (d.sh_degree + 1);
+
+  FrameView f;
+  memcpy(f.P, cam->projection, sizeof(f.P));
+  f.vw = (float)p->width;
+  f.vh = (float)p->height;
+  f.vnear = cam->depth_near;
+  f.vfar = cam->depth_far;
+  f.filter = p->desc.filter_variance;
+  f.axis = p->desc.boundary_policy;
+  f.tiles_x = p->tiles_x;
+  f.tiles_y = p->tiles_y;
+  f.object_count = cam->object_count;
+  f.antialias = p->desc.antialias_mode;
+  f.subpixel = p->desc.subpixel_sample_culling ? 1u : 0u;
+  f.depth_mode = p->desc.depth_sort_mode;
+  f.objects = p->objects_dev[slot];
+  memcpy(f.background, p->desc.background, sizeof(f.background));
+  f.t_threshold = p->desc.raster_transmittance_threshold;
+  f.depth_alpha_threshold = p->desc.depth_alpha_threshold;
+  f.invalid_depth = p->desc.invalid_depth_value;
+  f.chunk = p->desc.raster_chunk_size;
+  f.max_per_tile = p->desc.max_rasterized_splats_per_tile;
+  f.depth_encoding = p->desc.depth_encoding;
+
+  const uint32_t N = d.active_count;
+  const uint32_t ntile = p->tiles_x * p->tiles_y;
+  Control* ctl = p->ctl;
+  cudaMemsetAsync(ctl, 0, sizeof(Control), st);
+
+  // K1: projection.
+  mark(p, GS3D_STAGE_PROJECT, st);
+  launch_project(sv, f, p->mean, p->conic, p->color, p->counts, p->keys, st);
+  launches += N ? 1 : 0;
+  // Visibility compaction.
+  mark(p, GS3D_STAGE_COMPACT, st);
+  const int depth_passes = p->desc.depth_sort_mode == GS3D_DEPTH_FLOAT32 ? 4 : 2;
+  launch_compact(p->keys, N, p->vis_off, p->dk[0], p->dv[0], ctl, p->status, next_epoch(p, st), depth_passes, st);
+  ++launches;
+  // Depth sort.
+  mark(p, GS3D_STAGE_DEPTH_SORT, st);
+  int cur = 0;
+  for (int pass = 0; pass < depth_passes; ++pass) {
+    launch_onesweep(8, p->dk[cur], p->dv[cur], p->dk[cur ^ 1], p->dv[cur ^ 1], &ctl->visible_state[0], N, 8 * pass,
+                    ctl->depth_hist[pass], p->status, &ctl->tickets[kTicketSortBase + pass], next_epoch(p, st),
+                    &ctl->error, st);
+    cur ^= 1;
+    ++launches;
+  }
+  p->depth_final = cur;
+  // Ordered counts + saturating scan + dispatch/output state.
+  mark(p, GS3D_STAGE_SCAN, st);
+  const uint32_t cap32 = (uint32_t)p->capacity;
+  launch_scan_counts(p->dv[cur], p->counts, N, p->ordered, p->ioff, ctl, p->status, next_epoch(p, st), cap32,
+                     attempt, reset_valid, p->output_state, st);
+  ++launches;
+  // Emission + tile-sort histograms.
+  mark(p, GS3D_STAGE_EMIT, st);
+  const uint32_t tile_bits = std::max(1u, ceil_log2((uint64_t)ntile + 1));
+  const int tile_passes = (int)((tile_bits + 7) / 8);
+  const int digit_bits = (int)((tile_bits + tile_passes - 1) / tile_passes);
+  launch_emit(p->dv[cur], N, p->mean, p->conic, p->ordered, p->ioff, f, ctl, cap32, p->tk[0], p->tv[0], tile_passes,
+              digit_bits, st);
+  launches += N ? 1 : 0;
+  // Tile sort.
+  mark(p, GS3D_STAGE_TILE_SORT, st);
+  int tcur = 0;
+  for (int pass = 0; pass < tile_passes; ++pass) {
+    launch_onesweep(digit_bits, p->tk[tcur], p->tv[tcur], p->tk[tcur ^ 1], p->tv[tcur ^ 1], &ctl->state[0], cap32,
+                    digit_bits * pass, ctl->tile_hist[pass], p->status,
+                    &ctl->tickets[kTicketSortBase + 4 + pass], next_epoch(p, st), &ctl->error, st);
+    tcur ^= 1;
+    ++launches;
+  }
+  p->tile_final = tcur;
+  // Tile ranges.
+  mark(p, GS3D_STAGE_RANGES, st);
+  launch_tile_ranges(p->tk[tcur], ctl, ntile, p->tile_offsets, p->sms, st);
+  ++launches;
+  // Raster.
+  mark(p, GS3D_STAGE_RASTER, st);
+  launch_raster((int)p->desc.raster_precision, p->tile_offsets, p->tv[tcur], p->mean, p->conic, p->color, f, ctl,
+                targets->color, targets->color_format == GS3D_COLOR_RGBA16F ? 1 : 0, targets->depth, st);
+  ++launches;
+
+  mark(p, GS3D_STAGE_COUNT, st);
+  if (p->profiling) ++p->profiled;
+  cudaEventRecord(p->object_ev[slot], st);
+  p->object_ev_used[slot] = true;
+  p->last_stream = st;
+  p->last_launches = launches;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(p, e, "launching the pass");
+  return GS3D_OK;
+}
+
+gs3d_status gs3d_pipeline_read_stats(gs3d_pipeline* p, gs3d_stats* out) {
+  if (!p || !out) return GS3D_ERROR_INVALID_ARGUMENT;
+  cudaSetDevice(p->device);
+  cudaError_t e = cudaStreamSynchronize(p->last_stream);
+  if (e != cudaSuccess) return cuda_fail(p, e, "synchronising the render stream");
+  Control c;
+  e = cudaMemcpy(&c, p->ctl, sizeof(Control), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(p, e, "reading the pass state");
+  memset(out, 0, sizeof(*out));
+  out->visible_gaussian_count = c.visible_state[0];
+  out->intersection_count = c.state[0];
+  out->requested_intersections = c.state[1];
+  out->overflow = c.state[3];
+  out->intersection_capacity = p->capacity;
+  out->device_error = c.error;
+  if (c.error) return fail(p, GS3D_ERROR_DEVICE_TIMEOUT, "a device-side look-back wait expired");
+  return GS3D_OK;
+}
+
+gs3d_status gs3d_pipeline_get_resources(gs3d_pipeline* p, gs3d_resources* r) {
+  if (!p || !r) return GS3D_ERROR_INVALID_ARGUMENT;
+  if (!p->prepared) return fail(p, GS3D_ERROR_NOT_PREPARED, "TiledGaussianPipeline must be prepared first");
+  memset(r, 0, sizeof(*r));
+  r->projected_mean = (const float*)p->mean;
+  r->projected_conic = (const float*)p->conic;
+  r->projected_color = (const float*)p->color;
+  r->tile_counts = p->counts;
+  r->visible_offsets = p->vis_off;
+  r->depth_sorted_keys = p->dk[p->depth_final];
+  r->depth_sorted_ids = p->dv[p->depth_final];
+  r->depth_ordered_tile_counts = p->ordered;
+  r->intersection_offsets = p->ioff;
+  r->dispatch_state = p->ctl->state;
+  r->visible_state = p->ctl->visible_state;
+  r->sorted_tile_ids = p->tk[p->tile_final];
+  r->sorted_gaussian_ids = p->tv[p->tile_final];
+  r->tile_offsets = p->tile_offsets;
+  r->output_state = p->output_state;
+  r->active_count = p->data.active_count;
+  r->tiles_x = p->tiles_x;
+  r->tiles_y = p->tiles_y;
+  r->intersection_capacity = p->capacity;
+  return GS3D_OK;
+}
+
+const char* gs3d_pipeline_last_error(gs3d_pipeline* p) { return p ? p->error.c_str() : ""; }
+
+uint32_t gs3d_pipeline_last_launch_count(gs3d_pipeline* p) { return p ? p->last_launches : 0u; }
+
+gs3d_status gs3d_pipeline_set_profiling(gs3d_pipeline* p, int enabled) {
+  if (!p) return GS3D_ERROR_INVALID_ARGUMENT;
+  p->profiling = enabled != 0;
+  return GS3D_OK;
+}
+
+gs3d_status gs3d_pipeline_stage_times(gs3d_pipeline* p, float* ms, uint32_t* renders) {
+  if (!p || !ms) return GS3D_ERROR_INVALID_ARGUMENT;
+  cudaSetDevice(p->device);
+  for (uint32_t s = 0; s < GS3D_STAGE_COUNT; ++s) ms[s] = 0.0f;
+  const uint32_t n = p->profiled;
+  for (uint32_t r = 0; r < n; ++r) {
+    cudaEvent_t* ev = p->events.data() + (size_t)r * kStageEvents;
+    cudaError_t e = cudaEventSynchronize(ev[GS3D_STAGE_COUNT]);
+    if (e != cudaSuccess) return cuda_fail(p, e, "waiting for profiled render");
+    for (uint32_t s = 0; s < GS3D_STAGE_COUNT; ++s) {
+      float t = 0.0f;
+      cudaEventElapsedTime(&t, ev[s], ev[s + 1]);
+      ms[s] += t;
+    }
+  }
+  if (n)
+    for (uint32_t s = 0; s < GS3D_STAGE_COUNT; ++s) ms[s] /= (float)n;
+  if (renders) *renders = n;
+  p->profiled = 0;
+  return GS3D_OK;
+}
+
+const char* gs3d_stage_name(uint32_t stage) {
+  static const char* names[GS3D_STAGE_COUNT] = {"project", "compact", "depth_sort", "scan",
+                                                "emit", "tile_sort", "ranges", "raster"};
+  return stage < GS3D_STAGE_COUNT ? names[stage] : "unknown";
+}
+
+uint64_t gs3d_capacity_next(uint64_t maximum, double growth, double headroom, uint64_t current, uint64_t demand) {
+  // IntersectionCapacityPolicy.ts:90-100
+  if (demand > maximum) return 0;
+  const double a = ceil((double)demand * headroom);
+  const double b = ceil((double)current * growth);
+  const double desired = a > b ? a : b;
+  const double rounded = ceil(desired / 256.0) * 256.0;
+  return (uint64_t)(rounded < (double)maximum ? rounded : (double)maximum);
+}
+
+}  // extern "C"

@@ -1,0 +1,238 @@
+/*
+ * gs3d — GB300-native tiled Gaussian-splatting pass, C ABI.
+ *
+ * This library replaces the data path behind the reference's
+ * TiledGaussianPipeline (src/renderer/pipeline/TiledGaussianPipeline.ts:39-484),
+ * whose only caller is GaussianPass.updateBefore
+ * (src/renderer/GaussianPass.ts:710-805). Every entry point below names the
+ * reference interface it stands in for. The ABI uses plain C types and
+ * pointers only: device buffers are CUDA device pointers, the stream is a
+ * cudaStream_t passed as void*.
+ *
+ * Threading: a pipeline is used by one host thread at a time; all work is
+ * enqueued asynchronously on the stream given to gs3d_pipeline_render and
+ * never blocks the caller, except gs3d_pipeline_read_stats (a small
+ * synchronous readback, the analogue of readStats()).
+ *
+ * Errors: every call returns a gs3d_status. No C++ exception crosses the ABI.
+ * gs3d_pipeline_last_error() returns a message for the last failure.
+ * Device-side conditions (intersection overflow, a bounded device wait that
+ * expired) are reported through the 16-byte output state and the stats.
+ */
+#ifndef GS3D_H
+#define GS3D_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GS3D_ABI_VERSION 1u
+
+typedef enum gs3d_status {
+  GS3D_OK = 0,
+  /* TypeError in the reference: wrong formats, null pointers, bad enums. */
+  GS3D_ERROR_INVALID_ARGUMENT = 1,
+  /* RangeError in the reference (e.g. TiledGaussianPipeline.ts:294-296). */
+  GS3D_ERROR_RANGE = 2,
+  /* Error("must be prepared before rendering"), TiledGaussianPipeline.ts:324-329. */
+  GS3D_ERROR_NOT_PREPARED = 3,
+  /* "allocation-failed" output status (types.ts:209-233). */
+  GS3D_ERROR_OUT_OF_MEMORY = 4,
+  /* Any other CUDA runtime failure. */
+  GS3D_ERROR_CUDA = 5,
+  /* A bounded device-side wait (scan/sort look-back) gave up; the frame is invalid. */
+  GS3D_ERROR_DEVICE_TIMEOUT = 6,
+  /* The build does not support the requested option. */
+  GS3D_ERROR_UNSUPPORTED = 7
+} gs3d_status;
+
+/* DepthSortMode (types.ts:11). */
+typedef enum gs3d_depth_sort_mode { GS3D_DEPTH_FLOAT32 = 0, GS3D_DEPTH_PACKED16 = 1 } gs3d_depth_sort_mode;
+/* AntialiasMode (types.ts:12). */
+typedef enum gs3d_antialias_mode { GS3D_ANTIALIAS_COMPENSATED = 0, GS3D_ANTIALIAS_CLASSIC = 1 } gs3d_antialias_mode;
+/* GaussianBoundaryPolicy (types.ts:17). */
+typedef enum gs3d_boundary_policy {
+  GS3D_BOUNDARY_CLIP = 0,
+  GS3D_BOUNDARY_REPEAT_X = 1,
+  GS3D_BOUNDARY_REPEAT_Y = 2
+} gs3d_boundary_policy;
+/* Rasterizer arithmetic. FP32 is the reference's form. EXACT is FP32 with the
+ * deterministic math library and no FMA contraction (bit-identical to the CPU
+ * restatement). HALF2 evaluates Gaussian weights two pixels per lane in packed
+ * half precision with FP32 transmittance and colour accumulation. */
+typedef enum gs3d_raster_precision {
+  GS3D_RASTER_FP32 = 0,
+  GS3D_RASTER_EXACT = 1,
+  GS3D_RASTER_HALF2 = 2
+} gs3d_raster_precision;
+/* Colour target format: the reference's rgba16float texture, or rgba32float. */
+typedef enum gs3d_color_format { GS3D_COLOR_RGBA16F = 0, GS3D_COLOR_RGBA32F = 1 } gs3d_color_format;
+
+/* GaussianData packed buffers (src/renderer/GaussianData.ts:10-33,108-138),
+ * compact geometry + rgb8e8 SH, as produced by the Rust backend's
+ * encode_attributes (rust/gaussian-backend/src/engine.rs:1801-1891).
+ * All pointers are device pointers owned by the caller (the Store); the
+ * pipeline holds them like the reference's lease (GaussianData.retain) until
+ * gs3d_pipeline_update_data or gs3d_pipeline_destroy. */
+typedef struct gs3d_gaussian_data {
+  uint32_t count;        /* slot capacity */
+  uint32_t active_count; /* ordinals drawn; <= count */
+  uint32_t sh_degree;    /* 0..3 */
+  uint32_t reserved;
+  const void* means;           /* float32[count][4]: xyz, objectId or -1 */
+  const void* scales_opacity;  /* uint32[count][2]: f16 ln-scales + f16 opacity */
+  const void* rotations;       /* uint32[count]: oct101012 */
+  const void* sh_coefficients; /* uint32[count * (deg+1)^2 + count]: rgb8e8 + active-slot tail */
+} gs3d_gaussian_data;
+
+/* Constructor options of TiledGaussianPipeline (TiledGaussianPipeline.ts:65-85)
+ * and the GaussianRenderDomain (types.ts:20-25). Zero-initialise, then call
+ * gs3d_pipeline_desc_defaults() to get the reference's defaults. */
+typedef struct gs3d_pipeline_desc {
+  uint32_t abi_version;           /* GS3D_ABI_VERSION */
+  int32_t device;                 /* CUDA device ordinal */
+  uint32_t depth_sort_mode;       /* gs3d_depth_sort_mode, default float32 */
+  uint32_t antialias_mode;        /* gs3d_antialias_mode, default compensated */
+  uint64_t intersection_capacity; /* records; default 262,144 */
+  float background[4];            /* default transparent black */
+  uint32_t max_rasterized_splats_per_tile; /* 0 = null (uncapped) */
+  uint32_t raster_chunk_size;     /* default 8192; 0 = null (single-block tiles) */
+  uint32_t subpixel_sample_culling; /* default 1 */
+  float raster_transmittance_threshold; /* default 1e-4, in (0,1) */
+  float depth_alpha_threshold;    /* default 0.95, in [0,1] */
+  float filter_variance;          /* default 0.3 */
+  float invalid_depth_value;      /* default 1 */
+  uint32_t boundary_policy;       /* gs3d_boundary_policy, default clip */
+  uint32_t raster_precision;      /* gs3d_raster_precision, default FP32 */
+  uint32_t depth_encoding;        /* 0: default device depth node; 1: raw alpha-weighted depth */
+} gs3d_pipeline_desc;
+
+/* Per-frame camera state: what FrameUniforms.update and ObjectFrameState.update
+ * produce on the CPU (FrameUniforms.ts:41-58, ObjectFrameState.ts:78-119). */
+typedef struct gs3d_camera {
+  float projection[16];   /* column-major projectionMatrix */
+  float view[16];         /* column-major matrixWorldInverse */
+  float depth_near;       /* depthRange (defaults to camera near/far) */
+  float depth_far;
+  const float* object_table; /* HOST pointer: object_count x 40 floats */
+  uint32_t object_count;
+  uint32_t reserved;
+} gs3d_camera;
+
+/* Render targets: device pointers, row-major width x height pixels. */
+typedef struct gs3d_targets {
+  void* color;          /* rgba16f (uint16 x4) or rgba32f (float x4) */
+  uint32_t color_format; /* gs3d_color_format */
+  uint32_t reserved;
+  float* depth;         /* float32 per pixel, or NULL (outputDepth = false) */
+} gs3d_targets;
+
+/* readStats() (IntersectionStage.ts:197-213, types.ts:94-103). */
+typedef struct gs3d_stats {
+  uint32_t visible_gaussian_count;
+  uint32_t intersection_count;
+  uint32_t requested_intersections; /* saturates at 0xffffffff */
+  uint32_t overflow;
+  uint64_t intersection_capacity;
+  uint32_t device_error;            /* nonzero: a bounded device wait expired */
+  uint32_t reserved;
+} gs3d_stats;
+
+/* getResources() (TiledGaussianPipeline.ts:391-406, types.ts:174-193).
+ * Device pointers into the pipeline's workspaces, valid until the next
+ * resize/update/destroy. Record buffers are structure-of-arrays here: the
+ * reference's uvec2 (key, id) records are split into key and id arrays. */
+typedef struct gs3d_resources {
+  const float* projected_mean;     /* float4 per active ordinal: x, y, depth, opacity */
+  const float* projected_conic;    /* float4: conic xyz, radiusX + 512 radiusY */
+  const float* projected_color;    /* float4: rgb, bitcast(slot ^ 0x3f800000) */
+  const uint32_t* tile_counts;
+  const uint32_t* visible_offsets;
+  const uint32_t* depth_sorted_keys; /* depth key per visible rank */
+  const uint32_t* depth_sorted_ids;  /* active ordinal per visible rank */
+  const uint32_t* depth_ordered_tile_counts;
+  const uint32_t* intersection_offsets;
+  const uint32_t* dispatch_state;    /* uvec4: count, total, radix blocks, overflow */
+  const uint32_t* visible_state;     /* uvec4: visible, visible, radix blocks, 0 */
+  const uint32_t* sorted_tile_ids;   /* tile id per sorted intersection */
+  const uint32_t* sorted_gaussian_ids; /* active ordinal per sorted intersection */
+  const uint32_t* tile_offsets;      /* tilesX*tilesY + 1 */
+  const uint32_t* output_state;      /* uvec4: attempt, version, demand, overflow */
+  uint32_t active_count;
+  uint32_t tiles_x;
+  uint32_t tiles_y;
+  uint32_t reserved;
+  uint64_t intersection_capacity;
+} gs3d_resources;
+
+typedef struct gs3d_pipeline gs3d_pipeline;
+
+/* Library identity. */
+uint32_t gs3d_abi_version(void);
+const char* gs3d_status_string(gs3d_status status);
+
+/* Fill *desc with the reference defaults (GaussianPass.ts:170-256). */
+void gs3d_pipeline_desc_defaults(gs3d_pipeline_desc* desc);
+
+/* new TiledGaussianPipeline(...) (TiledGaussianPipeline.ts:65-163). */
+gs3d_status gs3d_pipeline_create(const gs3d_pipeline_desc* desc, const gs3d_gaussian_data* data,
+                                 gs3d_pipeline** out);
+/* dispose() (TiledGaussianPipeline.ts:408-425). Safe on NULL. */
+void gs3d_pipeline_destroy(gs3d_pipeline* pipeline);
+
+/* updateData(data) (TiledGaussianPipeline.ts:203-218). */
+gs3d_status gs3d_pipeline_update_data(gs3d_pipeline* pipeline, const gs3d_gaussian_data* data);
+/* resizeIntersections(capacity) (TiledGaussianPipeline.ts:220-231). */
+gs3d_status gs3d_pipeline_resize_intersections(gs3d_pipeline* pipeline, uint64_t capacity);
+/* prepareFrame(width, height) (TiledGaussianPipeline.ts:286-322): RANGE if a
+ * tile axis exceeds 65,535. Camera state comes with each render call. */
+gs3d_status gs3d_pipeline_prepare_frame(gs3d_pipeline* pipeline, uint32_t width, uint32_t height);
+/* render(attempt, resetValid) (TiledGaussianPipeline.ts:324-341): enqueue the
+ * whole pass on `stream`. NOT_PREPARED before prepare_frame. */
+gs3d_status gs3d_pipeline_render(gs3d_pipeline* pipeline, const gs3d_camera* camera, uint32_t attempt,
+                                 int reset_valid, const gs3d_targets* targets, void* stream);
+/* readStats() (TiledGaussianPipeline.ts:353-366): synchronises the stream of
+ * the last render. */
+gs3d_status gs3d_pipeline_read_stats(gs3d_pipeline* pipeline, gs3d_stats* stats);
+/* getResources() (TiledGaussianPipeline.ts:391-406). */
+gs3d_status gs3d_pipeline_get_resources(gs3d_pipeline* pipeline, gs3d_resources* resources);
+/* Message of the last failed call on this pipeline ("" if none). */
+const char* gs3d_pipeline_last_error(gs3d_pipeline* pipeline);
+/* Kernel launches enqueued by the last render call. */
+uint32_t gs3d_pipeline_last_launch_count(gs3d_pipeline* pipeline);
+
+/* Kernel timing, the analogue of the reference's profileKernels option
+ * (GaussianPass.ts:280-281; sandbox KernelTimingInspector). While enabled,
+ * every render records CUDA events between its stages. */
+typedef enum gs3d_stage {
+  GS3D_STAGE_PROJECT = 0,     /* decode + project + cull + SH + tile count */
+  GS3D_STAGE_COMPACT = 1,     /* visibility scan + compaction */
+  GS3D_STAGE_DEPTH_SORT = 2,  /* radix sort of (depth key, ordinal) */
+  GS3D_STAGE_SCAN = 3,        /* depth-ordered counts + intersection scan */
+  GS3D_STAGE_EMIT = 4,        /* intersection emission */
+  GS3D_STAGE_TILE_SORT = 5,   /* radix sort of (tile, ordinal) */
+  GS3D_STAGE_RANGES = 6,      /* tile ranges */
+  GS3D_STAGE_RASTER = 7,      /* tile rasterizer */
+  GS3D_STAGE_COUNT = 8
+} gs3d_stage;
+gs3d_status gs3d_pipeline_set_profiling(gs3d_pipeline* pipeline, int enabled);
+/* Mean stage durations in milliseconds over the renders profiled since the
+ * last call (ms must hold GS3D_STAGE_COUNT floats); *renders receives how
+ * many renders were averaged. Synchronises those renders' events. */
+gs3d_status gs3d_pipeline_stage_times(gs3d_pipeline* pipeline, float* ms, uint32_t* renders);
+const char* gs3d_stage_name(uint32_t stage);
+
+/* IntersectionCapacityPolicy.next(current, demand)
+ * (src/renderer/pipeline/IntersectionCapacityPolicy.ts:90-100): the capacity
+ * to grow to, or 0 for null (demand above maximum). */
+uint64_t gs3d_capacity_next(uint64_t maximum, double growth, double headroom, uint64_t current,
+                            uint64_t demand);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GS3D_H */

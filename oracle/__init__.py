@@ -238,21 +238,27 @@ def render(scene: dict, frame: dict, precision: int = 0, output_depth: bool = Tr
 
 
 def _estimate_records(L, sc, fr, n) -> int:
-    """Total intersections of this frame (a projection-only oracle pass)."""
+    """Total intersections of this frame (a counting pass).
+
+    Capacity 0 makes any non-empty frame overflow, which skips emission and
+    raster; an empty frame still rasterizes (background only), so every
+    buffer here is sized for the full frame and kept alive for the call."""
     probe = GsoFrame.from_buffer_copy(fr)
-    probe.capacity = 0  # forces overflow: no emission, no raster
+    probe.capacity = 0
     W, H = int(fr.viewport[0]), int(fr.viewport[1])
     tiles = ((W + 15) // 16) * ((H + 15) // 16)
-    bufs = {k: np.zeros(max(n, 1) * 4, np.float32) for k in ("m", "c", "col")}
-    u = {k: np.zeros(max(n, 1), np.uint32) for k in ("tc", "vo", "oc", "io")}
-    ds = np.zeros(max(n, 1) * 2, np.uint32)
-    to = np.zeros(tiles + 1, np.uint32)
-    rg = np.zeros(4, np.float32)
+    m = max(n, 1)
+    keep = {
+        "m": np.zeros(m * 4, np.float32), "c": np.zeros(m * 4, np.float32), "col": np.zeros(m * 4, np.float32),
+        "tc": np.zeros(m, np.uint32), "vo": np.zeros(m, np.uint32), "oc": np.zeros(m, np.uint32),
+        "io": np.zeros(m, np.uint32), "ds": np.zeros(m * 2, np.uint32), "to": np.zeros(tiles + 1, np.uint32),
+        "rg": np.zeros(W * H * 4, np.float32), "sr": np.zeros(2, np.uint32),
+    }
     out = GsoOutputs()
-    out.proj_mean, out.proj_conic, out.proj_color = (_ptr(bufs["m"]), _ptr(bufs["c"]), _ptr(bufs["col"]))
-    out.tile_counts, out.visible_offsets = _ptr(u["tc"]), _ptr(u["vo"])
-    out.ordered_counts, out.intersection_offsets = _ptr(u["oc"]), _ptr(u["io"])
-    out.depth_sorted, out.tile_offsets, out.rgba, out.depth = _ptr(ds), _ptr(to), _ptr(rg), 0
-    out.sorted_records = _ptr(np.zeros(2, np.uint32))
+    out.proj_mean, out.proj_conic, out.proj_color = _ptr(keep["m"]), _ptr(keep["c"]), _ptr(keep["col"])
+    out.tile_counts, out.visible_offsets = _ptr(keep["tc"]), _ptr(keep["vo"])
+    out.ordered_counts, out.intersection_offsets = _ptr(keep["oc"]), _ptr(keep["io"])
+    out.depth_sorted, out.tile_offsets, out.rgba, out.depth = _ptr(keep["ds"]), _ptr(keep["to"]), _ptr(keep["rg"]), 0
+    out.sorted_records = _ptr(keep["sr"])
     L.gso_render(C.byref(sc), C.byref(probe), C.byref(out), 0)
     return int(out.state[1])

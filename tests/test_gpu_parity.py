@@ -1,0 +1,194 @@
+"""CUDA pass vs the CPU oracle on identical packed inputs, through the C ABI.
+
+Integer stages (tile counts, visible offsets, depth keys and stable order,
+intersection offsets, sorted (tile, ordinal) records, tile ranges, dispatch
+and output state) are bit-exact. The EXACT raster form is bit-exact too; the
+FP32 raster form (hardware exp/log, fused multiply-add) is held to
+max |err| <= 4e-3 against the oracle's FP32 image and >= 50 dB PSNR against
+the FP64 twin.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import scenes
+from gpu_harness import GpuRun, assert_bit_exact, psnr
+
+pytestmark = pytest.mark.gpu
+
+sc = scenes()
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "small_scene.npz")
+FP32_MAX_ABS = 4e-3
+MIN_PSNR_DB = 50.0
+
+
+def small_cases():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(os.path.dirname(__file__), "golden",
+                                                                              "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    return mg.small_scene_cases()
+
+
+def cube(n=6000, seed=11, **kw):
+    return sc.uniform_cloud(n, seed=seed, log_scale=kw.pop("log_scale", (-2.4, 0.6)), **kw)
+
+
+def cam(eye=(0.5, 1.0, 11.0), target=(0, 0, 0), w=200, h=120, **opts):
+    return sc.make_frame(sc.look_at(eye, target), w, h, 55.0, 0.1, 100.0, **opts)
+
+
+CASES = {
+    "default": lambda: (cube(), cam()),
+    "packed16": lambda: (cube(seed=12), cam(depth_sort_mode=1)),
+    "classic": lambda: (cube(seed=13), cam(antialias=1)),
+    "no_subpixel_cull": lambda: (cube(seed=14, log_scale=(-4.5, 0.5)), cam(subpixel_culling=0)),
+    "repeat_x": lambda: (cube(seed=15), cam(w=97, h=64, boundary_axis=1)),
+    "repeat_y": lambda: (cube(seed=16), cam(w=80, h=61, boundary_axis=2)),
+    "chunked": lambda: (cube(8000, seed=17, log_scale=(-1.6, 0.4), opacity_logit=(-2.0, 0.5)),
+                        cam(w=64, h=48, raster_chunk_size=256)),
+    "capped": lambda: (cube(8000, seed=18, log_scale=(-1.8, 0.4)), cam(w=96, h=64, max_splats_per_tile=100)),
+    "background_depth_raw": lambda: (cube(seed=19), cam(background=(0.1, 0.2, 0.3, 0.6), depth_encoding=1,
+                                                        depth_alpha_threshold=0.3)),
+    "odd_size": lambda: (cube(seed=20), cam(w=33, h=17)),
+    "degree1": lambda: (sc.uniform_cloud(3000, seed=21, degree=1, log_scale=(-2.4, 0.6)), cam()),
+    "degree0": lambda: (sc.uniform_cloud(3000, seed=22, degree=0, log_scale=(-2.4, 0.6)), cam()),
+    "degree2": lambda: (sc.uniform_cloud(3000, seed=23, degree=2, log_scale=(-2.4, 0.6)), cam()),
+    "behind_camera": lambda: (cube(seed=24), cam(eye=(0, 0, 2.0), target=(0, 0, 10.0))),
+}
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_bit_exact_against_oracle(name):
+    scene, frame = CASES[name]()
+    o = oracle.render(scene, frame, 0)
+    run = GpuRun(scene, frame, "exact", capacity=max(int(o["state"][1]), 1))
+    g = run.render(frame)
+    run.close()
+    assert int(o["state"][1]) > 0 or name == "behind_camera"
+    assert_bit_exact(g, o)
+
+
+def test_golden_fixture_vectors():
+    scene, frames = small_cases()
+    gold = np.load(GOLDEN)
+    for name, frame in frames.items():
+        run = GpuRun(scene, frame, "exact")
+        g = run.render(frame)
+        run.close()
+        for key in ("tile_counts", "visible_offsets", "depth_sorted", "intersection_offsets", "sorted_records",
+                    "tile_offsets", "state", "visible_state"):
+            assert np.array_equal(g[key], gold[f"{name}_{key}"]), (name, key)
+        assert np.array_equal(g["rgba"].astype(np.float16), gold[f"{name}_rgba"])
+
+
+@pytest.mark.parametrize("name", ["default", "chunked", "repeat_x", "background_depth_raw"])
+def test_fp32_raster_tolerance(name):
+    scene, frame = CASES[name]()
+    o = oracle.render(scene, frame, 0)
+    o64 = oracle.render(scene, frame, 1)
+    run = GpuRun(scene, frame, "fp32", capacity=max(int(o["state"][1]), 1))
+    g = run.render(frame)
+    run.close()
+    assert_bit_exact(g, o, image=False)
+    assert np.abs(g["rgba"] - o["rgba"]).max() <= FP32_MAX_ABS
+    assert psnr(g["rgba"][..., :3], o64["rgba"][..., :3]) >= MIN_PSNR_DB
+
+
+def test_rgba16f_target_is_the_rounded_fp32_image():
+    scene, frame = CASES["default"]()
+    run = GpuRun(scene, frame, "exact")
+    g32 = run.render(frame, "rgba32f")
+    g16 = run.render(frame, "rgba16f")
+    run.close()
+    assert np.array_equal(g32["rgba"].astype(np.float16), g16["rgba"].astype(np.float16))
+
+
+def test_repeated_renders_are_identical_and_versioned():
+    scene, frame = CASES["default"]()
+    run = GpuRun(scene, frame, "fp32")
+    a = run.render(frame, attempt=1)
+    b = run.render(frame, attempt=2)
+    run.close()
+    for key in ("sorted_records", "tile_offsets", "depth_sorted", "intersection_offsets"):
+        assert np.array_equal(a[key], b[key])
+    assert np.array_equal(a["rgba"], b["rgba"])
+    assert list(b["output_state"])[:2] == [2, 2]
+
+
+def test_overflow_keeps_previous_image_and_reports_demand():
+    scene, frame = CASES["default"]()
+    o = oracle.render(scene, frame, 0)
+    total = int(o["state"][1])
+    run = GpuRun(scene, frame, "exact", capacity=total - 1)
+    g = run.render(frame, attempt=5, color_init=0.25)
+    assert g["stats"]["overflow"] and g["stats"]["requestedIntersections"] == total
+    assert np.all(g["rgba"] == 0.25)
+    assert list(g["output_state"]) == [5, 0, total, 1]
+    # grow (the host capacity policy) and render again: complete, version = attempt
+    run.pipe.resize_intersections(total)
+    g2 = run.render(frame, attempt=6)
+    run.close()
+    assert list(g2["output_state"]) == [6, 6, total, 0]
+    assert_bit_exact(g2, oracle.render(scene, dict(frame, attempt=6), 0))
+
+
+def test_empty_active_list():
+    scene, frame = CASES["default"]()
+    scene = dict(scene, active_count=0)
+    o = oracle.render(scene, frame, 0)
+    run = GpuRun(scene, frame, "exact")
+    g = run.render(frame)
+    run.close()
+    assert int(g["visible_state"][0]) == 0 and int(g["state"][0]) == 0
+    assert np.all(g["tile_offsets"] == 0)
+    assert np.array_equal(g["rgba"], o["rgba"])
+
+
+def test_prepare_and_option_errors():
+    scene, frame = CASES["default"]()
+    run = GpuRun(scene, frame, "exact")
+    import importlib
+    P = importlib.import_module("3dgs_tile_webgpu_gb300")
+    with pytest.raises(ValueError):
+        run.pipe.prepare_frame(16 * 65536, 16)  # TiledGaussianPipeline.ts:294-296
+    fresh = P.TiledGaussianPipeline(run.ds.data(), {"intersection_capacity": 1024})
+    with pytest.raises(P.GaussianPassError):
+        fresh.render(P.make_camera(frame), 0x1000)  # render before prepareFrame
+    fresh.dispose()
+    run.close()
+
+
+def test_config1_full_size_bit_exact():
+    # 100k Gaussians, 1280x720, camera at (0,0,15), 60 deg (benchmark configuration 1)
+    scene = sc.config1_scene()
+    frame = sc.config1_frame()
+    o = oracle.render(scene, frame, 0)
+    run = GpuRun(scene, frame, "exact", capacity=max(int(o["state"][1]), 1))
+    g = run.render(frame)
+    run.close()
+    assert_bit_exact(g, o)
+
+
+def test_clustered_properties_at_scale():
+    # 1M clustered Gaussians at 1920x1080: size-independent invariants.
+    scene = sc.clustered_cloud(1_000_000, seed=1002)
+    frame = sc.config2_frames(1)[0]
+    run = GpuRun(scene, frame, "fp32", capacity=1 << 25)
+    g = run.render(frame)
+    run.close()
+    recs = g["sorted_records"]
+    assert recs.shape[0] == int(g["tile_counts"].sum()) == int(g["state"][1]) > 0
+    keys = g["proj_mean"][:, 2].view(np.uint32)
+    order = np.lexsort((recs[:, 1], keys[recs[:, 1]], recs[:, 0]))
+    assert np.array_equal(order, np.arange(recs.shape[0]))
+    assert np.array_equal(np.bincount(recs[:, 1], minlength=g["tile_counts"].size), g["tile_counts"])
+    ntile = g["tile_offsets"].size - 1
+    assert np.array_equal(g["tile_offsets"], np.searchsorted(recs[:, 0], np.arange(ntile + 1)))
+    ds = g["depth_sorted"]
+    assert np.all(np.diff(ds[:, 0].astype(np.int64)) >= 0)
+    vis = np.nonzero(g["tile_counts"])[0]
+    assert np.array_equal(np.sort(ds[:, 1]), vis)
