@@ -41,6 +41,9 @@ __global__ void __launch_bounds__(kBlock) k_project(SceneView s, FrameView f, fl
                                                     float4* __restrict__ conic_out, float4* __restrict__ color_out,
                                                     uint32_t* __restrict__ count_out, uint32_t* __restrict__ key_out) {
   constexpr int C = (DEG + 1) * (DEG + 1);
+  __shared__ float s_snorm[256];
+  s_snorm[threadIdx.x] = snorm8_value(threadIdx.x);
+  __syncthreads();
   const uint32_t gid = blockIdx.x * kBlock + threadIdx.x;
   if (gid >= s.active) return;
   float4 mo4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -108,7 +111,7 @@ __global__ void __launch_bounds__(kBlock) k_project(SceneView s, FrameView f, fl
     if (cnt == 0) break;
     uint32_t co[C];
     load_sh<DEG>(s.sh + (size_t)slot * C, co);
-    const f3 col = eval_sh<DEG>(co, vdir);
+    const f3 col = eval_sh<DEG>(co, vdir, s_snorm);
     mo4 = make_float4(pr.cx, pr.cy, pr.depth, op);
     conic_out[gid] = make_float4(pr.conic_x, pr.conic_y, pr.conic_z, rx + ry * 512.0f);
     color_out[gid] = make_float4(col.x, col.y, col.z, __uint_as_float(slot ^ kActiveTag));

@@ -2,18 +2,25 @@
 // storeFinalPixel :930-964, finalizeGaussianDepth.ts:18-68, chunk split
 // rasterChunks.ts:3-99 and composite TileRasterizer.ts:807-902).
 //
-// One 256-thread block per 16x16 tile, one pixel per thread (lane -> pixel in
-// the reference's compact Morton order, rasterHelpers.ts:3-12, so a warp
-// covers an 8x4 patch). Each batch of 256 sorted records is gathered into
-// shared memory once and read by every pixel; the block leaves the tile as
-// soon as no pixel is still accumulating (__syncthreads_or).
+// One 256-thread block per 16x16 tile, one pixel per thread, lanes mapped to
+// pixels in the reference's compact Morton order (rasterHelpers.ts:3-12), so
+// warp w owns an 8x4 patch of the tile. Each batch of 256 sorted records is
+// gathered into shared memory once. While staging, the thread that loads a
+// record also tests the splat's support box against the eight warp patches
+// and stores an 8-bit mask; each warp then walks only the records whose bit
+// is set (ballot + find-first-set, ascending, so front-to-back order holds).
+// The culling is conservative: a skipped (pixel, splat) pair is one where the
+// per-pixel test `power < -threshold` would reject the splat anyway, so the
+// result is unchanged, bit for bit. The block leaves the tile when no pixel
+// is still accumulating (__syncthreads_or), a warp leaves a batch when all
+// its pixels are done (__all_sync).
 //
 // Tiles holding more than `chunk` samples are evaluated as the reference's
 // exact chunks: every chunk starts at transmittance 1 and its partial
-// (colour, transmittance, depth) is composited in order. The block runs the
-// chunks of its tile one after another and stops compositing once the
-// composite transmittance falls below the threshold, which yields exactly the
-// composite the reference's parallel chunk tasks produce.
+// (colour, transmittance, depth) is composited in order; the block runs the
+// chunks of its tile one after another and stops once the composite
+// transmittance falls below the threshold, which yields exactly the composite
+// of the reference's parallel chunk tasks.
 //
 // The MATH policy supplies exp/log: deterministic (bit-identical to the CPU
 // restatement when the translation unit is built with --fmad=false) or the
@@ -50,23 +57,29 @@ __device__ __forceinline__ float rclamp(float x, float lo, float hi) {
   return y > hi ? hi : y;
 }
 
+// Frame values the rasterizer reads per sample, held in registers.
+struct RasterFrame {
+  float vw, vh, t_threshold;
+  uint32_t axis;
+};
+
 // tileContribution.ts:66-82 gaussian_boundary_delta.
-__device__ __forceinline__ void boundary_delta(float pxc, float pyc, float4 m, float4 c, const FrameView& f,
-                                               float* dx, float* dy) {
+__device__ __forceinline__ void boundary_delta(float pxc, float pyc, float cx, float cy, float ca, float cb,
+                                               float cc, const RasterFrame& f, float* dx, float* dy) {
   if (f.axis == 0u) {
-    *dx = pxc - m.x;
-    *dy = pyc - m.y;
+    *dx = pxc - cx;
+    *dy = pyc - cy;
     return;
   }
-  float ccx = m.x, ccy = m.y;
-  if (f.axis == 1u) ccx = ccx - floorf(m.x / f.vw) * f.vw;
-  if (f.axis == 2u) ccy = ccy - floorf(m.y / f.vh) * f.vh;
+  float ccx = cx, ccy = cy;
+  if (f.axis == 1u) ccx = ccx - floorf(cx / f.vw) * f.vw;
+  if (f.axis == 2u) ccy = ccy - floorf(cy / f.vh) * f.vh;
   float ddx = pxc - ccx, ddy = pyc - ccy;
   if (f.axis == 1u) {
-    float opt = (-c.y * ddy) / c.x;
+    float opt = (-cb * ddy) / ca;
     ddx = ddx - floorf((ddx - opt) / f.vw + 0.5f) * f.vw;
   } else {
-    float opt = (-c.y * ddx) / c.z;
+    float opt = (-cb * ddx) / cc;
     ddy = ddy - floorf((ddy - opt) / f.vh + 0.5f) * f.vh;
   }
   *dx = ddx;
@@ -77,52 +90,98 @@ struct PixelAcc {
   float r, g, b, t, d;
 };
 
+// Shared batch: geometry (cx, cy, opacity, threshold), conic (a, b, c, depth),
+// colour, and the warp-patch mask.
+struct Batch {
+  float4 geo[kBlock];
+  float4 con[kBlock];
+  float4 col[kBlock];
+  uint8_t mask[kBlock];
+};
+
+// Which of the tile's eight 8x4 warp patches can hold a pixel centre inside
+// the splat's support {q(d) <= 2 threshold}. Conservative: the support's
+// bounding box is widened by 5 % + 0.25 px, far beyond the rounding of the
+// per-pixel evaluation for conics whose condition number is below 4e4 (the
+// 0.3 px^2 filter bounds it near 3.3e4); worse-conditioned splats, periodic
+// boundaries and non-finite values keep every bit set.
+__device__ __forceinline__ uint32_t patch_mask(float cx, float cy, float ca, float cb, float cc, float thr,
+                                               float tile_x0, float tile_y0, uint32_t axis) {
+  if (axis != 0u) return 0xffu;
+  const float det = ca * cc - cb * cb;
+  const float tr = ca + cc;
+  if (!(det > 0.0f) || !(tr * tr <= 4e4f * det) || !(thr >= 0.0f)) return 0xffu;
+  const float q = 2.0f * thr;
+  const float hx = sqrtf(q * cc / det) * 1.05f + 0.25f;
+  const float hy = sqrtf(q * ca / det) * 1.05f + 0.25f;
+  if (!(hx < 1e30f) || !(hy < 1e30f)) return 0xffu;
+  uint32_t m = 0;
+#pragma unroll
+  for (uint32_t w = 0; w < 8; ++w) {
+    const float x0 = tile_x0 + (float)(8u * ((w >> 1) & 1u)) + 0.5f;
+    const float y0 = tile_y0 + (float)(4u * ((w & 1u) | (((w >> 2) & 1u) << 1))) + 0.5f;
+    const bool hit = cx + hx >= x0 && cx - hx <= x0 + 7.0f && cy + hy >= y0 && cy - hy <= y0 + 3.0f;
+    m |= hit ? (1u << w) : 0u;
+  }
+  return m;
+}
+
+// One (pixel, splat) step of the front-to-back blend (TileRasterizer.ts:616-707).
+template <class M>
+__device__ __forceinline__ bool blend_one(const Batch& sb, uint32_t j, float pxc, float pyc, const RasterFrame& f,
+                                          PixelAcc& a) {
+  const float4 g = sb.geo[j];
+  const float4 c = sb.con[j];
+  float dx, dy;
+  boundary_delta(pxc, pyc, g.x, g.y, c.x, c.y, c.z, f, &dx, &dy);
+  const float power = ((c.x * (dx * dx) + ((c.y * 2.0f) * dx) * dy) + c.z * (dy * dy)) * -0.5f;
+  if (power > 0.0f || power < -g.w) return false;
+  const float alpha = rclamp(g.z * M::exp(power), 0.0f, 0.99f);
+  if (alpha < (float)(1.0 / 255.0)) return false;
+  const float4 col = sb.col[j];
+  const float contrib = a.t * alpha;
+  a.r = a.r + col.x * contrib;
+  a.g = a.g + col.y * contrib;
+  a.b = a.b + col.z * contrib;
+  a.d = a.d + c.w * contrib;
+  a.t = a.t * (1.0f - alpha);
+  return a.t < f.t_threshold;
+}
+
 // Blend samples [s0, s1) of the tile into `a` (block-cooperative; every thread
 // of the block must call it). `done` marks pixels that take no more samples.
 template <class M>
 __device__ __forceinline__ void blend_range(uint32_t begin, uint32_t source_count, uint32_t raster_count,
                                             uint32_t s0, uint32_t s1, bool capped, const uint32_t* __restrict__ ids,
                                             const float4* __restrict__ mean, const float4* __restrict__ conic,
-                                            const float4* __restrict__ color, const FrameView& f, float pxc,
-                                            float pyc, bool done, PixelAcc& a, float4* s_mean, float4* s_conic,
-                                            float4* s_color) {
-  const uint32_t t = threadIdx.x;
+                                            const float4* __restrict__ color, const RasterFrame& f, float tile_x0,
+                                            float tile_y0, float pxc, float pyc, bool done, PixelAcc& a, Batch& sb) {
+  const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
   for (uint32_t b = s0; b < s1; b += kBlock) {
     if (!__syncthreads_or(!done)) break;
-    uint32_t i = b + t;
+    const uint32_t i = b + t;
     if (i < s1) {
       uint32_t src = i;
       if (capped) src = (uint32_t)floorf((((float)i + 0.5f) * (float)source_count) / (float)raster_count);
-      uint32_t g = __ldg(ids + begin + src);
-      float4 m = __ldg(mean + g);
-      float4 c = __ldg(conic + g);
-      s_mean[t] = m;
-      s_conic[t] = make_float4(c.x, c.y, c.z, M::log(m.w * 255.0f));
-      s_color[t] = __ldg(color + g);
+      const uint32_t g = __ldg(ids + begin + src);
+      const float4 m = __ldg(mean + g);
+      const float4 c = __ldg(conic + g);
+      const float thr = M::log(m.w * 255.0f);
+      sb.geo[t] = make_float4(m.x, m.y, m.w, thr);
+      sb.con[t] = make_float4(c.x, c.y, c.z, m.z);
+      sb.col[t] = __ldg(color + g);
+      sb.mask[t] = (uint8_t)patch_mask(m.x, m.y, c.x, c.y, c.z, thr, tile_x0, tile_y0, f.axis);
     }
     __syncthreads();
-    if (!done) {
-      uint32_t n = min((uint32_t)kBlock, s1 - b);
-      for (uint32_t j = 0; j < n; ++j) {
-        float4 m = s_mean[j];
-        float4 c = s_conic[j];
-        float dx, dy;
-        boundary_delta(pxc, pyc, m, c, f, &dx, &dy);
-        float power = ((c.x * (dx * dx) + ((c.y * 2.0f) * dx) * dy) + c.z * (dy * dy)) * -0.5f;
-        if (power > 0.0f || power < -c.w) continue;
-        float alpha = rclamp(m.w * M::exp(power), 0.0f, 0.99f);
-        if (alpha < (float)(1.0 / 255.0)) continue;
-        float4 col = s_color[j];
-        float contrib = a.t * alpha;
-        a.r = a.r + col.x * contrib;
-        a.g = a.g + col.y * contrib;
-        a.b = a.b + col.z * contrib;
-        a.d = a.d + m.z * contrib;
-        a.t = a.t * (1.0f - alpha);
-        if (a.t < f.t_threshold) {
-          done = true;
-          break;
-        }
+    const uint32_t n = min((uint32_t)kBlock, s1 - b);
+    for (uint32_t c0 = 0; c0 < n; c0 += 32) {
+      if (__all_sync(0xffffffffu, done)) break;
+      const uint32_t k = c0 + lane;
+      uint32_t bits = __ballot_sync(0xffffffffu, k < n && ((sb.mask[k] >> warp) & 1u));
+      while (bits) {
+        const uint32_t j = c0 + (uint32_t)(__ffs(bits) - 1);
+        bits &= bits - 1u;
+        if (!done) done = blend_one<M>(sb, j, pxc, pyc, f, a);
       }
     }
   }
@@ -157,40 +216,41 @@ __global__ void __launch_bounds__(kBlock) k_raster(const uint32_t* __restrict__ 
                                                    const uint32_t* __restrict__ ids,
                                                    const float4* __restrict__ mean,
                                                    const float4* __restrict__ conic,
-                                                   const float4* __restrict__ color, FrameView f,
+                                                   const float4* __restrict__ color, FrameView fv,
                                                    const Control* __restrict__ ctl, void* __restrict__ out,
                                                    float* __restrict__ depth_out) {
   // Overflow: the reference zeroes the raster dispatch, so nothing is written.
   if (ctl->state[3] != 0u) return;
-  __shared__ float4 s_mean[kBlock];
-  __shared__ float4 s_conic[kBlock];
-  __shared__ float4 s_color[kBlock];
+  __shared__ Batch sb;
+  const RasterFrame f = {fv.vw, fv.vh, fv.t_threshold, fv.axis};
   const uint32_t tile = blockIdx.x;
-  const uint32_t tx = tile % f.tiles_x, ty = tile / f.tiles_x;
+  const uint32_t tx = tile % fv.tiles_x, ty = tile / fv.tiles_x;
   const uint32_t lx = morton_compact(threadIdx.x), ly = morton_compact(threadIdx.x >> 1);
   const uint32_t px = tx * kTileSize + lx, py = ty * kTileSize + ly;
-  const uint32_t W = (uint32_t)f.vw, H = (uint32_t)f.vh;
+  const uint32_t W = (uint32_t)fv.vw, H = (uint32_t)fv.vh;
   const bool active = px < W && py < H;
   const uint32_t begin = tile_offsets[tile], end = tile_offsets[tile + 1];
   const uint32_t source_count = end - begin;
-  const bool capped = f.max_per_tile != 0u;
-  const uint32_t raster_count = capped ? min(source_count, f.max_per_tile) : source_count;
-  const bool chunked = f.chunk != 0u && raster_count > f.chunk;
+  const bool capped = fv.max_per_tile != 0u;
+  const uint32_t raster_count = capped ? min(source_count, fv.max_per_tile) : source_count;
+  const uint32_t chunk = fv.chunk;
+  const bool chunked = chunk != 0u && raster_count > chunk;
   const float pxc = (float)px + 0.5f, pyc = (float)py + 0.5f;
+  const float tile_x0 = (float)(tx * kTileSize), tile_y0 = (float)(ty * kTileSize);
   PixelAcc a = {0.0f, 0.0f, 0.0f, 1.0f, 0.0f};
   if (!chunked) {
-    blend_range<M>(begin, source_count, raster_count, 0, raster_count, capped, ids, mean, conic, color, f, pxc,
-                   pyc, !active, a, s_mean, s_conic, s_color);
+    blend_range<M>(begin, source_count, raster_count, 0, raster_count, capped, ids, mean, conic, color, f, tile_x0,
+                   tile_y0, pxc, pyc, !active, a, sb);
   } else {
-    const uint32_t nchunk = (raster_count + f.chunk - 1) / f.chunk;
+    const uint32_t nchunk = (raster_count + chunk - 1) / chunk;
     bool finished = !active;
     for (uint32_t ch = 0; ch < nchunk; ++ch) {
       if (!__syncthreads_or(!finished)) break;
-      const uint32_t s0 = ch * f.chunk;
-      const uint32_t s1 = min(s0 + f.chunk, raster_count);
+      const uint32_t s0 = ch * chunk;
+      const uint32_t s1 = min(s0 + chunk, raster_count);
       PixelAcc p = {0.0f, 0.0f, 0.0f, 1.0f, 0.0f};
-      blend_range<M>(begin, source_count, raster_count, s0, s1, capped, ids, mean, conic, color, f, pxc, pyc,
-                     finished, p, s_mean, s_conic, s_color);
+      blend_range<M>(begin, source_count, raster_count, s0, s1, capped, ids, mean, conic, color, f, tile_x0, tile_y0,
+                     pxc, pyc, finished, p, sb);
       if (!finished) {
         a.r = a.r + p.r * a.t;
         a.g = a.g + p.g * a.t;
@@ -202,11 +262,11 @@ __global__ void __launch_bounds__(kBlock) k_raster(const uint32_t* __restrict__ 
     }
   }
   if (!active) return;
-  const float bga = rclamp(f.background[3], 0.0f, 1.0f);
-  float r = a.r + (f.background[0] * a.t) * bga;
-  float g = a.g + (f.background[1] * a.t) * bga;
-  float b = a.b + (f.background[2] * a.t) * bga;
-  float alpha = 1.0f - a.t * (1.0f - bga);
+  const float bga = rclamp(fv.background[3], 0.0f, 1.0f);
+  const float r = a.r + (fv.background[0] * a.t) * bga;
+  const float g = a.g + (fv.background[1] * a.t) * bga;
+  const float b = a.b + (fv.background[2] * a.t) * bga;
+  const float alpha = 1.0f - a.t * (1.0f - bga);
   const size_t o = (size_t)py * W + px;
   if (HALF_OUT) {
     __half2 lo = __floats2half2_rn(r, g);
@@ -218,7 +278,7 @@ __global__ void __launch_bounds__(kBlock) k_raster(const uint32_t* __restrict__ 
   } else {
     reinterpret_cast<float4*>(out)[o] = make_float4(r, g, b, alpha);
   }
-  if (depth_out) depth_out[o] = finalize_depth(a.d, a.t, f);
+  if (depth_out) depth_out[o] = finalize_depth(a.d, a.t, fv);
 }
 
 }  // namespace gs

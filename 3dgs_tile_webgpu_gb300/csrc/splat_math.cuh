@@ -193,18 +193,24 @@ __device__ __forceinline__ Projected project(f3 view, const m3& cv, const float*
   return o;
 }
 
-// projectionHelpers.ts:150-155: unpack4x8snorm(.xyz) * exp2(e)
-__device__ __forceinline__ f3 decode_sh(uint32_t packed) {
+// projectionHelpers.ts:150-155: unpack4x8snorm(.xyz) * exp2(e). `snorm`
+// holds max(b / 127, -1) for every signed byte b (index b & 255), the exact
+// quotients, so the lookup is bit-identical to dividing.
+__device__ __forceinline__ f3 decode_sh(uint32_t packed, const float* snorm) {
   int e = (int)((packed >> 24) & 255u) - 127;
   float scale = gsdm::pow2i(e);
-  float m0 = maxf((float)(int)(int8_t)(uint8_t)(packed) / 127.0f, -1.0f);
-  float m1 = maxf((float)(int)(int8_t)(uint8_t)(packed >> 8) / 127.0f, -1.0f);
-  float m2 = maxf((float)(int)(int8_t)(uint8_t)(packed >> 16) / 127.0f, -1.0f);
+  float m0 = snorm[packed & 255u];
+  float m1 = snorm[(packed >> 8) & 255u];
+  float m2 = snorm[(packed >> 16) & 255u];
   return {m0 * scale, m1 * scale, m2 * scale};
 }
 
-__device__ __forceinline__ void sh_acc(f3& col, float w, uint32_t packed) {
-  f3 c = decode_sh(packed);
+__device__ __forceinline__ float snorm8_value(uint32_t byte) {
+  return maxf((float)(int)(int8_t)(uint8_t)byte / 127.0f, -1.0f);
+}
+
+__device__ __forceinline__ void sh_acc(f3& col, float w, uint32_t packed, const float* snorm) {
+  f3 c = decode_sh(packed, snorm);
   col.x = col.x + w * c.x;
   col.y = col.y + w * c.y;
   col.z = col.z + w * c.z;
@@ -212,33 +218,33 @@ __device__ __forceinline__ void sh_acc(f3& col, float w, uint32_t packed) {
 
 // projectionHelpers.ts:118-179 for rgb8e8; co[] holds the C coefficients.
 template <int DEG>
-__device__ __forceinline__ f3 eval_sh(const uint32_t* co, f3 d) {
+__device__ __forceinline__ f3 eval_sh(const uint32_t* co, f3 d, const float* snorm) {
   float x = d.x, y = d.y, z = d.z;
-  f3 c0 = decode_sh(co[0]);
+  f3 c0 = decode_sh(co[0], snorm);
   const float k0 = 0.28209479177387814f;
   f3 col = {k0 * c0.x, k0 * c0.y, k0 * c0.z};
   if (DEG >= 1) {
-    sh_acc(col, -0.4886025119029199f * y, co[1]);
-    sh_acc(col, 0.4886025119029199f * z, co[2]);
-    sh_acc(col, -0.4886025119029199f * x, co[3]);
+    sh_acc(col, -0.4886025119029199f * y, co[1], snorm);
+    sh_acc(col, 0.4886025119029199f * z, co[2], snorm);
+    sh_acc(col, -0.4886025119029199f * x, co[3], snorm);
   }
   if (DEG >= 2) {
     float xx = x * x, yy = y * y, zz = z * z;
-    sh_acc(col, (1.0925484305920792f * x) * y, co[4]);
-    sh_acc(col, (-1.0925484305920792f * y) * z, co[5]);
-    sh_acc(col, 0.31539156525252005f * ((2.0f * zz - xx) - yy), co[6]);
-    sh_acc(col, (-1.0925484305920792f * x) * z, co[7]);
-    sh_acc(col, 0.5462742152960396f * (xx - yy), co[8]);
+    sh_acc(col, (1.0925484305920792f * x) * y, co[4], snorm);
+    sh_acc(col, (-1.0925484305920792f * y) * z, co[5], snorm);
+    sh_acc(col, 0.31539156525252005f * ((2.0f * zz - xx) - yy), co[6], snorm);
+    sh_acc(col, (-1.0925484305920792f * x) * z, co[7], snorm);
+    sh_acc(col, 0.5462742152960396f * (xx - yy), co[8], snorm);
   }
   if (DEG >= 3) {
     float xx = x * x, yy = y * y, zz = z * z;
-    sh_acc(col, (-0.5900435899266435f * y) * (3.0f * xx - yy), co[9]);
-    sh_acc(col, ((2.890611442640554f * x) * y) * z, co[10]);
-    sh_acc(col, (-0.4570457994644658f * y) * ((4.0f * zz - xx) - yy), co[11]);
-    sh_acc(col, (0.3731763325901154f * z) * ((2.0f * zz - 3.0f * xx) - 3.0f * yy), co[12]);
-    sh_acc(col, (-0.4570457994644658f * x) * ((4.0f * zz - xx) - yy), co[13]);
-    sh_acc(col, (1.445305721320277f * z) * (xx - yy), co[14]);
-    sh_acc(col, (-0.5900435899266435f * x) * (xx - 3.0f * yy), co[15]);
+    sh_acc(col, (-0.5900435899266435f * y) * (3.0f * xx - yy), co[9], snorm);
+    sh_acc(col, ((2.890611442640554f * x) * y) * z, co[10], snorm);
+    sh_acc(col, (-0.4570457994644658f * y) * ((4.0f * zz - xx) - yy), co[11], snorm);
+    sh_acc(col, (0.3731763325901154f * z) * ((2.0f * zz - 3.0f * xx) - 3.0f * yy), co[12], snorm);
+    sh_acc(col, (-0.4570457994644658f * x) * ((4.0f * zz - xx) - yy), co[13], snorm);
+    sh_acc(col, (1.445305721320277f * z) * (xx - yy), co[14], snorm);
+    sh_acc(col, (-0.5900435899266435f * x) * (xx - 3.0f * yy), co[15], snorm);
   }
   return {clampf(col.x + 0.5f, 0.0f, 1.0f), clampf(col.y + 0.5f, 0.0f, 1.0f), clampf(col.z + 0.5f, 0.0f, 1.0f)};
 }
