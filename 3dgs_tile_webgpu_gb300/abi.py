@@ -12,6 +12,7 @@ GS3D_ERROR_OUT_OF_MEMORY = 4
 GS3D_ERROR_CUDA = 5
 GS3D_ERROR_DEVICE_TIMEOUT = 6
 GS3D_ERROR_UNSUPPORTED = 7
+STATIC_COMPACT_MAX_ITEMS = 16777216
 STAGES = ("project", "compact", "depth_sort", "scan", "emit", "tile_sort", "ranges", "raster")
 STATUS_NAMES = {0: "ok", 1: "invalid-argument", 2: "range", 3: "not-prepared", 4: "allocation-failed",
                 5: "cuda-error", 6: "device-timeout", 7: "unsupported"}
@@ -79,6 +80,7 @@ SIGNATURES = {
     "gs3d_pipeline_set_profiling": (C.c_int, [_P, C.c_int]),
     "gs3d_pipeline_stage_times": (C.c_int, [_P, C.POINTER(C.c_float), C.POINTER(C.c_uint32)]),
     "gs3d_stage_name": (C.c_char_p, [C.c_uint32]),
+    "gs3d_compact_visible_static": (C.c_int, [_P, C.c_uint32, _P, _P, _P, _P, _P]),
     "gs3d_capacity_next": (C.c_uint64, [C.c_uint64, C.c_double, C.c_double, C.c_uint64, C.c_uint64]),
 }
 

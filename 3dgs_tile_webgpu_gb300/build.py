@@ -25,6 +25,7 @@ UNITS = {
     "sort.cu": [],
     "raster.cu": [],
     "pipeline.cu": [],
+    "static_scratch.cu": [],
 }
 
 

@@ -225,6 +225,26 @@ gs3d_status gs3d_pipeline_set_profiling(gs3d_pipeline* pipeline, int enabled);
 gs3d_status gs3d_pipeline_stage_times(gs3d_pipeline* pipeline, float* ms, uint32_t* renders);
 const char* gs3d_stage_name(uint32_t stage);
 
+/* Visibility compaction with no device allocation. This entry point has no
+ * counterpart in the reference. It serves callers that cannot call cudaMalloc
+ * where they enqueue work: code running during CUDA graph capture, hosts that
+ * route all device memory through their own arena, real-time loops that must
+ * not stall on the allocator. The caller passes every input and output; the
+ * kernel's scratch is a static device array of about 140 KB per GPU, held
+ * until the process exits.
+ *   keys[n]            per-ordinal depth key, 0xffffffff = not visible
+ *   visible_offsets[n] exclusive count of visible ordinals before each one
+ *   keys_out/ids_out   (key, ordinal) of the visible ordinals, in ordinal order
+ *   result[2]          device words: visible count, error flags (nonzero: a
+ *                      bounded device wait expired)
+ * n must not exceed GS3D_STATIC_COMPACT_MAX_ITEMS (else GS3D_ERROR_RANGE);
+ * keys must be 16-byte aligned. The first call on a device sets up the static
+ * array's address and must come before any stream capture. All calls share
+ * the array: calls that overlap on the GPU race, so order them on one stream. */
+#define GS3D_STATIC_COMPACT_MAX_ITEMS 16777216u
+gs3d_status gs3d_compact_visible_static(const uint32_t* keys, uint32_t n, uint32_t* visible_offsets,
+                                        uint32_t* keys_out, uint32_t* ids_out, uint32_t* result, void* stream);
+
 /* IntersectionCapacityPolicy.next(current, demand)
  * (src/renderer/pipeline/IntersectionCapacityPolicy.ts:90-100): the capacity
  * to grow to, or 0 for null (demand above maximum). */
