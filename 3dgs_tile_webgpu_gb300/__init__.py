@@ -18,7 +18,7 @@ import os
 import threading
 
 from . import abi
-from .abi import (GS3D_OK, Camera, GaussianData, PipelineDesc, Resources, Stats, Targets)
+from .abi import (GS3D_OK, Camera, GaussianData, PipelineDesc, Resources, Stats, Targets, View)
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "_build", "libgs3d.so")
@@ -170,6 +170,36 @@ class TiledGaussianPipeline:
         st = self._lib.gs3d_pipeline_render(self._p, C.byref(camera), int(attempt), 1 if reset_valid else 0,
                                             C.byref(t), C.c_void_p(int(stream)))
         _raise(self._lib, st, self._p)
+
+    def render_batch(self, views: list, attempt: int = 1, reset_valid: bool = False, stream: int = 0) -> None:
+        """Render several views in one launch sequence.
+
+        ``views`` holds (GaussianData, Camera, width, height, color_ptr,
+        depth_ptr, color_format) tuples."""
+        arr = (View * len(views))()
+        keep = []
+        for i, (data, cam, w, h, color_ptr, depth_ptr, fmt) in enumerate(views):
+            arr[i].data = C.pointer(data)
+            arr[i].camera = C.pointer(cam)
+            arr[i].width, arr[i].height = int(w), int(h)
+            arr[i].targets.color = int(color_ptr)
+            arr[i].targets.color_format = {"rgba16f": 0, "rgba32f": 1}[fmt]
+            arr[i].targets.depth = (C.cast(C.c_void_p(int(depth_ptr)), C.POINTER(C.c_float))
+                                    if depth_ptr else None)
+            keep.append((data, cam))
+        st = self._lib.gs3d_pipeline_render_batch(self._p, arr, len(views), int(attempt), 1 if reset_valid else 0,
+                                                  C.c_void_p(int(stream)))
+        _raise(self._lib, st, self._p)
+
+    def batch_layout(self) -> tuple[list, list]:
+        """(item_base, tile_base) of the last render, one entry per view plus the total."""
+        n = C.c_uint32()
+        self._lib.gs3d_pipeline_batch_layout(self._p, None, None, 0, C.byref(n))
+        items = (C.c_uint32 * (n.value + 1))()
+        tiles = (C.c_uint32 * (n.value + 1))()
+        _raise(self._lib, self._lib.gs3d_pipeline_batch_layout(self._p, items, tiles, n.value + 1, C.byref(n)),
+               self._p)
+        return list(items), list(tiles)
 
     def read_stats(self) -> dict:
         s = Stats()

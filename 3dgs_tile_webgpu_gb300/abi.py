@@ -46,6 +46,11 @@ class Targets(C.Structure):
                 ("depth", C.POINTER(C.c_float))]
 
 
+class View(C.Structure):
+    _fields_ = [("data", C.POINTER(GaussianData)), ("camera", C.POINTER(Camera)), ("width", C.c_uint32),
+                ("height", C.c_uint32), ("targets", Targets)]
+
+
 class Stats(C.Structure):
     _fields_ = [("visible_gaussian_count", C.c_uint32), ("intersection_count", C.c_uint32),
                 ("requested_intersections", C.c_uint32), ("overflow", C.c_uint32),
@@ -58,7 +63,7 @@ class Resources(C.Structure):
         "depth_sorted_keys", "depth_sorted_ids", "depth_ordered_tile_counts", "intersection_offsets",
         "dispatch_state", "visible_state", "sorted_tile_ids", "sorted_gaussian_ids", "tile_offsets",
         "output_state")] + [("active_count", C.c_uint32), ("tiles_x", C.c_uint32), ("tiles_y", C.c_uint32),
-                            ("reserved", C.c_uint32), ("intersection_capacity", C.c_uint64)]
+                            ("total_tiles", C.c_uint32), ("intersection_capacity", C.c_uint64)]
 
 
 # Every symbol include/gs3d.h declares, with (restype, argtypes).
@@ -73,6 +78,9 @@ SIGNATURES = {
     "gs3d_pipeline_resize_intersections": (C.c_int, [_P, C.c_uint64]),
     "gs3d_pipeline_prepare_frame": (C.c_int, [_P, C.c_uint32, C.c_uint32]),
     "gs3d_pipeline_render": (C.c_int, [_P, C.POINTER(Camera), C.c_uint32, C.c_int, C.POINTER(Targets), _P]),
+    "gs3d_pipeline_render_batch": (C.c_int, [_P, C.POINTER(View), C.c_uint32, C.c_uint32, C.c_int, _P]),
+    "gs3d_pipeline_batch_layout": (C.c_int, [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.c_uint32,
+                                             C.POINTER(C.c_uint32)]),
     "gs3d_pipeline_read_stats": (C.c_int, [_P, C.POINTER(Stats)]),
     "gs3d_pipeline_get_resources": (C.c_int, [_P, C.POINTER(Resources)]),
     "gs3d_pipeline_last_error": (C.c_char_p, [_P]),

@@ -11,38 +11,66 @@ namespace gs {
 constexpr int kBlock = 256;  // threads per block for the linear kernels
 constexpr uint32_t kTileSize = 16;  // pixels per tile side (src/renderer/pipeline/constants.ts:1)
 
-// Packed scene buffers (GaussianData), device pointers.
-struct SceneView {
+// One view of a batch: a scene (packed GaussianData buffers), a camera
+// (FrameUniforms.ts:18-58 + the object table), a viewport and its targets.
+// Views are concatenated: view v owns items [item_base, item_base + active)
+// (item_base is a multiple of kBlock so every projection block belongs to one
+// view) and global tile ids [tile_base, tile_base + tiles_x * tiles_y).
+struct ViewDesc {
   const float4* means;     // count
   const uint2* shape;      // count
   const uint32_t* rot;     // count
   const uint32_t* sh;      // count * C + count (active tail at count * C)
-  uint32_t count;
-  uint32_t active;
-  uint32_t degree;
-  uint32_t C;
-};
-
-// Frame uniforms (FrameUniforms.ts:18-58) plus pass options.
-struct FrameView {
+  const float* objects;    // object_count * 40
+  void* color;             // rgba16f or rgba32f, width * height
+  float* depth;            // width * height or null
+  uint32_t count, active, degree, C;
+  uint32_t object_count, color_half;
+  uint32_t tiles_x, tiles_y;
+  uint32_t item_base, tile_base, block_base, pad0;
   float P[16];             // projection, column-major
   float vw, vh, vnear, vfar;
+};
+
+// Pass options shared by every view (TiledGaussianPipeline constructor options).
+struct PassOptions {
   float filter;
   uint32_t axis;           // boundary axis 0/1/2
-  uint32_t tiles_x, tiles_y;
-  uint32_t object_count;
   uint32_t antialias;      // 0 compensated, 1 classic
   uint32_t subpixel;       // subpixel sample culling
   uint32_t depth_mode;     // 0 float32, 1 packed16
-  const float* objects;    // object_count * 40, device
+  uint32_t chunk;          // raster chunk size, 0 = none
+  uint32_t max_per_tile;   // 0 = uncapped
+  uint32_t depth_encoding; // 0 device depth, 1 raw
   float background[4];
   float t_threshold;
   float depth_alpha_threshold;
   float invalid_depth;
-  uint32_t chunk;          // raster chunk size, 0 = none
-  uint32_t max_per_tile;   // 0 = uncapped
-  uint32_t depth_encoding; // 0 device depth, 1 raw
+  uint32_t pad0;
 };
+
+// The batch table in device memory: three ascending base arrays (nviews + 1
+// entries each, the last one the total) followed by the view descriptors.
+struct BatchView {
+  const uint32_t* item_base;
+  const uint32_t* tile_base;
+  const uint32_t* block_base;
+  const ViewDesc* views;
+  uint32_t nviews;
+  uint32_t total_items;
+  uint32_t total_tiles;
+  uint32_t total_blocks;
+};
+
+// Index of the view whose [base[v], base[v+1]) range holds x.
+__device__ __forceinline__ uint32_t find_view(const uint32_t* base, uint32_t nviews, uint32_t x) {
+  uint32_t lo = 0, hi = nviews;  // base[lo] <= x < base[hi]
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (__ldg(base + mid) <= x) lo = mid; else hi = mid;
+  }
+  return lo;
+}
 
 // Per-frame control block, zeroed before each render.
 struct Control {
@@ -144,8 +172,8 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* s
 }
 
 // Launch wrappers implemented in the .cu files.
-void launch_project(const SceneView& s, const FrameView& f, float4* mean, float4* conic, float4* color,
-                    uint32_t* counts, uint32_t* keys, cudaStream_t st);
+void launch_project(const BatchView& b, const PassOptions& o, float4* mean, float4* conic, float4* color,
+                    uint32_t* counts, uint32_t* keys, int max_degree, cudaStream_t st);
 void launch_compact(const uint32_t* keys, uint32_t n, uint32_t* vis_off, uint32_t* keys_out, uint32_t* vals_out,
                     Control* ctl, unsigned long long* status, uint32_t epoch, int depth_passes, cudaStream_t st);
 void launch_scan_counts(const uint32_t* sorted_ids, const uint32_t* tile_counts, uint32_t n_max,
@@ -153,9 +181,9 @@ void launch_scan_counts(const uint32_t* sorted_ids, const uint32_t* tile_counts,
                         uint32_t epoch, uint32_t capacity, uint32_t attempt, int reset_valid, uint32_t* output_state,
                         cudaStream_t st);
 void launch_emit(const uint32_t* sorted_ids, uint32_t n_max, const float4* mean, const float4* conic,
-                 const uint32_t* ordered, const uint32_t* offsets, const FrameView& f, Control* ctl,
-                 uint32_t capacity, uint32_t* tile_keys, uint32_t* tile_vals, int tile_passes, int tile_digit_bits,
-                 cudaStream_t st);
+                 const uint32_t* ordered, const uint32_t* offsets, const BatchView& b, const PassOptions& o,
+                 Control* ctl, uint32_t capacity, uint32_t* tile_keys, uint32_t* tile_vals, int tile_passes,
+                 int tile_digit_bits, cudaStream_t st);
 void launch_tile_ranges(const uint32_t* sorted_tiles, Control* ctl, uint32_t ntile, uint32_t* offsets, int sms,
                         cudaStream_t st);
 // Onesweep LSD pass. n is read from *n_ptr on the device.
@@ -163,12 +191,12 @@ void launch_onesweep(int bits, const uint32_t* keys_in, const uint32_t* vals_in,
                      uint32_t* vals_out, const uint32_t* n_ptr, uint32_t n_max, int shift, const uint32_t* hist,
                      unsigned long long* status, uint32_t* ticket, uint32_t epoch, uint32_t* err, cudaStream_t st);
 constexpr uint32_t kSortTile = 4096;  // items per onesweep block
-// Rasterizer (precision: 0 fp32, 1 exact, 2 half2).
+// Rasterizer over every tile of the batch (precision: 0 fp32, 1 exact, 2 half2).
 void launch_raster(int precision, const uint32_t* tile_offsets, const uint32_t* sorted_ids, const float4* mean,
-                   const float4* conic, const float4* color, const FrameView& f, const Control* ctl, void* color_out,
-                   int color_half, float* depth_out, cudaStream_t st);
+                   const float4* conic, const float4* color, const BatchView& b, const PassOptions& o,
+                   const Control* ctl, cudaStream_t st);
 void launch_raster_exact(const uint32_t* tile_offsets, const uint32_t* sorted_ids, const float4* mean,
-                         const float4* conic, const float4* color, const FrameView& f, const Control* ctl,
-                         void* color_out, int color_half, float* depth_out, cudaStream_t st);
+                         const float4* conic, const float4* color, const BatchView& b, const PassOptions& o,
+                         const Control* ctl, cudaStream_t st);
 
 }  // namespace gs

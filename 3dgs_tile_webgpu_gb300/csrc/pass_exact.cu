@@ -14,51 +14,60 @@ namespace gs {
 
 // ---------------------------------------------------------------------------
 // K1: decode + project + cull + SH + tile count, one thread per active ordinal
-// (ProjectionStage.ts:385-649). Writes the projected mean/conic/colour/count
-// like the reference, plus the depth sort key (or kInvisibleKey), which the
-// compaction kernel consumes instead of re-reading the 16-byte means.
-template <int DEG>
-__device__ __forceinline__ void load_sh(const uint32_t* __restrict__ p, uint32_t* co) {
-  constexpr int C = (DEG + 1) * (DEG + 1);
-  if (DEG == 3) {
+// of every view (ProjectionStage.ts:385-649). Writes the projected
+// mean/conic/colour/count like the reference, plus the depth sort key (or
+// kInvisibleKey), which the compaction consumes instead of re-reading the
+// 16-byte means. Each block belongs to one view; the padding items after a
+// view's last ordinal are written as invisible.
+__device__ __forceinline__ void load_sh(const uint32_t* __restrict__ p, uint32_t degree, uint32_t* co) {
+  if (degree == 3) {
     const uint4* v = reinterpret_cast<const uint4*>(p);
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       uint4 w = __ldg(v + i);
       co[4 * i] = w.x; co[4 * i + 1] = w.y; co[4 * i + 2] = w.z; co[4 * i + 3] = w.w;
     }
-  } else if (DEG == 1) {
-    uint4 w = __ldg(reinterpret_cast<const uint4*>(p));
-    co[0] = w.x; co[1] = w.y; co[2] = w.z; co[3] = w.w;
   } else {
-#pragma unroll
-    for (int i = 0; i < C; ++i) co[i] = __ldg(p + i);
+    const uint32_t C = (degree + 1) * (degree + 1);
+    for (uint32_t i = 0; i < C; ++i) co[i] = __ldg(p + i);
   }
 }
 
-template <int DEG>
-__global__ void __launch_bounds__(kBlock) k_project(SceneView s, FrameView f, float4* __restrict__ mean_out,
+__device__ __forceinline__ f3 eval_sh_any(uint32_t degree, const uint32_t* co, f3 d, const float* snorm) {
+  switch (degree) {
+    case 0: return eval_sh<0>(co, d, snorm);
+    case 1: return eval_sh<1>(co, d, snorm);
+    case 2: return eval_sh<2>(co, d, snorm);
+    default: return eval_sh<3>(co, d, snorm);
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k_project(BatchView b, PassOptions o, float4* __restrict__ mean_out,
                                                     float4* __restrict__ conic_out, float4* __restrict__ color_out,
                                                     uint32_t* __restrict__ count_out, uint32_t* __restrict__ key_out) {
-  constexpr int C = (DEG + 1) * (DEG + 1);
   __shared__ float s_snorm[256];
+  __shared__ uint32_t s_view;
   s_snorm[threadIdx.x] = snorm8_value(threadIdx.x);
+  if (threadIdx.x == 0) s_view = find_view(b.block_base, b.nviews, blockIdx.x);
   __syncthreads();
-  const uint32_t gid = blockIdx.x * kBlock + threadIdx.x;
-  if (gid >= s.active) return;
+  const ViewDesc& v = b.views[s_view];
+  const uint32_t gid = (blockIdx.x - v.block_base) * kBlock + threadIdx.x;  // ordinal within the view
+  const uint32_t item = v.item_base + gid;
   float4 mo4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   uint32_t cnt = 0, key = kInvisibleKey;
   do {
-    const uint32_t slot = __ldg(s.sh + (size_t)s.count * C + gid);
-    if (slot >= s.count) break;  // out-of-range tail entries never draw
-    const float4 mo = __ldg(s.means + slot);
+    if (gid >= v.active) break;  // padding up to the view's next block boundary
+    const uint32_t C = v.C;
+    const uint32_t slot = __ldg(v.sh + (size_t)v.count * C + gid);
+    if (slot >= v.count) break;  // out-of-range tail entries never draw
+    const float4 mo = __ldg(v.means + slot);
     if (mo.w < 0.0f) break;  // empty slot (ProjectionStage.ts:408-410)
     const uint32_t obj = (uint32_t)mo.w;
-    if (obj >= f.object_count) break;  // unwritten object rows are zero
-    const float* ot = f.objects + 40 * (size_t)obj;
+    if (obj >= v.object_count) break;  // unwritten object rows are zero
+    const float* ot = v.objects + 40 * (size_t)obj;
     if (!(__ldg(ot + 36) > 0.0f)) break;  // object visibility (:445-450)
-    const float4 so = decode_scale_opacity(__ldg(s.shape + slot));
-    const float4 q = decode_rotation(__ldg(s.rot + slot));
+    const float4 so = decode_scale_opacity(__ldg(v.shape + slot));
+    const float4 q = decode_rotation(__ldg(v.rot + slot));
     float mv[16];
 #pragma unroll
     for (int i = 0; i < 16; ++i) mv[i] = __ldg(ot + 16 + i);
@@ -77,10 +86,14 @@ __global__ void __launch_bounds__(kBlock) k_project(SceneView s, FrameView f, fl
 #pragma unroll
       for (int r = 0; r < 3; ++r) l2v.m[c][r] = mv[4 * c + r];
     const m3 cv = view_covariance(so, q, l2v);
-    const Projected pr = project({vx, vy, vz}, cv, f.P, f.vw, f.vh, f.vnear, f.vfar, f.filter);
+    float P[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) P[i] = v.P[i];
+    const float vw = v.vw, vh = v.vh;
+    const Projected pr = project({vx, vy, vz}, cv, P, vw, vh, v.vnear, v.vfar, o.filter);
     if (!pr.ok) break;
     float op = clampf(so.w, 0.0f, 1.0f);
-    if (f.antialias == 0u) op = op * sqrtf(clampf(pr.orig_det / pr.det, 0.0f, 1.0f));
+    if (o.antialias == 0u) op = op * sqrtf(clampf(pr.orig_det / pr.det, 0.0f, 1.0f));
     if (op < (float)(1.0 / 255.0) || op != op) break;
     const float thr = gsdm::logf_(op * 255.0f);
     const float ex = sqrtf((thr * 2.0f) * clampf(pr.cov_x, 1e-12f, 1e4f));
@@ -88,55 +101,51 @@ __global__ void __launch_bounds__(kBlock) k_project(SceneView s, FrameView f, fl
     const float rx = ceilf(ex), ry = ceilf(ey);
     if (rx <= 0.0f || ry <= 0.0f) break;
     const float bminx = pr.cx - rx, bminy = pr.cy - ry, bmaxx = pr.cx + rx, bmaxy = pr.cy + ry;
-    if ((f.axis != 1u && (bmaxx < 0.0f || bminx >= f.vw)) || (f.axis != 2u && (bmaxy < 0.0f || bminy >= f.vh)))
+    if ((o.axis != 1u && (bmaxx < 0.0f || bminx >= vw)) || (o.axis != 2u && (bmaxy < 0.0f || bminy >= vh)))
       break;
-    if (f.subpixel != 0u &&
-        !subpixel_has_sample(pr.cx, pr.cy, pr.conic_x, pr.conic_y, pr.conic_z, thr, ex, ey, (uint32_t)f.vw,
-                             (uint32_t)f.vh, f.axis)) {
+    if (o.subpixel != 0u &&
+        !subpixel_has_sample(pr.cx, pr.cy, pr.conic_x, pr.conic_y, pr.conic_z, thr, ex, ey, (uint32_t)vw,
+                             (uint32_t)vh, o.axis)) {
       mo4 = make_float4(pr.cx, pr.cy, pr.depth, -1.0f);  // subpixel marker (:572-587)
       break;
     }
-    const float mtx = (float)((int)f.tiles_x - 1), mty = (float)((int)f.tiles_y - 1);
+    const int tiles_x = (int)v.tiles_x, tiles_y = (int)v.tiles_y;
+    const float mtx = (float)(tiles_x - 1), mty = (float)(tiles_y - 1);
     int tminx = (int)clampf(floorf(bminx / 16.0f), 0.0f, mtx);
     int tminy = (int)clampf(floorf(bminy / 16.0f), 0.0f, mty);
     int tmaxx = (int)clampf(floorf(bmaxx / 16.0f), 0.0f, mtx);
     int tmaxy = (int)clampf(floorf(bmaxy / 16.0f), 0.0f, mty);
-    if (f.axis == 1u) { tminx = 0; tmaxx = (int)f.tiles_x - 1; }
-    if (f.axis == 2u) { tminy = 0; tmaxy = (int)f.tiles_y - 1; }
+    if (o.axis == 1u) { tminx = 0; tmaxx = tiles_x - 1; }
+    if (o.axis == 2u) { tminy = 0; tmaxy = tiles_y - 1; }
     for (int ty = tminy; ty <= tmaxy; ++ty)
       for (int tx = tminx; tx <= tmaxx; ++tx)
-        if (boundary_tile_hit(pr.cx, pr.cy, pr.conic_x, pr.conic_y, pr.conic_z, thr, rx, ry, tx, ty, f.vw, f.vh,
-                              f.axis))
+        if (boundary_tile_hit(pr.cx, pr.cy, pr.conic_x, pr.conic_y, pr.conic_z, thr, rx, ry, tx, ty, vw, vh,
+                              o.axis))
           ++cnt;
     if (cnt == 0) break;
-    uint32_t co[C];
-    load_sh<DEG>(s.sh + (size_t)slot * C, co);
-    const f3 col = eval_sh<DEG>(co, vdir, s_snorm);
+    uint32_t co[16];
+    load_sh(v.sh + (size_t)slot * C, v.degree, co);
+    const f3 col = eval_sh_any(v.degree, co, vdir, s_snorm);
     mo4 = make_float4(pr.cx, pr.cy, pr.depth, op);
-    conic_out[gid] = make_float4(pr.conic_x, pr.conic_y, pr.conic_z, rx + ry * 512.0f);
-    color_out[gid] = make_float4(col.x, col.y, col.z, __uint_as_float(slot ^ kActiveTag));
-    if (f.depth_mode == 0u) {
+    conic_out[item] = make_float4(pr.conic_x, pr.conic_y, pr.conic_z, rx + ry * 512.0f);
+    color_out[item] = make_float4(col.x, col.y, col.z, __uint_as_float(slot ^ kActiveTag));
+    if (o.depth_mode == 0u) {
       key = __float_as_uint(pr.depth);  // visibility.ts:139
     } else {
-      float t = clampf((pr.depth - f.vnear) / (f.vfar - f.vnear), 0.0f, 1.0f);
+      float t = clampf((pr.depth - v.vnear) / (v.vfar - v.vnear), 0.0f, 1.0f);
       key = (uint32_t)gsdm::round_even_small(t * 65535.0f);  // visibility.ts:140-144
     }
   } while (false);
-  mean_out[gid] = mo4;
-  count_out[gid] = cnt;
-  key_out[gid] = key;
+  mean_out[item] = mo4;
+  count_out[item] = cnt;
+  key_out[item] = key;
 }
 
-void launch_project(const SceneView& s, const FrameView& f, float4* mean, float4* conic, float4* color,
-                    uint32_t* counts, uint32_t* keys, cudaStream_t st) {
-  if (s.active == 0) return;
-  const uint32_t grid = (s.active + kBlock - 1) / kBlock;
-  switch (s.degree) {
-    case 0: k_project<0><<<grid, kBlock, 0, st>>>(s, f, mean, conic, color, counts, keys); break;
-    case 1: k_project<1><<<grid, kBlock, 0, st>>>(s, f, mean, conic, color, counts, keys); break;
-    case 2: k_project<2><<<grid, kBlock, 0, st>>>(s, f, mean, conic, color, counts, keys); break;
-    default: k_project<3><<<grid, kBlock, 0, st>>>(s, f, mean, conic, color, counts, keys); break;
-  }
+void launch_project(const BatchView& b, const PassOptions& o, float4* mean, float4* conic, float4* color,
+                    uint32_t* counts, uint32_t* keys, int max_degree, cudaStream_t st) {
+  (void)max_degree;
+  if (b.total_blocks == 0) return;
+  k_project<<<b.total_blocks, kBlock, 0, st>>>(b, o, mean, conic, color, counts, keys);
 }
 
 // ---------------------------------------------------------------------------
@@ -299,13 +308,15 @@ void launch_scan_counts(const uint32_t* ids, const uint32_t* tile_counts, uint32
 
 // ---------------------------------------------------------------------------
 // Intersection emission (intersections.ts:43-111): per depth rank, one
-// (tile, ordinal) record for every tile the splat contributes to, written at
-// the rank's scanned offset; sentinel padding if fewer hits than reserved.
-// Also accumulates the tile sort's digit histograms.
+// (tile, item) record for every tile the splat contributes to, written at the
+// rank's scanned offset; sentinel padding if fewer hits than reserved. Tile
+// ids are global over the batch (the view's tile_base + local id; the
+// sentinel is the batch's tile total). Also accumulates the tile sort's digit
+// histograms.
 __global__ void __launch_bounds__(kBlock) k_emit(const uint32_t* __restrict__ ids, const float4* __restrict__ mean,
                                                  const float4* __restrict__ conic,
                                                  const uint32_t* __restrict__ ordered,
-                                                 const uint32_t* __restrict__ offsets, FrameView f,
+                                                 const uint32_t* __restrict__ offsets, BatchView bv, PassOptions o,
                                                  Control* __restrict__ ctl, uint32_t capacity,
                                                  uint32_t* __restrict__ tile_keys, uint32_t* __restrict__ tile_vals,
                                                  int passes, int digit_bits) {
@@ -317,29 +328,33 @@ __global__ void __launch_bounds__(kBlock) k_emit(const uint32_t* __restrict__ id
   const uint32_t n = ctl->visible_state[0];
   const uint32_t r = blockIdx.x * kBlock + tid;
   const uint32_t mask = (1u << digit_bits) - 1u;
-  const uint32_t ntile = f.tiles_x * f.tiles_y;
+  const uint32_t sentinel = bv.total_tiles;
   if (r < n) {
     const uint32_t g = ids[r];
+    const ViewDesc& v = bv.views[find_view(bv.item_base, bv.nviews, g)];
     const float4 m = __ldg(mean + g);
     const float4 c = __ldg(conic + g);
     const uint32_t packed = (uint32_t)c.w;
     const float rx = (float)(packed % 512u), ry = (float)(packed / 512u);
     const float thr = gsdm::logf_(m.w * 255.0f);
-    const float mtx = (float)((int)f.tiles_x - 1), mty = (float)((int)f.tiles_y - 1);
+    const int tiles_x = (int)v.tiles_x, tiles_y = (int)v.tiles_y;
+    const uint32_t tile_base = v.tile_base;
+    const float vw = v.vw, vh = v.vh;
+    const float mtx = (float)(tiles_x - 1), mty = (float)(tiles_y - 1);
     int tminx = (int)clampf(floorf((m.x - rx) / 16.0f), 0.0f, mtx);
     int tminy = (int)clampf(floorf((m.y - ry) / 16.0f), 0.0f, mty);
     int tmaxx = (int)clampf(floorf((m.x + rx) / 16.0f), 0.0f, mtx);
     int tmaxy = (int)clampf(floorf((m.y + ry) / 16.0f), 0.0f, mty);
-    if (f.axis == 1u) { tminx = 0; tmaxx = (int)f.tiles_x - 1; }
-    if (f.axis == 2u) { tminy = 0; tmaxy = (int)f.tiles_y - 1; }
+    if (o.axis == 1u) { tminx = 0; tmaxx = tiles_x - 1; }
+    if (o.axis == 2u) { tminy = 0; tmaxy = tiles_y - 1; }
     const uint32_t reserved = ordered[r];
     const uint32_t base = offsets[r];
     uint32_t local = 0;
     for (int ty = tminy; ty <= tmaxy; ++ty)
       for (int tx = tminx; tx <= tmaxx; ++tx)
-        if (boundary_tile_hit(m.x, m.y, c.x, c.y, c.z, thr, rx, ry, tx, ty, f.vw, f.vh, f.axis)) {
+        if (boundary_tile_hit(m.x, m.y, c.x, c.y, c.z, thr, rx, ry, tx, ty, vw, vh, o.axis)) {
           if (local < reserved && base + local < capacity) {
-            const uint32_t t = (uint32_t)ty * f.tiles_x + (uint32_t)tx;
+            const uint32_t t = tile_base + (uint32_t)ty * (uint32_t)tiles_x + (uint32_t)tx;
             tile_keys[base + local] = t;
             tile_vals[base + local] = g;
             for (int p = 0; p < passes; ++p) atomicAdd(&s_hist[p][(t >> (p * digit_bits)) & mask], 1u);
@@ -348,9 +363,9 @@ __global__ void __launch_bounds__(kBlock) k_emit(const uint32_t* __restrict__ id
         }
     for (uint32_t pad = local; pad < reserved; ++pad)
       if (base + pad < capacity) {
-        tile_keys[base + pad] = ntile;
+        tile_keys[base + pad] = sentinel;
         tile_vals[base + pad] = g;
-        for (int p = 0; p < passes; ++p) atomicAdd(&s_hist[p][(ntile >> (p * digit_bits)) & mask], 1u);
+        for (int p = 0; p < passes; ++p) atomicAdd(&s_hist[p][(sentinel >> (p * digit_bits)) & mask], 1u);
       }
   }
   __syncthreads();
@@ -361,13 +376,13 @@ __global__ void __launch_bounds__(kBlock) k_emit(const uint32_t* __restrict__ id
 }
 
 void launch_emit(const uint32_t* ids, uint32_t n_max, const float4* mean, const float4* conic,
-                 const uint32_t* ordered, const uint32_t* offsets, const FrameView& f, Control* ctl,
-                 uint32_t capacity, uint32_t* tile_keys, uint32_t* tile_vals, int passes, int digit_bits,
-                 cudaStream_t st) {
+                 const uint32_t* ordered, const uint32_t* offsets, const BatchView& b, const PassOptions& o,
+                 Control* ctl, uint32_t capacity, uint32_t* tile_keys, uint32_t* tile_vals, int passes,
+                 int digit_bits, cudaStream_t st) {
   if (n_max == 0) return;
   const uint32_t grid = (n_max + kBlock - 1) / kBlock;
-  k_emit<<<grid, kBlock, 0, st>>>(ids, mean, conic, ordered, offsets, f, ctl, capacity, tile_keys, tile_vals, passes,
-                                  digit_bits);
+  k_emit<<<grid, kBlock, 0, st>>>(ids, mean, conic, ordered, offsets, b, o, ctl, capacity, tile_keys, tile_vals,
+                                  passes, digit_bits);
 }
 
 // ---------------------------------------------------------------------------
@@ -393,15 +408,10 @@ void launch_tile_ranges(const uint32_t* keys, Control* ctl, uint32_t ntile, uint
 
 // ---------------------------------------------------------------------------
 void launch_raster_exact(const uint32_t* tile_offsets, const uint32_t* ids, const float4* mean, const float4* conic,
-                         const float4* color, const FrameView& f, const Control* ctl, void* color_out,
-                         int color_half, float* depth_out, cudaStream_t st) {
-  const uint32_t grid = f.tiles_x * f.tiles_y;
-  if (color_half)
-    k_raster<ExactMath, true><<<grid, kBlock, 0, st>>>(tile_offsets, ids, mean, conic, color, f, ctl, color_out,
-                                                       depth_out);
-  else
-    k_raster<ExactMath, false><<<grid, kBlock, 0, st>>>(tile_offsets, ids, mean, conic, color, f, ctl, color_out,
-                                                        depth_out);
+                         const float4* color, const BatchView& b, const PassOptions& o, const Control* ctl,
+                         cudaStream_t st) {
+  if (b.total_tiles == 0) return;
+  k_raster<ExactMath><<<b.total_tiles, kBlock, 0, st>>>(tile_offsets, ids, mean, conic, color, b, o, ctl);
 }
 
 }  // namespace gs

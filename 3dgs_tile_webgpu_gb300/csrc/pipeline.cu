@@ -18,7 +18,8 @@ using namespace gs;
 
 namespace {
 
-constexpr uint32_t kObjectRing = 4;  // pinned object-table staging slots
+constexpr uint32_t kObjectRing = 4;  // pinned batch-table staging slots
+constexpr uint32_t kMaxViews = 4096;
 constexpr uint32_t kEpochMask = (1u << 30) - 1u;
 constexpr uint32_t kStageEvents = GS3D_STAGE_COUNT + 1;
 
@@ -60,13 +61,17 @@ struct gs3d_pipeline {
   unsigned long long* status = nullptr;
   size_t status_words = 0;
   uint32_t epoch = 0;
-  // Object table staging.
-  uint32_t object_cap = 0;
-  float* objects_dev[kObjectRing] = {};
-  float* objects_pinned[kObjectRing] = {};
-  cudaEvent_t object_ev[kObjectRing] = {};
-  bool object_ev_used[kObjectRing] = {};
+  // Batch-table staging (bases, view descriptors, object tables), a ring of
+  // pinned host buffers each mirrored by a device buffer.
+  size_t stage_cap = 0;
+  unsigned char* stage_dev[kObjectRing] = {};
+  unsigned char* stage_pinned[kObjectRing] = {};
+  cudaEvent_t stage_ev[kObjectRing] = {};
+  bool stage_ev_used[kObjectRing] = {};
   uint32_t frame_index = 0;
+  // Layout of the last batch.
+  std::vector<uint32_t> item_bases, tile_bases;
+  uint32_t total_items = 0, total_tiles = 0;
   // Frame.
   bool prepared = false;
   uint32_t width = 0, height = 0, tiles_x = 0, tiles_y = 0;
@@ -200,20 +205,20 @@ gs3d_status ensure_capacity(gs3d_pipeline* p, uint64_t capacity) {
   return ensure_status(p);
 }
 
-gs3d_status ensure_objects(gs3d_pipeline* p, uint32_t objects) {
-  if (objects <= p->object_cap) return GS3D_OK;
-  const uint32_t cap = std::max(objects, std::max(8u, p->object_cap * 2u));
+gs3d_status ensure_stage(gs3d_pipeline* p, size_t bytes) {
+  if (bytes <= p->stage_cap) return GS3D_OK;
+  const size_t cap = std::max(bytes, std::max<size_t>(16384, p->stage_cap * 2));
   for (uint32_t i = 0; i < kObjectRing; ++i) {
-    if (p->object_ev_used[i]) cudaEventSynchronize(p->object_ev[i]);
-    dfree(p->objects_dev[i]);
-    if (p->objects_pinned[i]) cudaFreeHost(p->objects_pinned[i]);
-    p->objects_pinned[i] = nullptr;
-    cudaError_t e = dalloc(p->objects_dev[i], (size_t)cap * 40);
-    if (e != cudaSuccess) return cuda_fail(p, e, "allocating object table");
-    e = cudaMallocHost((void**)&p->objects_pinned[i], (size_t)cap * 40 * sizeof(float));
-    if (e != cudaSuccess) return cuda_fail(p, e, "allocating pinned object table");
+    if (p->stage_ev_used[i]) cudaEventSynchronize(p->stage_ev[i]);
+    dfree(p->stage_dev[i]);
+    if (p->stage_pinned[i]) cudaFreeHost(p->stage_pinned[i]);
+    p->stage_pinned[i] = nullptr;
+    cudaError_t e = dalloc(p->stage_dev[i], cap);
+    if (e != cudaSuccess) return cuda_fail(p, e, "allocating the batch table");
+    e = cudaMallocHost((void**)&p->stage_pinned[i], cap);
+    if (e != cudaSuccess) return cuda_fail(p, e, "allocating the pinned batch table");
   }
-  p->object_cap = cap;
+  p->stage_cap = cap;
   return GS3D_OK;
 }
 
@@ -244,10 +249,10 @@ void release_all(gs3d_pipeline* p) {
   for (cudaEvent_t e : p->events) cudaEventDestroy(e);
   p->events.clear();
   for (uint32_t i = 0; i < kObjectRing; ++i) {
-    if (p->object_ev_used[i]) cudaEventSynchronize(p->object_ev[i]);
-    if (p->object_ev[i]) cudaEventDestroy(p->object_ev[i]);
-    dfree(p->objects_dev[i]);
-    if (p->objects_pinned[i]) cudaFreeHost(p->objects_pinned[i]);
+    if (p->stage_ev_used[i]) cudaEventSynchronize(p->stage_ev[i]);
+    if (p->stage_ev[i]) cudaEventDestroy(p->stage_ev[i]);
+    dfree(p->stage_dev[i]);
+    if (p->stage_pinned[i]) cudaFreeHost(p->stage_pinned[i]);
   }
   dfree(p->mean); dfree(p->conic); dfree(p->color); dfree(p->counts); dfree(p->keys); dfree(p->vis_off);
   dfree(p->dk[0]); dfree(p->dk[1]); dfree(p->dv[0]); dfree(p->dv[1]); dfree(p->ordered); dfree(p->ioff);
@@ -319,7 +324,7 @@ gs3d_status gs3d_pipeline_create(const gs3d_pipeline_desc* desc, const gs3d_gaus
     return GS3D_ERROR_CUDA;
   }
   cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, p->device);
-  for (uint32_t i = 0; i < kObjectRing; ++i) cudaEventCreateWithFlags(&p->object_ev[i], cudaEventDisableTiming);
+  for (uint32_t i = 0; i < kObjectRing; ++i) cudaEventCreateWithFlags(&p->stage_ev[i], cudaEventDisableTiming);
   if ((e = dalloc(p->ctl, 1)) || (e = dalloc(p->output_state, 4))) {
     s = cuda_fail(p, e, "allocating control block");
     release_all(p);
@@ -329,7 +334,7 @@ gs3d_status gs3d_pipeline_create(const gs3d_pipeline_desc* desc, const gs3d_gaus
   cudaMemset(p->output_state, 0, 4 * sizeof(uint32_t));
   cudaMemset(p->ctl, 0, sizeof(Control));
   if ((s = ensure_slots(p, data->count)) != GS3D_OK || (s = ensure_capacity(p, desc->intersection_capacity)) != GS3D_OK ||
-      (s = ensure_objects(p, 8)) != GS3D_OK) {
+      (s = ensure_stage(p, 16384)) != GS3D_OK) {
     release_all(p);
     delete p;
     return s;
@@ -392,74 +397,162 @@ gs3d_status gs3d_pipeline_prepare_frame(gs3d_pipeline* p, uint32_t width, uint32
   return GS3D_OK;
 }
 
-gs3d_status gs3d_pipeline_render(gs3d_pipeline* p, const gs3d_camera* cam, uint32_t attempt, int reset_valid,
-                                 const gs3d_targets* targets, void* stream) {
-  if (!p) return GS3D_ERROR_INVALID_ARGUMENT;
-  // TiledGaussianPipeline.ts:324-329
-  if (!p->prepared) return fail(p, GS3D_ERROR_NOT_PREPARED, "TiledGaussianPipeline must be prepared before rendering");
-  if (!cam || !targets || !targets->color) return fail(p, GS3D_ERROR_INVALID_ARGUMENT, "camera and color target required");
-  if (targets->color_format > 1) return fail(p, GS3D_ERROR_INVALID_ARGUMENT, "unknown color format");
-  if (cam->object_count > 0 && !cam->object_table) return fail(p, GS3D_ERROR_INVALID_ARGUMENT, "object table is null");
-  if (!(cam->depth_near >= 0.0f) || !(cam->depth_far > cam->depth_near))
-    return fail(p, GS3D_ERROR_RANGE, "depth range must satisfy 0 <= near < far");
-  cudaSetDevice(p->device);
-  cudaStream_t st = (cudaStream_t)stream;
-  gs3d_status s = ensure_objects(p, std::max(1u, cam->object_count));
-  if (s != GS3D_OK) return s;
-  uint32_t launches = 0;
+}  // extern "C"
 
-  // Object table: pinned staging ring -> device (ObjectFrameState.update).
-  const uint32_t slot = p->frame_index++ % kObjectRing;
-  if (p->object_ev_used[slot]) cudaEventSynchronize(p->object_ev[slot]);
-  const size_t obj_bytes = (size_t)cam->object_count * 40 * sizeof(float);
-  if (obj_bytes) {
-    memcpy(p->objects_pinned[slot], cam->object_table, obj_bytes);
-    cudaMemcpyAsync(p->objects_dev[slot], p->objects_pinned[slot], obj_bytes, cudaMemcpyHostToDevice, st);
+namespace {
+
+size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
+
+// Validate, lay out and enqueue a batch of views: the whole pass of
+// TiledGaussianPipeline.render (TiledGaussianPipeline.ts:324-341) for every view
+// in one launch sequence.
+gs3d_status enqueue(gs3d_pipeline* p, const gs3d_view* views, uint32_t n, uint32_t attempt, int reset_valid,
+                    cudaStream_t st) {
+  if (n == 0 || n > kMaxViews) return fail(p, GS3D_ERROR_RANGE, "a batch holds 1 to 4096 views");
+  uint64_t items = 0, tiles = 0, blocks = 0;
+  size_t objects = 0;
+  for (uint32_t i = 0; i < n; ++i) {
+    const gs3d_view& v = views[i];
+    gs3d_status s = validate_data(p, v.data);
+    if (s != GS3D_OK) return s;
+    if (!v.camera || !v.targets.color) return fail(p, GS3D_ERROR_INVALID_ARGUMENT, "camera and color target required");
+    if (v.targets.color_format > 1) return fail(p, GS3D_ERROR_INVALID_ARGUMENT, "unknown color format");
+    if (v.camera->object_count > 0 && !v.camera->object_table)
+      return fail(p, GS3D_ERROR_INVALID_ARGUMENT, "object table is null");
+    if (!(v.camera->depth_near >= 0.0f) || !(v.camera->depth_far > v.camera->depth_near))
+      return fail(p, GS3D_ERROR_RANGE, "depth range must satisfy 0 <= near < far");
+    if (v.width == 0 || v.height == 0) return fail(p, GS3D_ERROR_RANGE, "render size must be positive");
+    const uint32_t tx = tiles_for(v.width), ty = tiles_for(v.height);
+    // TiledGaussianPipeline.ts:294-296
+    if (tx > 65535u || ty > 65535u) return fail(p, GS3D_ERROR_RANGE, "Render size exceeds WebGPU's tile dispatch limit");
+    const uint64_t b = ((uint64_t)v.data->active_count + kBlock - 1) / kBlock;
+    blocks += b;
+    items += b * kBlock;
+    tiles += (uint64_t)tx * ty;
+    objects += v.camera->object_count;
+  }
+  if (items >= 0xffffffffull || tiles >= 0x7fffffffull) return fail(p, GS3D_ERROR_RANGE, "batch too large");
+
+  // Workspaces (grow only; synchronise before freeing buffers a queued frame may use).
+  if (items > p->slot_cap || tiles + 1 > p->tile_cap ||
+      status_words_needed((uint32_t)items, p->capacity) > p->status_words) {
+    if (p->last_stream) cudaStreamSynchronize(p->last_stream);
+  }
+  gs3d_status s = ensure_slots(p, (uint32_t)items);
+  if (s != GS3D_OK) return s;
+  if ((s = ensure_status(p)) != GS3D_OK) return s;
+  if (tiles + 1 > p->tile_cap) {
+    uint32_t cap = 1;
+    while (cap < tiles + 1) cap <<= 1;
+    cudaError_t e = dalloc(p->tile_offsets, cap);
+    if (e != cudaSuccess) return cuda_fail(p, e, "allocating tile offsets");
+    cudaMemset(p->tile_offsets, 0, (size_t)cap * sizeof(uint32_t));
+    p->tile_cap = cap;
   }
 
-  const gs3d_gaussian_data& d = p->data;
-  SceneView sv;
-  sv.means = (const float4*)d.means;
-  sv.shape = (const uint2*)d.scales_opacity;
-  sv.rot = (const uint32_t*)d.rotations;
-  sv.sh = (const uint32_t*)d.sh_coefficients;
-  sv.count = d.count;
-  sv.active = d.active_count;
-  sv.degree = d.sh_degree;
-  sv.C = (d.sh_degree + 1) * (d.sh_degree + 1);
+  // Batch table: bases, view descriptors, object tables; one H2D copy.
+  const size_t bases_bytes = align16(3 * (size_t)(n + 1) * sizeof(uint32_t));
+  const size_t views_off = bases_bytes;
+  const size_t objects_off = align16(views_off + (size_t)n * sizeof(ViewDesc));
+  const size_t stage_bytes = objects_off + objects * 40 * sizeof(float);
+  if ((s = ensure_stage(p, stage_bytes)) != GS3D_OK) return s;
+  const uint32_t slot = p->frame_index++ % kObjectRing;
+  if (p->stage_ev_used[slot]) cudaEventSynchronize(p->stage_ev[slot]);
+  unsigned char* host = p->stage_pinned[slot];
+  unsigned char* dev = p->stage_dev[slot];
+  uint32_t* h_item = (uint32_t*)host;
+  uint32_t* h_tile = h_item + (n + 1);
+  uint32_t* h_block = h_tile + (n + 1);
+  ViewDesc* h_views = (ViewDesc*)(host + views_off);
+  float* h_obj = (float*)(host + objects_off);
+  uint32_t item = 0, tile = 0, block = 0;
+  size_t obj = 0;
+  p->item_bases.assign(n + 1, 0);
+  p->tile_bases.assign(n + 1, 0);
+  for (uint32_t i = 0; i < n; ++i) {
+    const gs3d_view& v = views[i];
+    const gs3d_gaussian_data& d = *v.data;
+    ViewDesc& w = h_views[i];
+    memset(&w, 0, sizeof(w));
+    w.means = (const float4*)d.means;
+    w.shape = (const uint2*)d.scales_opacity;
+    w.rot = (const uint32_t*)d.rotations;
+    w.sh = (const uint32_t*)d.sh_coefficients;
+    w.objects = (const float*)(dev + objects_off) + obj * 40;
+    w.color = v.targets.color;
+    w.depth = v.targets.depth;
+    w.count = d.count;
+    w.active = d.active_count;
+    w.degree = d.sh_degree;
+    w.C = (d.sh_degree + 1) * (d.sh_degree + 1);
+    w.object_count = v.camera->object_count;
+    w.color_half = v.targets.color_format == GS3D_COLOR_RGBA16F ? 1u : 0u;
+    w.tiles_x = tiles_for(v.width);
+    w.tiles_y = tiles_for(v.height);
+    w.item_base = item;
+    w.tile_base = tile;
+    w.block_base = block;
+    memcpy(w.P, v.camera->projection, sizeof(w.P));
+    w.vw = (float)v.width;
+    w.vh = (float)v.height;
+    w.vnear = v.camera->depth_near;
+    w.vfar = v.camera->depth_far;
+    if (v.camera->object_count)
+      memcpy(h_obj + obj * 40, v.camera->object_table, (size_t)v.camera->object_count * 40 * sizeof(float));
+    h_item[i] = item;
+    h_tile[i] = tile;
+    h_block[i] = block;
+    p->item_bases[i] = item;
+    p->tile_bases[i] = tile;
+    const uint32_t b = (d.active_count + kBlock - 1) / kBlock;
+    block += b;
+    item += b * kBlock;
+    tile += w.tiles_x * w.tiles_y;
+    obj += v.camera->object_count;
+  }
+  h_item[n] = item;
+  h_tile[n] = tile;
+  h_block[n] = block;
+  p->item_bases[n] = item;
+  p->tile_bases[n] = tile;
+  p->total_items = item;
+  p->total_tiles = tile;
+  cudaMemcpyAsync(dev, host, stage_bytes, cudaMemcpyHostToDevice, st);
 
-  FrameView f;
-  memcpy(f.P, cam->projection, sizeof(f.P));
-  f.vw = (float)p->width;
-  f.vh = (float)p->height;
-  f.vnear = cam->depth_near;
-  f.vfar = cam->depth_far;
-  f.filter = p->desc.filter_variance;
-  f.axis = p->desc.boundary_policy;
-  f.tiles_x = p->tiles_x;
-  f.tiles_y = p->tiles_y;
-  f.object_count = cam->object_count;
-  f.antialias = p->desc.antialias_mode;
-  f.subpixel = p->desc.subpixel_sample_culling ? 1u : 0u;
-  f.depth_mode = p->desc.depth_sort_mode;
-  f.objects = p->objects_dev[slot];
-  memcpy(f.background, p->desc.background, sizeof(f.background));
-  f.t_threshold = p->desc.raster_transmittance_threshold;
-  f.depth_alpha_threshold = p->desc.depth_alpha_threshold;
-  f.invalid_depth = p->desc.invalid_depth_value;
-  f.chunk = p->desc.raster_chunk_size;
-  f.max_per_tile = p->desc.max_rasterized_splats_per_tile;
-  f.depth_encoding = p->desc.depth_encoding;
+  BatchView bv;
+  bv.item_base = (const uint32_t*)dev;
+  bv.tile_base = bv.item_base + (n + 1);
+  bv.block_base = bv.tile_base + (n + 1);
+  bv.views = (const ViewDesc*)(dev + views_off);
+  bv.nviews = n;
+  bv.total_items = item;
+  bv.total_tiles = tile;
+  bv.total_blocks = block;
 
-  const uint32_t N = d.active_count;
-  const uint32_t ntile = p->tiles_x * p->tiles_y;
+  PassOptions o;
+  memset(&o, 0, sizeof(o));
+  o.filter = p->desc.filter_variance;
+  o.axis = p->desc.boundary_policy;
+  o.antialias = p->desc.antialias_mode;
+  o.subpixel = p->desc.subpixel_sample_culling ? 1u : 0u;
+  o.depth_mode = p->desc.depth_sort_mode;
+  o.chunk = p->desc.raster_chunk_size;
+  o.max_per_tile = p->desc.max_rasterized_splats_per_tile;
+  o.depth_encoding = p->desc.depth_encoding;
+  memcpy(o.background, p->desc.background, sizeof(o.background));
+  o.t_threshold = p->desc.raster_transmittance_threshold;
+  o.depth_alpha_threshold = p->desc.depth_alpha_threshold;
+  o.invalid_depth = p->desc.invalid_depth_value;
+
+  const uint32_t N = item;
+  uint32_t launches = 0;
   Control* ctl = p->ctl;
   cudaMemsetAsync(ctl, 0, sizeof(Control), st);
 
   // K1: projection.
   mark(p, GS3D_STAGE_PROJECT, st);
-  launch_project(sv, f, p->mean, p->conic, p->color, p->counts, p->keys, st);
-  launches += N ? 1 : 0;
+  launch_project(bv, o, p->mean, p->conic, p->color, p->counts, p->keys, 3, st);
+  launches += block ? 1 : 0;
   // Visibility compaction.
   mark(p, GS3D_STAGE_COMPACT, st);
   const int depth_passes = p->desc.depth_sort_mode == GS3D_DEPTH_FLOAT32 ? 4 : 2;
@@ -484,11 +577,11 @@ gs3d_status gs3d_pipeline_render(gs3d_pipeline* p, const gs3d_camera* cam, uint3
   ++launches;
   // Emission + tile-sort histograms.
   mark(p, GS3D_STAGE_EMIT, st);
-  const uint32_t tile_bits = std::max(1u, ceil_log2((uint64_t)ntile + 1));
+  const uint32_t tile_bits = std::max(1u, ceil_log2((uint64_t)tile + 1));
   const int tile_passes = (int)((tile_bits + 7) / 8);
   const int digit_bits = (int)((tile_bits + tile_passes - 1) / tile_passes);
-  launch_emit(p->dv[cur], N, p->mean, p->conic, p->ordered, p->ioff, f, ctl, cap32, p->tk[0], p->tv[0], tile_passes,
-              digit_bits, st);
+  launch_emit(p->dv[cur], N, p->mean, p->conic, p->ordered, p->ioff, bv, o, ctl, cap32, p->tk[0], p->tv[0],
+              tile_passes, digit_bits, st);
   launches += N ? 1 : 0;
   // Tile sort.
   mark(p, GS3D_STAGE_TILE_SORT, st);
@@ -503,22 +596,62 @@ gs3d_status gs3d_pipeline_render(gs3d_pipeline* p, const gs3d_camera* cam, uint3
   p->tile_final = tcur;
   // Tile ranges.
   mark(p, GS3D_STAGE_RANGES, st);
-  launch_tile_ranges(p->tk[tcur], ctl, ntile, p->tile_offsets, p->sms, st);
+  launch_tile_ranges(p->tk[tcur], ctl, tile, p->tile_offsets, p->sms, st);
   ++launches;
   // Raster.
   mark(p, GS3D_STAGE_RASTER, st);
-  launch_raster((int)p->desc.raster_precision, p->tile_offsets, p->tv[tcur], p->mean, p->conic, p->color, f, ctl,
-                targets->color, targets->color_format == GS3D_COLOR_RGBA16F ? 1 : 0, targets->depth, st);
+  launch_raster((int)p->desc.raster_precision, p->tile_offsets, p->tv[tcur], p->mean, p->conic, p->color, bv, o, ctl,
+                st);
   ++launches;
 
   mark(p, GS3D_STAGE_COUNT, st);
   if (p->profiling) ++p->profiled;
-  cudaEventRecord(p->object_ev[slot], st);
-  p->object_ev_used[slot] = true;
+  cudaEventRecord(p->stage_ev[slot], st);
+  p->stage_ev_used[slot] = true;
   p->last_stream = st;
   p->last_launches = launches;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(p, e, "launching the pass");
+  return GS3D_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+gs3d_status gs3d_pipeline_render(gs3d_pipeline* p, const gs3d_camera* cam, uint32_t attempt, int reset_valid,
+                                 const gs3d_targets* targets, void* stream) {
+  if (!p) return GS3D_ERROR_INVALID_ARGUMENT;
+  // TiledGaussianPipeline.ts:324-329
+  if (!p->prepared) return fail(p, GS3D_ERROR_NOT_PREPARED, "TiledGaussianPipeline must be prepared before rendering");
+  if (!cam || !targets) return fail(p, GS3D_ERROR_INVALID_ARGUMENT, "camera and color target required");
+  cudaSetDevice(p->device);
+  gs3d_view v;
+  v.data = &p->data;
+  v.camera = cam;
+  v.width = p->width;
+  v.height = p->height;
+  v.targets = *targets;
+  return enqueue(p, &v, 1, attempt, reset_valid, (cudaStream_t)stream);
+}
+
+gs3d_status gs3d_pipeline_render_batch(gs3d_pipeline* p, const gs3d_view* views, uint32_t count, uint32_t attempt,
+                                       int reset_valid, void* stream) {
+  if (!p || !views) return GS3D_ERROR_INVALID_ARGUMENT;
+  cudaSetDevice(p->device);
+  p->prepared = true;
+  return enqueue(p, views, count, attempt, reset_valid, (cudaStream_t)stream);
+}
+
+gs3d_status gs3d_pipeline_batch_layout(gs3d_pipeline* p, uint32_t* item_base, uint32_t* tile_base,
+                                       uint32_t capacity, uint32_t* count) {
+  if (!p || !count) return GS3D_ERROR_INVALID_ARGUMENT;
+  const uint32_t n = p->item_bases.empty() ? 0u : (uint32_t)p->item_bases.size() - 1u;
+  *count = n;
+  for (uint32_t i = 0; i <= n && i < capacity; ++i) {
+    if (item_base) item_base[i] = p->item_bases[i];
+    if (tile_base) tile_base[i] = p->tile_bases[i];
+  }
   return GS3D_OK;
 }
 
@@ -560,9 +693,10 @@ gs3d_status gs3d_pipeline_get_resources(gs3d_pipeline* p, gs3d_resources* r) {
   r->sorted_gaussian_ids = p->tv[p->tile_final];
   r->tile_offsets = p->tile_offsets;
   r->output_state = p->output_state;
-  r->active_count = p->data.active_count;
+  r->active_count = p->total_items;
   r->tiles_x = p->tiles_x;
   r->tiles_y = p->tiles_y;
+  r->total_tiles = p->total_tiles;
   r->intersection_capacity = p->capacity;
   return GS3D_OK;
 }

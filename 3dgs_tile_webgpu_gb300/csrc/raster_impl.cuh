@@ -191,18 +191,19 @@ __device__ __forceinline__ void blend_range(uint32_t begin, uint32_t source_coun
 __device__ __forceinline__ bool finite_r(float v) { return v == v && fabsf(v) <= 3.402823e+38f; }
 
 // finalizeGaussianDepth.ts:18-68 with the default nodes (GaussianContextNodes.ts:127-132).
-__device__ __forceinline__ float finalize_depth(float wd, float trans, const FrameView& f) {
+__device__ __forceinline__ float finalize_depth(float wd, float trans, const PassOptions& o, float vnear,
+                                                float vfar) {
   float a = 1.0f - trans;
   float out = 0.0f;
   if (a > 0.0f) out = wd / a;
   bool scalar_valid = a > 0.0f && finite_r(wd) && finite_r(out) && out > 0.0f;
-  bool valid = scalar_valid && a > f.depth_alpha_threshold;
-  float dev = f.invalid_depth;
+  bool valid = scalar_valid && a > o.depth_alpha_threshold;
+  float dev = o.invalid_depth;
   if (valid) {
     float enc;
-    if (f.depth_encoding == 0u) {
+    if (o.depth_encoding == 0u) {
       float vz = -out;
-      enc = rclamp(((f.vnear + vz) * f.vfar) / ((f.vfar - f.vnear) * vz), 0.0f, 1.0f);
+      enc = rclamp(((vnear + vz) * vfar) / ((vfar - vnear) * vz), 0.0f, 1.0f);
     } else {
       enc = out;
     }
@@ -211,29 +212,35 @@ __device__ __forceinline__ float finalize_depth(float wd, float trans, const Fra
   return dev;
 }
 
-template <class M, bool HALF_OUT>
+// One block per tile of the batch; the tile's view supplies its viewport and
+// targets.
+template <class M>
 __global__ void __launch_bounds__(kBlock) k_raster(const uint32_t* __restrict__ tile_offsets,
                                                    const uint32_t* __restrict__ ids,
                                                    const float4* __restrict__ mean,
                                                    const float4* __restrict__ conic,
-                                                   const float4* __restrict__ color, FrameView fv,
-                                                   const Control* __restrict__ ctl, void* __restrict__ out,
-                                                   float* __restrict__ depth_out) {
+                                                   const float4* __restrict__ color, BatchView bv, PassOptions o,
+                                                   const Control* __restrict__ ctl) {
   // Overflow: the reference zeroes the raster dispatch, so nothing is written.
   if (ctl->state[3] != 0u) return;
   __shared__ Batch sb;
-  const RasterFrame f = {fv.vw, fv.vh, fv.t_threshold, fv.axis};
+  __shared__ uint32_t s_view;
+  if (threadIdx.x == 0) s_view = find_view(bv.tile_base, bv.nviews, blockIdx.x);
+  __syncthreads();
+  const ViewDesc& v = bv.views[s_view];
+  const RasterFrame f = {v.vw, v.vh, o.t_threshold, o.axis};
   const uint32_t tile = blockIdx.x;
-  const uint32_t tx = tile % fv.tiles_x, ty = tile / fv.tiles_x;
+  const uint32_t local = tile - v.tile_base;
+  const uint32_t tx = local % v.tiles_x, ty = local / v.tiles_x;
   const uint32_t lx = morton_compact(threadIdx.x), ly = morton_compact(threadIdx.x >> 1);
   const uint32_t px = tx * kTileSize + lx, py = ty * kTileSize + ly;
-  const uint32_t W = (uint32_t)fv.vw, H = (uint32_t)fv.vh;
+  const uint32_t W = (uint32_t)v.vw, H = (uint32_t)v.vh;
   const bool active = px < W && py < H;
   const uint32_t begin = tile_offsets[tile], end = tile_offsets[tile + 1];
   const uint32_t source_count = end - begin;
-  const bool capped = fv.max_per_tile != 0u;
-  const uint32_t raster_count = capped ? min(source_count, fv.max_per_tile) : source_count;
-  const uint32_t chunk = fv.chunk;
+  const bool capped = o.max_per_tile != 0u;
+  const uint32_t raster_count = capped ? min(source_count, o.max_per_tile) : source_count;
+  const uint32_t chunk = o.chunk;
   const bool chunked = chunk != 0u && raster_count > chunk;
   const float pxc = (float)px + 0.5f, pyc = (float)py + 0.5f;
   const float tile_x0 = (float)(tx * kTileSize), tile_y0 = (float)(ty * kTileSize);
@@ -262,23 +269,23 @@ __global__ void __launch_bounds__(kBlock) k_raster(const uint32_t* __restrict__ 
     }
   }
   if (!active) return;
-  const float bga = rclamp(fv.background[3], 0.0f, 1.0f);
-  const float r = a.r + (fv.background[0] * a.t) * bga;
-  const float g = a.g + (fv.background[1] * a.t) * bga;
-  const float b = a.b + (fv.background[2] * a.t) * bga;
+  const float bga = rclamp(o.background[3], 0.0f, 1.0f);
+  const float r = a.r + (o.background[0] * a.t) * bga;
+  const float g = a.g + (o.background[1] * a.t) * bga;
+  const float b = a.b + (o.background[2] * a.t) * bga;
   const float alpha = 1.0f - a.t * (1.0f - bga);
-  const size_t o = (size_t)py * W + px;
-  if (HALF_OUT) {
+  const size_t off = (size_t)py * W + px;
+  if (v.color_half) {
     __half2 lo = __floats2half2_rn(r, g);
     __half2 hi = __floats2half2_rn(b, alpha);
     uint2 w;
     w.x = *reinterpret_cast<uint32_t*>(&lo);
     w.y = *reinterpret_cast<uint32_t*>(&hi);
-    reinterpret_cast<uint2*>(out)[o] = w;
+    reinterpret_cast<uint2*>(v.color)[off] = w;
   } else {
-    reinterpret_cast<float4*>(out)[o] = make_float4(r, g, b, alpha);
+    reinterpret_cast<float4*>(v.color)[off] = make_float4(r, g, b, alpha);
   }
-  if (depth_out) depth_out[o] = finalize_depth(a.d, a.t, fv);
+  if (v.depth) v.depth[off] = finalize_depth(a.d, a.t, o, v.vnear, v.vfar);
 }
 
 }  // namespace gs

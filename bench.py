@@ -40,7 +40,8 @@ def parse():
     ap.add_argument("--cameras", type=int, default=16)
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--height", type=int, default=1080)
-    ap.add_argument("--precision", default="fp32", choices=["fp32", "exact"])
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "exact", "half2"])
+    ap.add_argument("--plain-precision", default="fp32", choices=["fp32", "exact"])
     ap.add_argument("--latency-frames", type=int, default=240)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
@@ -187,90 +188,118 @@ def main() -> None:
     cams = [P.make_camera(f) for f in frames]
     ds = dev.DeviceScene(scene)
     W, H = args.width, args.height
-    opts = {"raster_precision": args.precision, "intersection_capacity": 1 << 26}
-    pipe = P.TiledGaussianPipeline(ds.data(), opts)
-    pipe.prepare_frame(W, H)
-    color = torch.empty((H, W, 4), dtype=torch.float16, device="cuda")
+    ncam = len(cams)
+
+    def make_pipe(precision):
+        pp = P.TiledGaussianPipeline(ds.data(), {"raster_precision": precision, "intersection_capacity": 1 << 26})
+        pp.prepare_frame(W, H)
+        return pp
+
+    plain = make_pipe(args.plain_precision)
+    colors = [torch.empty((H, W, 4), dtype=torch.float16, device="cuda") for _ in range(ncam)]
     host = torch.empty((H, W, 4), dtype=torch.float16, pin_memory=True)
+    data = ds.data()
 
     # Size the intersection workspace from the demand of every camera
     # (IntersectionCapacityPolicy headroom 1.25).
     demand, stats = 0, []
     for cam in cams:
-        pipe.render(cam, color.data_ptr(), 0, color_format="rgba16f")
-        s = pipe.read_stats()
-        stats.append(s)
-        demand = max(demand, s["requestedIntersections"])
-    pipe.resize_intersections(int(demand * 1.25) + 256)
+        plain.render(cam, colors[0].data_ptr(), 0, color_format="rgba16f")
+        st = plain.read_stats()
+        stats.append(st)
+        demand = max(demand, st["requestedIntersections"])
+    plain.resize_intersections(int(demand * 1.25) + 256)
 
-    def step():
+    def step_plain():
         launches = 0
-        for cam in cams:
-            pipe.render(cam, color.data_ptr(), 0, color_format="rgba16f")
-            launches += pipe.last_launch_count()
+        for i, cam in enumerate(cams):
+            plain.render(cam, colors[i].data_ptr(), 0, color_format="rgba16f")
+            launches += plain.last_launch_count()
         return launches
 
-    for _ in range(max(args.warmup, 3)):
-        step()
-    torch.cuda.synchronize()
+    def timed(step, pipe_for_stages):
+        """Device time of exactly `steps` steps, per-stage events on."""
+        for _ in range(max(args.warmup, 3)):
+            step()
+        torch.cuda.synchronize()
+        clocks = Clocks(local)
+        pipe_for_stages.set_profiling(True)
+        pipe_for_stages.stage_times()
+        barrier()
+        torch.cuda.synchronize()
+        clocks.start()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        nl = 0
+        for _ in range(args.steps):
+            nl += step()
+        e1.record()
+        torch.cuda.synchronize()
+        ck = clocks.stop()
+        barrier()
+        ms = e0.elapsed_time(e1)
+        sm, prof = pipe_for_stages.stage_times()
+        pipe_for_stages.set_profiling(False)
+        if world > 1:
+            t = torch.tensor([ms], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, sm, prof, nl, ck
 
-    # Timed region: device time over exactly `steps` steps, per-stage events on.
-    clocks = Clocks(local)
-    pipe.set_profiling(True)
-    pipe.stage_times()
-    barrier()
-    torch.cuda.synchronize()
-    clocks.start()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ev0.record()
-    launches = 0
-    for _ in range(args.steps):
-        launches += step()
-    ev1.record()
-    torch.cuda.synchronize()
-    clock_info = clocks.stop()
-    barrier()
-    ms_total = ev0.elapsed_time(ev1)
-    stage_ms, profiled = pipe.stage_times()
-    pipe.set_profiling(False)
-    if world > 1:
-        t = torch.tensor([ms_total], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_total = float(t.item())
-    frames_done = args.steps * len(cams) * world
-    fps = frames_done / (ms_total / 1000.0)
+    ms_plain, stage_ms_plain, prof_plain, launches_plain, clocks_plain = timed(step_plain, plain)
+    fps_plain = args.steps * ncam * world / (ms_plain / 1000.0)
 
-    # Per-frame latency distribution (each frame synchronised on its own).
-    lat = []
-    for i in range(args.latency_frames):
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record()
-        pipe.render(cams[i % len(cams)], color.data_ptr(), 0, color_format="rgba16f")
-        b.record()
-        b.synchronize()
-        lat.append(a.elapsed_time(b))
-    lat.sort()
-    p50 = lat[len(lat) // 2]
-    p99 = lat[min(len(lat) - 1, int(0.99 * len(lat)))]
+    # Batched form: all cameras of a step in one launch sequence.
+    batched = P.TiledGaussianPipeline(ds.data(), {"raster_precision": args.precision,
+                                                  "intersection_capacity": int(demand * 1.25 * ncam) + 256})
+    views = [(data, cam, W, H, colors[i].data_ptr(), 0, "rgba16f") for i, cam in enumerate(cams)]
 
-    # End to end through the public API: camera/object table from host memory
-    # in, the rendered rgba16f image back to pinned host memory, every frame.
+    def step_batched():
+        batched.render_batch(views)
+        return batched.last_launch_count()
+
+    ms_total, stage_ms, profiled, launches, clock_info = timed(step_batched, batched)
+    fps = args.steps * ncam * world / (ms_total / 1000.0)
+    bstats = batched.read_stats()
+
+    # Latency distributions: one frame (plain) and one 16-camera batch, each
+    # synchronised on its own.
+    def latencies(fn, count):
+        out = []
+        for i in range(count):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn(i)
+            b.record()
+            b.synchronize()
+            out.append(a.elapsed_time(b))
+        out.sort()
+        return out[len(out) // 2], out[min(len(out) - 1, int(0.99 * len(out)))]
+
+    p50_plain, p99_plain = latencies(lambda i: plain.render(cams[i % ncam], colors[0].data_ptr(), 0,
+                                                            color_format="rgba16f"), args.latency_frames)
+    p50, p99 = latencies(lambda i: batched.render_batch(views), max(20, args.latency_frames // ncam))
+
+    # End to end through the public API (batched form): camera/object tables
+    # from host memory in, every rendered rgba16f image back to pinned host
+    # memory, every step.
     torch.cuda.synchronize()
     barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        for cam in cams:
-            pipe.render(cam, color.data_ptr(), 0, color_format="rgba16f")
-            host.copy_(color, non_blocking=True)
+        batched.render_batch(views)
+        for c in colors:
+            host.copy_(c, non_blocking=True)
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     if world > 1:
         t = torch.tensor([e2e_s], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         e2e_s = float(t.item())
+    frames_done = args.steps * ncam * world
     e2e_fps = frames_done / e2e_s
-    h2d = len(cams) * (16 * 4 + 40 * 4)  # projection + one object row per frame
-    d2h = len(cams) * W * H * 8
+    h2d = ncam * (16 * 4 + 40 * 4)  # projection + one object row per view
+    d2h = ncam * W * H * 8
 
     # Roofline of every stage; the dominant one is reported as `roofline`.
     hbm, peak_kind = peaks()
@@ -280,8 +309,12 @@ def main() -> None:
     tile_bits = max(1, int(np.ceil(np.log2(tiles + 1))))
     tile_passes = (tile_bits + 7) // 8
     stages = {}
+    # per batch: every stage processes all views of the step
+    bn, bv_, bi, bt = n * ncam, v * ncam, inter * ncam, tiles * ncam
+    btile_bits = max(1, int(np.ceil(np.log2(bt + 1))))
+    btile_passes = (btile_bits + 7) // 8
     for name, ms in stage_ms.items():
-        b = stage_bytes(name, n, v, inter, tiles, W * H, 16, 4, tile_passes, 8, False)
+        b = stage_bytes(name, bn, bv_, bi, bt, W * H * ncam, 16, 4, btile_passes, 8, False)
         gbs = b / (ms * 1e-3) / 1e9 if ms > 0 else 0.0
         stages[name] = {"ms": ms, "bytes": b, "GB/s": gbs, "frac": gbs / hbm}
     dom = max(stages, key=lambda k: stages[k]["ms"])
@@ -293,9 +326,9 @@ def main() -> None:
     psnr_db = None
     if rank == 0 and not args.no_cpu_baseline:
         import oracle
-        pipe.render(cams[0], color.data_ptr(), 0, color_format="rgba16f")
+        batched.render_batch(views)
         torch.cuda.synchronize()
-        img = color.float().cpu().numpy()
+        img = colors[0].float().cpu().numpy()
         t0 = time.perf_counter()
         o32 = oracle.render(scene, frames[0], 0, output_depth=False)
         cpu_s = time.perf_counter() - t0
@@ -305,21 +338,28 @@ def main() -> None:
         cpu = {"value": 1.0 / cpu_s, "unit": "frames/s", "cores": oracle.lib().gso_num_threads(), "kind": "port",
                "sample": "camera 0 of the workload, one 1080p frame (FP32 restatement, OpenMP)"}
 
-    pipe.dispose()
+    plain.dispose()
+    batched.dispose()
     if rank != 0:
         return
     out = {
         "metric": METRIC, "value": fps, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_total / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "vs_baseline": None, "dtype": "f16" if args.precision == "half2" else "f32", "data": "synthetic",
         "config": {"workload": f"{args.splats} clustered Gaussians (64-cluster mixture, SH3 rgb8e8, compact), "
-                               f"{W}x{H}, {len(cams)} orbit cameras per step, plain {args.precision} raster",
+                               f"{W}x{H}, {len(cams)} orbit cameras per step rendered as one batch, "
+                               f"{args.precision} raster",
                    "splats": args.splats, "width": W, "height": H, "cameras": len(cams),
                    "frames_per_step": len(cams), "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 (288 MB packed scene read every frame)",
                    "visible_mean": v, "intersections_mean": inter},
         "p50_ms": p50, "p99_ms": p99, "psnr_db_vs_fp64": psnr_db,
-        "forms": {"fp32": {"frames_per_s": fps, "p99_ms": p99, "psnr_db": psnr_db}, "half2_batched": None},
+        "forms": {"batched": {"precision": args.precision, "frames_per_s": fps, "views_per_batch": ncam,
+                              "p50_batch_ms": p50, "p99_batch_ms": p99, "psnr_db": psnr_db,
+                              "stats": bstats},
+                  "plain": {"precision": args.plain_precision, "frames_per_s": fps_plain,
+                            "p50_ms": p50_plain, "p99_ms": p99_plain, "stages_ms": stage_ms_plain,
+                            "gpu_launches": launches_plain, "clocks": clocks_plain}},
         "e2e": {"value": e2e_fps, "unit": "frames/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "roofline": roofline,

@@ -161,10 +161,10 @@ typedef struct gs3d_resources {
   const uint32_t* sorted_gaussian_ids; /* active ordinal per sorted intersection */
   const uint32_t* tile_offsets;      /* tilesX*tilesY + 1 */
   const uint32_t* output_state;      /* uvec4: attempt, version, demand, overflow */
-  uint32_t active_count;
-  uint32_t tiles_x;
+  uint32_t active_count;  /* items of the last render (a batch pads each view to 256) */
+  uint32_t tiles_x;       /* prepared frame (single-view render) */
   uint32_t tiles_y;
-  uint32_t reserved;
+  uint32_t total_tiles;   /* tiles of the last render over all views */
   uint64_t intersection_capacity;
 } gs3d_resources;
 
@@ -194,6 +194,28 @@ gs3d_status gs3d_pipeline_prepare_frame(gs3d_pipeline* pipeline, uint32_t width,
  * whole pass on `stream`. NOT_PREPARED before prepare_frame. */
 gs3d_status gs3d_pipeline_render(gs3d_pipeline* pipeline, const gs3d_camera* camera, uint32_t attempt,
                                  int reset_valid, const gs3d_targets* targets, void* stream);
+/* One view of a batch: a scene, a camera, a size and its targets. */
+typedef struct gs3d_view {
+  const gs3d_gaussian_data* data;
+  const gs3d_camera* camera;
+  uint32_t width;
+  uint32_t height;
+  gs3d_targets targets;
+} gs3d_view;
+
+/* Batched rendering (an extension; the reference renders one camera per
+ * pass): every view runs through one launch sequence. Views are
+ * concatenated: view v owns items [item_base[v], item_base[v] + active) and
+ * global tile ids [tile_base[v], tile_base[v+1]); each view's tiles hold
+ * exactly the records, order and image a single-view render of that view
+ * produces. The batch shares one intersection workspace: on overflow no view
+ * is published and the output state reports the batch's demand. */
+gs3d_status gs3d_pipeline_render_batch(gs3d_pipeline* pipeline, const gs3d_view* views, uint32_t count,
+                                       uint32_t attempt, int reset_valid, void* stream);
+/* item_base/tile_base of the last render (count + 1 entries each). */
+gs3d_status gs3d_pipeline_batch_layout(gs3d_pipeline* pipeline, uint32_t* item_base, uint32_t* tile_base,
+                                       uint32_t capacity, uint32_t* count);
+
 /* readStats() (TiledGaussianPipeline.ts:353-366): synchronises the stream of
  * the last render. */
 gs3d_status gs3d_pipeline_read_stats(gs3d_pipeline* pipeline, gs3d_stats* stats);

@@ -50,7 +50,7 @@ class GpuRun:
                          color_format)
         stats = self.pipe.read_stats()
         r = self.pipe.get_resources()
-        n = int(r.active_count)
+        n = int(self.ds.active_count)
         out = {"stats": stats, "launches": self.pipe.last_launch_count()}
         vis = dev.to_numpy(r.visible_state, (4,))
         state = dev.to_numpy(r.dispatch_state, (4,))
@@ -70,6 +70,7 @@ class GpuRun:
         out["sorted_records"] = np.stack([dev.to_numpy(r.sorted_tile_ids, (cnt,)),
                                           dev.to_numpy(r.sorted_gaussian_ids, (cnt,))], 1)
         out["tile_offsets"] = dev.to_numpy(r.tile_offsets, (ntile + 1,))
+        assert int(r.total_tiles) == ntile
         out["rgba"] = color.float().cpu().numpy()
         out["depth"] = depth.cpu().numpy()
         return out
@@ -102,3 +103,62 @@ def assert_bit_exact(g: dict, o: dict, image: bool = True) -> None:
 def psnr(a: np.ndarray, b: np.ndarray) -> float:
     mse = float(np.mean((a.astype(np.float64) - b.astype(np.float64)) ** 2))
     return float("inf") if mse == 0 else 10.0 * np.log10(1.0 / mse)
+
+
+def render_batch(scenes_frames: list, precision: str = "exact", capacity: int = 1 << 22,
+                 color_format: str = "rgba32f") -> list:
+    """Render (scene, frame) pairs in one batch and split every buffer per view.
+
+    Each view's result uses the view's own ordinals and local tile ids, so it
+    compares directly with a single-view oracle render of that view."""
+    import torch
+    dss = [dev.DeviceScene(s) for s, _ in scenes_frames]
+    pipe = P.TiledGaussianPipeline(dss[0].data(), pipeline_options(scenes_frames[0][1], precision, capacity))
+    targets, views = [], []
+    for ds, (scene, frame) in zip(dss, scenes_frames):
+        W, H = int(frame["width"]), int(frame["height"])
+        dtype = torch.float16 if color_format == "rgba16f" else torch.float32
+        color = torch.zeros((H, W, 4), dtype=dtype, device="cuda")
+        depth = torch.zeros((H, W), dtype=torch.float32, device="cuda")
+        targets.append((color, depth))
+        views.append((ds.data(), P.make_camera(frame), W, H, color.data_ptr(), depth.data_ptr(), color_format))
+    pipe.render_batch(views)
+    stats = pipe.read_stats()
+    r = pipe.get_resources()
+    item_base, tile_base = pipe.batch_layout()
+    vis = dev.to_numpy(r.visible_state, (4,))
+    state = dev.to_numpy(r.dispatch_state, (4,))
+    V, cnt = int(vis[0]), int(state[0])
+    total_items, total_tiles = item_base[-1], tile_base[-1]
+    g = {
+        "proj_mean": dev.to_numpy(r.projected_mean, (total_items, 4), np.float32),
+        "proj_conic": dev.to_numpy(r.projected_conic, (total_items, 4), np.float32),
+        "proj_color": dev.to_numpy(r.projected_color, (total_items, 4), np.float32),
+        "tile_counts": dev.to_numpy(r.tile_counts, (total_items,)),
+        "visible_offsets": dev.to_numpy(r.visible_offsets, (total_items,)),
+        "depth_keys": dev.to_numpy(r.depth_sorted_keys, (V,)),
+        "depth_ids": dev.to_numpy(r.depth_sorted_ids, (V,)),
+        "ordered_counts": dev.to_numpy(r.depth_ordered_tile_counts, (V,)),
+        "tiles": dev.to_numpy(r.sorted_tile_ids, (cnt,)),
+        "gids": dev.to_numpy(r.sorted_gaussian_ids, (cnt,)),
+        "tile_offsets": dev.to_numpy(r.tile_offsets, (total_tiles + 1,)),
+    }
+    out = []
+    for i, (ds, (scene, frame)) in enumerate(zip(dss, scenes_frames)):
+        a, n = item_base[i], ds.active_count
+        t0, t1 = tile_base[i], tile_base[i + 1]
+        sel = (g["depth_ids"] >= a) & (g["depth_ids"] < a + n)
+        lo, hi = int(g["tile_offsets"][t0]), int(g["tile_offsets"][t1])
+        color, depth = targets[i]
+        out.append({
+            "proj_mean": g["proj_mean"][a:a + n], "proj_conic": g["proj_conic"][a:a + n],
+            "proj_color": g["proj_color"][a:a + n], "tile_counts": g["tile_counts"][a:a + n],
+            "visible_offsets": g["visible_offsets"][a:a + n] - g["visible_offsets"][a] if n else g["visible_offsets"][:0],
+            "depth_sorted": np.stack([g["depth_keys"][sel], g["depth_ids"][sel] - a], 1),
+            "ordered_counts": g["ordered_counts"][sel],
+            "sorted_records": np.stack([g["tiles"][lo:hi] - t0, g["gids"][lo:hi] - a], 1),
+            "tile_offsets": g["tile_offsets"][t0:t1 + 1] - lo,
+            "rgba": color.float().cpu().numpy(), "depth": depth.cpu().numpy(),
+        })
+    pipe.dispose()
+    return out, stats

@@ -192,3 +192,29 @@ def test_clustered_properties_at_scale():
     assert np.all(np.diff(ds[:, 0].astype(np.int64)) >= 0)
     vis = np.nonzero(g["tile_counts"])[0]
     assert np.array_equal(np.sort(ds[:, 1]), vis)
+
+
+def test_batched_views_match_single_view_renders():
+    # Three clouds, five cameras, mixed resolutions, one launch sequence.
+    from gpu_harness import render_batch
+    clouds = [cube(5000, seed=41), cube(3000, seed=42, log_scale=(-2.0, 0.5)),
+              sc.uniform_cloud(4000, seed=43, degree=1, log_scale=(-2.4, 0.6))]
+    frames = [cam(w=200, h=120), cam(eye=(3, 2, 9), w=97, h=64), cam(eye=(-4, 1, 10), w=160, h=96),
+              cam(eye=(0, 6, 8), w=33, h=17), cam(w=128, h=128)]
+    pairs = [(clouds[0], frames[0]), (clouds[1], frames[1]), (clouds[2], frames[2]), (clouds[0], frames[3]),
+             (clouds[1], frames[4])]
+    views, stats = render_batch(pairs, "exact")
+    for (scene, frame), g in zip(pairs, views):
+        o = oracle.render(scene, frame, 0)
+        vis = o["tile_counts"] > 0
+        assert np.array_equal(g["tile_counts"], o["tile_counts"])
+        assert np.array_equal(g["proj_mean"].view(np.uint32), o["proj_mean"].view(np.uint32))
+        assert np.array_equal(g["proj_conic"][vis].view(np.uint32), o["proj_conic"][vis].view(np.uint32))
+        assert np.array_equal(g["proj_color"][vis].view(np.uint32), o["proj_color"][vis].view(np.uint32))
+        assert np.array_equal(g["visible_offsets"], o["visible_offsets"])
+        assert np.array_equal(g["depth_sorted"], o["depth_sorted"])
+        assert np.array_equal(g["ordered_counts"], o["ordered_counts"])
+        assert np.array_equal(g["sorted_records"], o["sorted_records"])
+        assert np.array_equal(g["tile_offsets"], o["tile_offsets"])
+        assert np.array_equal(g["rgba"].view(np.uint32), o["rgba"].view(np.uint32))
+        assert np.array_equal(g["depth"].view(np.uint32), o["depth"].view(np.uint32))
