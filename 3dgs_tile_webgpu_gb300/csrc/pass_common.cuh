@@ -106,33 +106,85 @@ __device__ __forceinline__ unsigned long long pack_status(uint32_t epoch, unsign
 }
 __device__ __forceinline__ uint32_t sat_add(uint32_t a, uint32_t b) { return a + min(b, 0xffffffffu - a); }
 
-// Walk back from tile-1 summing published values until an inclusive prefix is
-// found. Bounded: after kSpinLimit polls of one word the wait is declared
-// expired, bit 0 of *err is set and the missing value counts as zero, so the
+// Wait (bounded) until *p carries this launch's epoch. On expiry the error
+// word gets bit 0 and the caller treats the word as an inclusive zero, so the
 // kernel always finishes and the host sees the error.
-template <bool SATURATE>
-__device__ __forceinline__ uint32_t lookback(const unsigned long long* status, uint32_t stride, uint32_t tile,
-                                             uint32_t epoch, uint32_t* err) {
-  uint32_t excl = 0;
-  int64_t t = (int64_t)tile - 1;
-  while (t >= 0) {
-    const unsigned long long* p = status + (size_t)t * stride;
-    unsigned long long v = ld_acquire(p);
-    uint32_t polls = 0;
-    uint32_t backoff = 8;
-    while ((uint32_t)(v >> 34) != epoch) {
-      if (++polls >= kSpinLimit) {
-        atomicOr(err, 1u);
-        return excl;
-      }
-      __nanosleep(backoff);
-      backoff = backoff < 256 ? backoff * 2 : 256;
-      v = ld_acquire(p);
+__device__ __forceinline__ unsigned long long wait_status(const unsigned long long* p, unsigned long long v,
+                                                          uint32_t epoch, uint32_t* err, bool* expired) {
+  uint32_t polls = 0, backoff = 8;
+  while ((uint32_t)(v >> 34) != epoch) {
+    if (++polls >= kSpinLimit) {
+      atomicOr(err, 1u);
+      *expired = true;
+      return 0;
     }
-    uint32_t val = (uint32_t)v;
-    excl = SATURATE ? sat_add(excl, val) : excl + val;
-    if (((v >> 32) & 3ull) == kFlagInclusive) break;
-    --t;
+    __nanosleep(backoff);
+    backoff = backoff < 256 ? backoff * 2 : 256;
+    v = ld_acquire(p);
+  }
+  return v;
+}
+
+// Warp-wide decoupled look-back for a single value per tile: every lane reads
+// one predecessor, so one round trip covers 32 tiles. Returns the exclusive
+// prefix of `tile` in every lane. All 32 lanes of the warp must call it.
+template <bool SATURATE>
+__device__ __forceinline__ uint32_t warp_lookback(const unsigned long long* status, uint32_t tile, uint32_t epoch,
+                                                  uint32_t* err) {
+  const uint32_t lane = threadIdx.x & 31u;
+  uint32_t excl = 0;
+  int64_t end = (int64_t)tile - 1;
+  while (end >= 0) {
+    const int64_t idx = end - (int64_t)lane;
+    bool incl = true, expired = false;
+    uint32_t val = 0;
+    if (idx >= 0) {
+      const unsigned long long* p = status + idx;
+      const unsigned long long v = wait_status(p, ld_acquire(p), epoch, err, &expired);
+      incl = expired || ((v >> 32) & 3ull) == kFlagInclusive;
+      val = expired ? 0u : (uint32_t)v;
+    }
+    const uint32_t inc_mask = __ballot_sync(0xffffffffu, incl);
+    const uint32_t stop = inc_mask ? (uint32_t)(__ffs(inc_mask) - 1) : 31u;  // nearest inclusive lane
+    uint32_t x = lane <= stop ? val : 0u;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const uint32_t y = __shfl_xor_sync(0xffffffffu, x, o);
+      x = SATURATE ? sat_add(x, y) : x + y;
+    }
+    excl = SATURATE ? sat_add(excl, x) : excl + x;
+    if (inc_mask) break;
+    end -= 32;
+  }
+  return excl;
+}
+
+// Per-thread decoupled look-back over a strided status column (one radix
+// digit): W predecessor words are requested at once, so one round trip
+// covers W tiles.
+template <int W>
+__device__ __forceinline__ uint32_t window_lookback(const unsigned long long* column, uint32_t stride, uint32_t tile,
+                                                    uint32_t epoch, uint32_t* err) {
+  uint32_t excl = 0;
+  int64_t end = (int64_t)tile - 1;
+  while (end >= 0) {
+    unsigned long long v[W];
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+      const int64_t idx = end - w;
+      v[w] = idx >= 0 ? ld_acquire(column + (size_t)idx * stride) : 0ull;
+    }
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+      const int64_t idx = end - w;
+      if (idx < 0) return excl;
+      bool expired = false;
+      const unsigned long long x = wait_status(column + (size_t)idx * stride, v[w], epoch, err, &expired);
+      if (expired) return excl;
+      excl += (uint32_t)x;
+      if (((x >> 32) & 3ull) == kFlagInclusive) return excl;
+    }
+    end -= W;
   }
   return excl;
 }

@@ -152,8 +152,8 @@ void launch_project(const BatchView& b, const PassOptions& o, float4* mean, floa
 // Visibility compaction (scan.ts:9-83 + visibility.ts:9-61): one pass with
 // decoupled look-back. Writes visibleOffsets, the (depthKey, ordinal) records
 // in ordinal order, the visible state, and the depth sort's digit histograms.
-constexpr uint32_t kItems = 4;
-constexpr uint32_t kScanTile = kBlock * kItems;  // 1024 items per tile
+constexpr uint32_t kItems = 8;
+constexpr uint32_t kScanTile = kBlock * kItems;  // 2048 items per tile
 
 __global__ void __launch_bounds__(kBlock) k_compact(const uint32_t* __restrict__ keys, uint32_t n,
                                                     uint32_t* __restrict__ vis_off, uint32_t* __restrict__ keys_out,
@@ -173,8 +173,11 @@ __global__ void __launch_bounds__(kBlock) k_compact(const uint32_t* __restrict__
   const uint32_t base = tile * kScanTile + tid * kItems;
   uint32_t k[kItems];
   if (base + kItems <= n) {
-    uint4 w = *reinterpret_cast<const uint4*>(keys + base);
-    k[0] = w.x; k[1] = w.y; k[2] = w.z; k[3] = w.w;
+#pragma unroll
+    for (uint32_t q = 0; q < kItems / 4; ++q) {
+      const uint4 w = *reinterpret_cast<const uint4*>(keys + base + 4 * q);
+      k[4 * q] = w.x; k[4 * q + 1] = w.y; k[4 * q + 2] = w.z; k[4 * q + 3] = w.w;
+    }
   } else {
 #pragma unroll
     for (uint32_t i = 0; i < kItems; ++i) k[i] = base + i < n ? keys[base + i] : kInvisibleKey;
@@ -184,18 +187,18 @@ __global__ void __launch_bounds__(kBlock) k_compact(const uint32_t* __restrict__
   for (uint32_t i = 0; i < kItems; ++i) c += k[i] != kInvisibleKey ? 1u : 0u;
   uint32_t total;
   const uint32_t excl = block_exclusive_scan<false>(c, s_warp, &total);
-  if (tid == 0) {
+  if (tid < 32) {
     unsigned long long* mine = status + tile;
     uint32_t prefix = 0;
     if (tile == 0) {
-      st_release(mine, pack_status(epoch, kFlagInclusive, total));
+      if (tid == 0) st_release(mine, pack_status(epoch, kFlagInclusive, total));
     } else {
-      st_release(mine, pack_status(epoch, kFlagAggregate, total));
-      prefix = lookback<false>(status, 1, tile, epoch, &ctl->error);
-      st_release(mine, pack_status(epoch, kFlagInclusive, prefix + total));
+      if (tid == 0) st_release(mine, pack_status(epoch, kFlagAggregate, total));
+      prefix = warp_lookback<false>(status, tile, epoch, &ctl->error);
+      if (tid == 0) st_release(mine, pack_status(epoch, kFlagInclusive, prefix + total));
     }
-    s_prefix = prefix;
-    if (tile == ntiles - 1) {
+    if (tid == 0) s_prefix = prefix;
+    if (tid == 0 && tile == ntiles - 1) {
       const uint32_t v = prefix + total;
       ctl->visible_state[0] = v;
       ctl->visible_state[1] = v;
@@ -258,18 +261,18 @@ __global__ void __launch_bounds__(kBlock) k_scan_counts(const uint32_t* __restri
   for (uint32_t i = 0; i < kItems; ++i) sum = sat_add(sum, c[i]);
   uint32_t total;
   const uint32_t excl = block_exclusive_scan<true>(sum, s_warp, &total);
-  if (tid == 0) {
+  if (tid < 32) {
     unsigned long long* mine = status + tile;
     uint32_t prefix = 0;
     if (tile == 0) {
-      st_release(mine, pack_status(epoch, kFlagInclusive, total));
+      if (tid == 0) st_release(mine, pack_status(epoch, kFlagInclusive, total));
     } else {
-      st_release(mine, pack_status(epoch, kFlagAggregate, total));
-      prefix = lookback<true>(status, 1, tile, epoch, &ctl->error);
-      st_release(mine, pack_status(epoch, kFlagInclusive, sat_add(prefix, total)));
+      if (tid == 0) st_release(mine, pack_status(epoch, kFlagAggregate, total));
+      prefix = warp_lookback<true>(status, tile, epoch, &ctl->error);
+      if (tid == 0) st_release(mine, pack_status(epoch, kFlagInclusive, sat_add(prefix, total)));
     }
-    s_prefix = prefix;
-    if (tile == ntiles - 1) {
+    if (tid == 0) s_prefix = prefix;
+    if (tid == 0 && tile == ntiles - 1) {
       const uint32_t all = sat_add(prefix, total);
       const bool overflow = all > capacity;
       const uint32_t count = overflow ? 0u : all;

@@ -10,9 +10,10 @@
 // by the kernel that produced the keys, so each block only:
 //   1. takes the next tile id from an atomic ticket (tiles are processed in
 //      launch order, which keeps the look-back deadlock-free);
-//   2. ranks its 4096 keys per digit with __match_any_sync (warp-striped
-//      layout: item j*32+lane of each warp's 512-item segment, so ranks follow
-//      index order and the sort is stable);
+//   2. ranks its 4096 keys per digit within each warp by ballot bit-splitting
+//      (warp-striped layout: item j*32+lane of each warp's 512-item segment,
+//      so ranks follow index order and the sort is stable), while the values
+//      stream into shared memory with cp.async;
 //   3. publishes its per-digit counts and resolves its global per-digit base
 //      with decoupled look-back (one thread per digit, bounded waits);
 //   4. stages keys and values in shared memory in block-sorted order and
@@ -27,21 +28,44 @@ namespace gs {
 constexpr int kSortWarps = 8;
 constexpr int kSortItems = 16;  // kSortTile = 8 warps * 32 lanes * 16 items
 
+// Lanes of the warp holding the same BITS-bit digit, by ballot bit-splitting.
 template <int BITS>
-__global__ void __launch_bounds__(kBlock, 2)
+__device__ __forceinline__ uint32_t match_digit(uint32_t d, uint32_t valid_mask) {
+  uint32_t peers = valid_mask;
+#pragma unroll
+  for (int b = 0; b < BITS; ++b) {
+    const bool bit = (d >> b) & 1u;
+    const uint32_t bal = __ballot_sync(0xffffffffu, bit);
+    peers &= bit ? bal : ~bal;
+  }
+  return peers;
+}
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const uint32_t s = (uint32_t)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit_wait() {
+  asm volatile("cp.async.commit_group;" ::: "memory");
+  asm volatile("cp.async.wait_all;" ::: "memory");
+}
+
+template <int BITS>
+__global__ void __launch_bounds__(kBlock, 3)
     k_onesweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
                uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, const uint32_t* __restrict__ n_ptr,
                int shift, const uint32_t* __restrict__ hist, unsigned long long* __restrict__ status,
                uint32_t* __restrict__ ticket, uint32_t epoch, uint32_t* __restrict__ err) {
   constexpr uint32_t RADIX = 1u << BITS;
   constexpr uint32_t MASK = RADIX - 1u;
-  constexpr uint32_t INVALID = 0xffffu;
   __shared__ uint32_t s_warp_hist[kSortWarps][RADIX];
   __shared__ uint32_t s_block_excl[RADIX];
   __shared__ uint32_t s_global_base[RADIX];
   __shared__ uint32_t s_hist_excl[RADIX];
-  __shared__ uint32_t s_keys[kSortTile];
-  __shared__ uint32_t s_vals[kSortTile];
+  extern __shared__ uint4 s_dyn[];  // keys, values, raw values: 3 x kSortTile words
+  uint32_t* s_keys = reinterpret_cast<uint32_t*>(s_dyn);
+  uint32_t* s_vals = s_keys + kSortTile;
+  uint32_t* s_vraw = s_vals + kSortTile;
   __shared__ uint32_t s_scan[kBlock / 32];
   __shared__ uint32_t s_tile;
 
@@ -53,43 +77,56 @@ __global__ void __launch_bounds__(kBlock, 2)
   const uint32_t tile = s_tile;
   const uint32_t base = tile * kSortTile;
   if (base >= n) return;
+  const uint32_t wbase = base + warp * 32u * kSortItems;
+
+  // Keys into registers (warp-striped: item j*32+lane of the warp's
+  // segment); values into shared memory asynchronously, in the same order.
+  uint32_t k[kSortItems];
+#pragma unroll
+  for (int j = 0; j < kSortItems; ++j) {
+    const uint32_t idx = wbase + (uint32_t)j * 32u + lane;
+    k[j] = idx < n ? keys_in[idx] : 0u;
+  }
+  uint32_t* vraw = s_vraw + warp * 32u * kSortItems;
+  for (uint32_t c = lane; c < 8u * kSortItems; c += 32u) {
+    const uint32_t first = wbase + 4u * c;
+    if (first + 4u <= n) {
+      cp_async16(vraw + 4u * c, vals_in + first);
+    } else {
+      for (uint32_t e = 0; e < 4u; ++e)
+        if (first + e < n) vraw[4u * c + e] = vals_in[first + e];
+    }
+  }
 
   // Exclusive scan of the pass's global digit histogram.
   {
-    uint32_t h = tid < RADIX ? hist[tid] : 0u;
+    const uint32_t h = tid < RADIX ? hist[tid] : 0u;
     uint32_t tot;
-    uint32_t e = block_exclusive_scan<false>(h, s_scan, &tot);
+    const uint32_t e = block_exclusive_scan<false>(h, s_scan, &tot);
     if (tid < RADIX) s_hist_excl[tid] = e;
   }
 
-  // Load (warp-striped) and rank.
-  const uint32_t wbase = base + warp * 32u * kSortItems;
-  uint32_t k[kSortItems], v[kSortItems], rank[kSortItems];
-  uint32_t d[kSortItems];
+  // Rank: position among equal digits of this warp, in index order.
+  const uint32_t lt = (1u << lane) - 1u;
+  uint32_t rank[kSortItems];
 #pragma unroll
   for (int j = 0; j < kSortItems; ++j) {
     const uint32_t idx = wbase + (uint32_t)j * 32u + lane;
     const bool ok = idx < n;
-    k[j] = ok ? keys_in[idx] : 0u;
-    v[j] = ok ? vals_in[idx] : 0u;
-    d[j] = ok ? (k[j] >> shift) & MASK : INVALID;
-  }
-  const uint32_t lt = (1u << lane) - 1u;
-#pragma unroll
-  for (int j = 0; j < kSortItems; ++j) {
-    const uint32_t peers = __match_any_sync(0xffffffffu, d[j]);
-    const uint32_t leader = __ffs(peers) - 1u;
+    const uint32_t valid = __ballot_sync(0xffffffffu, ok);
+    const uint32_t d = (k[j] >> shift) & MASK;
+    const uint32_t peers = match_digit<BITS>(d, valid);
     const uint32_t before = __popc(peers & lt);
     uint32_t cnt = 0;
-    if (d[j] != INVALID) cnt = s_warp_hist[warp][d[j]];
+    if (ok) cnt = s_warp_hist[warp][d];
     rank[j] = cnt + before;
     __syncwarp();
-    if (lane == leader && d[j] != INVALID) s_warp_hist[warp][d[j]] = cnt + __popc(peers);
+    if (ok && before == 0) s_warp_hist[warp][d] = cnt + __popc(peers);
     __syncwarp();
   }
   __syncthreads();
 
-  // Per digit: exclusive offsets across warps and the block count.
+  // Per digit: exclusive offsets across warps and the block count; publish.
   uint32_t block_count = 0;
   if (tid < RADIX) {
 #pragma unroll
@@ -109,20 +146,23 @@ __global__ void __launch_bounds__(kBlock, 2)
   if (tid < RADIX) {
     uint32_t prefix = 0;
     if (tile > 0) {
-      prefix = lookback<false>(status + tid, RADIX, tile, epoch, err);
+      prefix = window_lookback<8>(status + tid, RADIX, tile, epoch, err);
       st_release(status + (size_t)tile * RADIX + tid, pack_status(epoch, kFlagInclusive, prefix + block_count));
     }
     s_global_base[tid] = s_hist_excl[tid] + prefix;
   }
+  cp_async_commit_wait();
   __syncthreads();
 
-  // Stage in block-sorted order.
+  // Stage keys and values in block-sorted order.
 #pragma unroll
   for (int j = 0; j < kSortItems; ++j) {
-    if (d[j] != INVALID) {
-      const uint32_t pos = s_block_excl[d[j]] + s_warp_hist[warp][d[j]] + rank[j];
+    const uint32_t idx = wbase + (uint32_t)j * 32u + lane;
+    if (idx < n) {
+      const uint32_t d = (k[j] >> shift) & MASK;
+      const uint32_t pos = s_block_excl[d] + s_warp_hist[warp][d] + rank[j];
       s_keys[pos] = k[j];
-      s_vals[pos] = v[j];
+      s_vals[pos] = vraw[(uint32_t)j * 32u + lane];
     }
   }
   __syncthreads();
@@ -138,14 +178,31 @@ __global__ void __launch_bounds__(kBlock, 2)
   }
 }
 
+constexpr size_t kSortDynSmem = 3 * kSortTile * sizeof(uint32_t);
+
+template <int B>
+void launch_bits(uint32_t grid, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
+                 uint32_t* vals_out, const uint32_t* n_ptr, int shift, const uint32_t* hist,
+                 unsigned long long* status, uint32_t* ticket, uint32_t epoch, uint32_t* err, cudaStream_t st) {
+  static bool configured[64] = {};  // opt-in to >48 KB shared memory, once per device
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64 || !configured[dev]) {
+    cudaFuncSetAttribute(k_onesweep<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSortDynSmem);
+    if (dev >= 0 && dev < 64) configured[dev] = true;
+  }
+  k_onesweep<B><<<grid, kBlock, kSortDynSmem, st>>>(keys_in, vals_in, keys_out, vals_out, n_ptr, shift, hist, status,
+                                                    ticket, epoch, err);
+}
+
 void launch_onesweep(int bits, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
                      uint32_t* vals_out, const uint32_t* n_ptr, uint32_t n_max, int shift, const uint32_t* hist,
                      unsigned long long* status, uint32_t* ticket, uint32_t epoch, uint32_t* err, cudaStream_t st) {
   const uint32_t grid = n_max == 0 ? 1u : (uint32_t)(((uint64_t)n_max + kSortTile - 1) / kSortTile);
-#define GS_SWEEP(B)                                                                                         \
-  case B:                                                                                                   \
-    k_onesweep<B><<<grid, kBlock, 0, st>>>(keys_in, vals_in, keys_out, vals_out, n_ptr, shift, hist, status, \
-                                           ticket, epoch, err);                                             \
+#define GS_SWEEP(B)                                                                                      \
+  case B:                                                                                                \
+    launch_bits<B>(grid, keys_in, vals_in, keys_out, vals_out, n_ptr, shift, hist, status, ticket, epoch, \
+                   err, st);                                                                             \
     break;
   switch (bits) {
     GS_SWEEP(1)
