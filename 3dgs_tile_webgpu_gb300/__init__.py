@@ -85,7 +85,7 @@ def default_options() -> dict:
         "subpixel_sample_culling": True, "raster_transmittance_threshold": 1e-4,
         "depth_alpha_threshold": 0.95, "filter_variance": 0.3, "invalid_depth_value": 1.0,
         "boundary_policy": "clip", "raster_precision": "fp32", "depth_encoding": "device",
-        "device": 0,
+        "raster_stats": False, "device": 0,
     }
 
 
@@ -110,6 +110,7 @@ def make_desc(options: dict | None = None) -> PipelineDesc:
     d.boundary_policy = {"clip": 0, "repeat-x": 1, "repeat-y": 2}[o["boundary_policy"]]
     d.raster_precision = {"fp32": 0, "exact": 1, "half2": 2}[o["raster_precision"]]
     d.depth_encoding = {"device": 0, "raw": 1}[o["depth_encoding"]]
+    d.raster_stats = 1 if o["raster_stats"] else 0
     return d
 
 
@@ -207,7 +208,9 @@ class TiledGaussianPipeline:
         out = {"visibleGaussianCount": s.visible_gaussian_count, "intersectionCount": s.intersection_count,
                "requestedIntersections": s.requested_intersections,
                "intersectionCapacity": int(s.intersection_capacity), "overflow": bool(s.overflow),
-               "deviceError": int(s.device_error)}
+               "deviceError": int(s.device_error),
+               "rasterWork": {"checked": int(s.raster_checked), "blended": int(s.raster_blended),
+                              "pixels": int(s.raster_pixels), "alphaStopped": int(s.raster_alpha_stopped)}}
         _raise(self._lib, st, self._p)
         return out
 

@@ -32,7 +32,7 @@ class PipelineDesc(C.Structure):
                 ("raster_transmittance_threshold", C.c_float), ("depth_alpha_threshold", C.c_float),
                 ("filter_variance", C.c_float), ("invalid_depth_value", C.c_float),
                 ("boundary_policy", C.c_uint32), ("raster_precision", C.c_uint32),
-                ("depth_encoding", C.c_uint32)]
+                ("depth_encoding", C.c_uint32), ("raster_stats", C.c_uint32)]
 
 
 class Camera(C.Structure):
@@ -54,7 +54,9 @@ class View(C.Structure):
 class Stats(C.Structure):
     _fields_ = [("visible_gaussian_count", C.c_uint32), ("intersection_count", C.c_uint32),
                 ("requested_intersections", C.c_uint32), ("overflow", C.c_uint32),
-                ("intersection_capacity", C.c_uint64), ("device_error", C.c_uint32), ("reserved", C.c_uint32)]
+                ("intersection_capacity", C.c_uint64), ("device_error", C.c_uint32), ("reserved", C.c_uint32),
+                ("raster_checked", C.c_uint64), ("raster_blended", C.c_uint64), ("raster_pixels", C.c_uint64),
+                ("raster_alpha_stopped", C.c_uint64)]
 
 
 class Resources(C.Structure):

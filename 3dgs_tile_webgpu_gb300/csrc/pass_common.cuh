@@ -81,6 +81,9 @@ struct Control {
   uint32_t state[4];             // count, total, radix blocks, overflow
   uint32_t error;                // bit 0: look-back wait expired
   uint32_t pad[3];
+  unsigned long long raster_stats[4];  // checked, blended, pixels, alpha-stopped
+  uint32_t order_hist[34];       // raster work-list buckets (tile load classes)
+  uint32_t order_fill[34];
 };
 
 enum Ticket { kTicketCompact = 0, kTicketScan = 1, kTicketSortBase = 2 };
@@ -243,12 +246,15 @@ void launch_onesweep(int bits, const uint32_t* keys_in, const uint32_t* vals_in,
                      uint32_t* vals_out, const uint32_t* n_ptr, uint32_t n_max, int shift, const uint32_t* hist,
                      unsigned long long* status, uint32_t* ticket, uint32_t epoch, uint32_t* err, cudaStream_t st);
 constexpr uint32_t kSortTile = 4096;  // items per onesweep block
-// Rasterizer over every tile of the batch (precision: 0 fp32, 1 exact, 2 half2).
-void launch_raster(int precision, const uint32_t* tile_offsets, const uint32_t* sorted_ids, const float4* mean,
-                   const float4* conic, const float4* color, const BatchView& b, const PassOptions& o,
-                   const Control* ctl, cudaStream_t st);
-void launch_raster_exact(const uint32_t* tile_offsets, const uint32_t* sorted_ids, const float4* mean,
-                         const float4* conic, const float4* color, const BatchView& b, const PassOptions& o,
-                         const Control* ctl, cudaStream_t st);
+// Raster work list: every tile of the batch, heaviest load class first.
+void launch_tile_order(const uint32_t* tile_offsets, uint32_t ntile, Control* ctl, uint32_t* order, int sms,
+                       cudaStream_t st);
+// Rasterizer over every tile of the batch (precision: 0 fp32, 1 exact).
+void launch_raster(int precision, const uint32_t* tile_offsets, const uint32_t* order, const uint32_t* sorted_ids,
+                   const float4* mean, const float4* conic, const float4* color, const BatchView& b,
+                   const PassOptions& o, Control* ctl, bool stats, cudaStream_t st);
+void launch_raster_exact(const uint32_t* tile_offsets, const uint32_t* order, const uint32_t* sorted_ids,
+                         const float4* mean, const float4* conic, const float4* color, const BatchView& b,
+                         const PassOptions& o, Control* ctl, bool stats, cudaStream_t st);
 
 }  // namespace gs

@@ -410,11 +410,10 @@ void launch_tile_ranges(const uint32_t* keys, Control* ctl, uint32_t ntile, uint
 }
 
 // ---------------------------------------------------------------------------
-void launch_raster_exact(const uint32_t* tile_offsets, const uint32_t* ids, const float4* mean, const float4* conic,
-                         const float4* color, const BatchView& b, const PassOptions& o, const Control* ctl,
-                         cudaStream_t st) {
-  if (b.total_tiles == 0) return;
-  k_raster<ExactMath><<<b.total_tiles, kBlock, 0, st>>>(tile_offsets, ids, mean, conic, color, b, o, ctl);
+void launch_raster_exact(const uint32_t* tile_offsets, const uint32_t* order, const uint32_t* ids,
+                         const float4* mean, const float4* conic, const float4* color, const BatchView& b,
+                         const PassOptions& o, Control* ctl, bool stats, cudaStream_t st) {
+  launch_raster_policy<ExactMath>(tile_offsets, order, ids, mean, conic, color, b, o, ctl, stats, st);
 }
 
 }  // namespace gs

@@ -55,6 +55,7 @@ struct gs3d_pipeline {
   // Tiles.
   uint32_t tile_cap = 0;
   uint32_t* tile_offsets = nullptr;
+  uint32_t* tile_order = nullptr;
   // Control, output state, look-back status.
   Control* ctl = nullptr;
   uint32_t* output_state = nullptr;
@@ -127,6 +128,7 @@ gs3d_status validate_desc(gs3d_pipeline* p, const gs3d_pipeline_desc& d) {
   if (d.boundary_policy > 2) return fail(p, GS3D_ERROR_INVALID_ARGUMENT, "boundaryPolicy must be clip, repeat-x or repeat-y");
   if (d.raster_precision > 2) return fail(p, GS3D_ERROR_INVALID_ARGUMENT, "unknown raster precision");
   if (d.depth_encoding > 1) return fail(p, GS3D_ERROR_INVALID_ARGUMENT, "unknown depth encoding");
+  if (d.raster_precision == GS3D_RASTER_HALF2) return fail(p, GS3D_ERROR_UNSUPPORTED, "half2 raster not built");
   // GaussianPass.ts:178-192,231-255
   if (d.intersection_capacity == 0 || d.intersection_capacity > 0x7fffffffull)
     return fail(p, GS3D_ERROR_RANGE, "intersectionCapacity must be a positive integer below 2^31");
@@ -222,6 +224,24 @@ gs3d_status ensure_stage(gs3d_pipeline* p, size_t bytes) {
   return GS3D_OK;
 }
 
+// Tile offsets (tiles + 1 words) and the raster work list (tiles words), grown
+// together to the next power of two (TiledGaussianPipeline.ts:306-318).
+gs3d_status ensure_tiles(gs3d_pipeline* p, uint64_t tiles) {
+  if (tiles + 1 <= p->tile_cap && p->tile_offsets && p->tile_order) return GS3D_OK;
+  if (p->last_stream) cudaStreamSynchronize(p->last_stream);
+  uint64_t cap = 1;
+  while (cap < tiles + 1) cap <<= 1;
+  cudaError_t e = dalloc(p->tile_offsets, cap);
+  if (e == cudaSuccess) e = dalloc(p->tile_order, cap);
+  if (e != cudaSuccess) {
+    p->tile_cap = 0;
+    return cuda_fail(p, e, "allocating tile offsets");
+  }
+  cudaMemset(p->tile_offsets, 0, (size_t)cap * sizeof(uint32_t));
+  p->tile_cap = (uint32_t)cap;
+  return GS3D_OK;
+}
+
 uint32_t next_epoch(gs3d_pipeline* p, cudaStream_t st) {
   p->epoch = (p->epoch + 1u) & kEpochMask;
   if (p->epoch == 0) {
@@ -257,7 +277,7 @@ void release_all(gs3d_pipeline* p) {
   dfree(p->mean); dfree(p->conic); dfree(p->color); dfree(p->counts); dfree(p->keys); dfree(p->vis_off);
   dfree(p->dk[0]); dfree(p->dk[1]); dfree(p->dv[0]); dfree(p->dv[1]); dfree(p->ordered); dfree(p->ioff);
   dfree(p->tk[0]); dfree(p->tk[1]); dfree(p->tv[0]); dfree(p->tv[1]);
-  dfree(p->tile_offsets); dfree(p->ctl); dfree(p->output_state); dfree(p->status);
+  dfree(p->tile_offsets); dfree(p->tile_order); dfree(p->ctl); dfree(p->output_state); dfree(p->status);
 }
 
 }  // namespace
@@ -310,10 +330,6 @@ gs3d_status gs3d_pipeline_create(const gs3d_pipeline_desc* desc, const gs3d_gaus
   if ((s = validate_desc(p, *desc)) != GS3D_OK || (s = validate_data(p, data)) != GS3D_OK) {
     delete p;
     return s;
-  }
-  if (desc->raster_precision == GS3D_RASTER_HALF2) {
-    delete p;
-    return GS3D_ERROR_UNSUPPORTED;
   }
   p->desc = *desc;
   p->data = *data;
@@ -379,16 +395,8 @@ gs3d_status gs3d_pipeline_prepare_frame(gs3d_pipeline* p, uint32_t width, uint32
   if (tx > 65535u || ty > 65535u) return fail(p, GS3D_ERROR_RANGE, "Render size exceeds WebGPU's tile dispatch limit");
   cudaSetDevice(p->device);
   const uint32_t ntile = tx * ty;
-  if (ntile + 1 > p->tile_cap) {
-    if (p->last_stream) cudaStreamSynchronize(p->last_stream);
-    // tile capacity grows to the next power of two (TiledGaussianPipeline.ts:306-318)
-    uint32_t cap = 1;
-    while (cap < ntile + 1) cap <<= 1;
-    cudaError_t e = dalloc(p->tile_offsets, cap);
-    if (e != cudaSuccess) return cuda_fail(p, e, "allocating tile offsets");
-    cudaMemset(p->tile_offsets, 0, (size_t)cap * sizeof(uint32_t));
-    p->tile_cap = cap;
-  }
+  gs3d_status s = ensure_tiles(p, ntile);
+  if (s != GS3D_OK) return s;
   p->width = width;
   p->height = height;
   p->tiles_x = tx;
@@ -441,14 +449,7 @@ gs3d_status enqueue(gs3d_pipeline* p, const gs3d_view* views, uint32_t n, uint32
   gs3d_status s = ensure_slots(p, (uint32_t)items);
   if (s != GS3D_OK) return s;
   if ((s = ensure_status(p)) != GS3D_OK) return s;
-  if (tiles + 1 > p->tile_cap) {
-    uint32_t cap = 1;
-    while (cap < tiles + 1) cap <<= 1;
-    cudaError_t e = dalloc(p->tile_offsets, cap);
-    if (e != cudaSuccess) return cuda_fail(p, e, "allocating tile offsets");
-    cudaMemset(p->tile_offsets, 0, (size_t)cap * sizeof(uint32_t));
-    p->tile_cap = cap;
-  }
+  if ((s = ensure_tiles(p, tiles)) != GS3D_OK) return s;
 
   // Batch table: bases, view descriptors, object tables; one H2D copy.
   const size_t bases_bytes = align16(3 * (size_t)(n + 1) * sizeof(uint32_t));
@@ -598,10 +599,12 @@ gs3d_status enqueue(gs3d_pipeline* p, const gs3d_view* views, uint32_t n, uint32
   mark(p, GS3D_STAGE_RANGES, st);
   launch_tile_ranges(p->tk[tcur], ctl, tile, p->tile_offsets, p->sms, st);
   ++launches;
+  launch_tile_order(p->tile_offsets, tile, ctl, p->tile_order, p->sms, st);
+  launches += 2;
   // Raster.
   mark(p, GS3D_STAGE_RASTER, st);
-  launch_raster((int)p->desc.raster_precision, p->tile_offsets, p->tv[tcur], p->mean, p->conic, p->color, bv, o, ctl,
-                st);
+  launch_raster((int)p->desc.raster_precision, p->tile_offsets, p->tile_order, p->tv[tcur], p->mean, p->conic,
+                p->color, bv, o, ctl, p->desc.raster_stats != 0, st);
   ++launches;
 
   mark(p, GS3D_STAGE_COUNT, st);
@@ -670,6 +673,10 @@ gs3d_status gs3d_pipeline_read_stats(gs3d_pipeline* p, gs3d_stats* out) {
   out->overflow = c.state[3];
   out->intersection_capacity = p->capacity;
   out->device_error = c.error;
+  out->raster_checked = c.raster_stats[0];
+  out->raster_blended = c.raster_stats[1];
+  out->raster_pixels = c.raster_stats[2];
+  out->raster_alpha_stopped = c.raster_stats[3];
   if (c.error) return fail(p, GS3D_ERROR_DEVICE_TIMEOUT, "a device-side look-back wait expired");
   return GS3D_OK;
 }

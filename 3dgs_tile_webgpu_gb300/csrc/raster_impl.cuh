@@ -4,16 +4,17 @@
 //
 // One 256-thread block per 16x16 tile, one pixel per thread, lanes mapped to
 // pixels in the reference's compact Morton order (rasterHelpers.ts:3-12), so
-// warp w owns an 8x4 patch of the tile. Each batch of 256 sorted records is
-// gathered into shared memory once. While staging, the thread that loads a
-// record also tests the splat's support box against the eight warp patches
-// and stores an 8-bit mask; each warp then walks only the records whose bit
-// is set (ballot + find-first-set, ascending, so front-to-back order holds).
-// The culling is conservative: a skipped (pixel, splat) pair is one where the
-// per-pixel test `power < -threshold` would reject the splat anyway, so the
-// result is unchanged, bit for bit. The block leaves the tile when no pixel
-// is still accumulating (__syncthreads_or), a warp leaves a batch when all
-// its pixels are done (__all_sync).
+// warp w owns an 8x4 patch of the tile. Blocks take tiles from a work list
+// ordered heaviest first, so long tiles start early and do not form a tail.
+// Each batch of 256 sorted records is gathered into shared memory once.
+// While staging, the thread that loads a record also tests the splat's
+// support box against the eight warp patches and stores an 8-bit mask; each
+// warp then walks only the records whose bit is set (ballot + find-first-set,
+// ascending, so front-to-back order holds). The culling is conservative: a
+// skipped (pixel, splat) pair is one where the per-pixel test rejects the
+// splat anyway, so the result is unchanged. The block leaves the tile when no
+// pixel is still accumulating (__syncthreads_or), a warp leaves a batch when
+// all its pixels are done (__all_sync).
 //
 // Tiles holding more than `chunk` samples are evaluated as the reference's
 // exact chunks: every chunk starts at transmittance 1 and its partial
@@ -22,9 +23,14 @@
 // transmittance falls below the threshold, which yields exactly the composite
 // of the reference's parallel chunk tasks.
 //
-// The MATH policy supplies exp/log: deterministic (bit-identical to the CPU
-// restatement when the translation unit is built with --fmad=false) or the
-// hardware fast path.
+// Two arithmetic policies:
+//  * ExactMath: the reference's expressions and tests in their order, with the
+//    deterministic exp/log; bit-identical to the CPU restatement when the
+//    translation unit is built with --fmad=false.
+//  * FastMath: staging folds -1/2 and log2(e) into the conic so one fused
+//    quadratic gives the exponent in base 2, one compare rejects splats below
+//    the 1/255 threshold before the exponential (ex2.approx), and
+//    transmittance is updated as T - T*alpha.
 #pragma once
 
 #include <cuda_fp16.h>
@@ -34,14 +40,24 @@
 
 namespace gs {
 
+constexpr float kLog2e = 1.4426950408889634f;
+
 struct ExactMath {
+  static constexpr bool kExact = true;
   static __device__ __forceinline__ float exp(float x) { return gsdm::expf_(x); }
   static __device__ __forceinline__ float log(float x) { return gsdm::logf_(x); }
 };
 struct FastMath {
+  static constexpr bool kExact = false;
   static __device__ __forceinline__ float exp(float x) { return __expf(x); }
   static __device__ __forceinline__ float log(float x) { return __logf(x); }
 };
+
+__device__ __forceinline__ float ex2_approx(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
 
 __device__ __forceinline__ uint32_t morton_compact(uint32_t v) {
   uint32_t r = v & 0x55555555u;
@@ -64,9 +80,10 @@ struct RasterFrame {
 };
 
 // tileContribution.ts:66-82 gaussian_boundary_delta.
+template <bool PERIODIC>
 __device__ __forceinline__ void boundary_delta(float pxc, float pyc, float cx, float cy, float ca, float cb,
                                                float cc, const RasterFrame& f, float* dx, float* dy) {
-  if (f.axis == 0u) {
+  if (!PERIODIC) {
     *dx = pxc - cx;
     *dy = pyc - cy;
     return;
@@ -90,12 +107,15 @@ struct PixelAcc {
   float r, g, b, t, d;
 };
 
-// Shared batch: geometry (cx, cy, opacity, threshold), conic (a, b, c, depth),
-// colour, and the warp-patch mask.
+// Shared batch. Exact form: geo = (cx, cy, opacity, threshold), con = (a, b, c,
+// depth). Fast form: geo = (cx, cy, opacity, threshold * log2 e),
+// con = (-a/2 log2 e, -b log2 e, -c/2 log2 e, depth), with the conic of the
+// periodic form kept as (a, b, c) in raw[].
 struct Batch {
   float4 geo[kBlock];
   float4 con[kBlock];
   float4 col[kBlock];
+  float4 raw[kBlock];
   uint8_t mask[kBlock];
 };
 
@@ -127,36 +147,65 @@ __device__ __forceinline__ uint32_t patch_mask(float cx, float cy, float ca, flo
 }
 
 // One (pixel, splat) step of the front-to-back blend (TileRasterizer.ts:616-707).
-template <class M>
+// Returns true when the pixel is done (transmittance below the threshold).
+template <class M, bool PERIODIC>
 __device__ __forceinline__ bool blend_one(const Batch& sb, uint32_t j, float pxc, float pyc, const RasterFrame& f,
-                                          PixelAcc& a) {
+                                          PixelAcc& a, uint32_t* blended) {
   const float4 g = sb.geo[j];
   const float4 c = sb.con[j];
-  float dx, dy;
-  boundary_delta(pxc, pyc, g.x, g.y, c.x, c.y, c.z, f, &dx, &dy);
-  const float power = ((c.x * (dx * dx) + ((c.y * 2.0f) * dx) * dy) + c.z * (dy * dy)) * -0.5f;
-  if (power > 0.0f || power < -g.w) return false;
-  const float alpha = rclamp(g.z * M::exp(power), 0.0f, 0.99f);
-  if (alpha < (float)(1.0 / 255.0)) return false;
+  float alpha;
+  if (M::kExact) {
+    float dx, dy;
+    boundary_delta<PERIODIC>(pxc, pyc, g.x, g.y, c.x, c.y, c.z, f, &dx, &dy);
+    const float power = ((c.x * (dx * dx) + ((c.y * 2.0f) * dx) * dy) + c.z * (dy * dy)) * -0.5f;
+    if (power > 0.0f || power < -g.w) return false;
+    alpha = rclamp(g.z * M::exp(power), 0.0f, 0.99f);
+    if (alpha < (float)(1.0 / 255.0)) return false;
+  } else {
+    float dx, dy;
+    if (PERIODIC) {
+      const float4 r = sb.raw[j];
+      boundary_delta<true>(pxc, pyc, g.x, g.y, r.x, r.y, r.z, f, &dx, &dy);
+    } else {
+      dx = pxc - g.x;
+      dy = pyc - g.y;
+    }
+    const float p2 = fmaf(c.x * dx, dx, fmaf(c.y * dx, dy, (c.z * dy) * dy));
+    if (!(p2 >= -g.w)) return false;  // below 1/255 (and the NaN-safe reject)
+    alpha = fminf(g.z * ex2_approx(fminf(p2, 0.0f)), 0.99f);
+  }
   const float4 col = sb.col[j];
   const float contrib = a.t * alpha;
   a.r = a.r + col.x * contrib;
   a.g = a.g + col.y * contrib;
   a.b = a.b + col.z * contrib;
   a.d = a.d + c.w * contrib;
-  a.t = a.t * (1.0f - alpha);
+  if (M::kExact)
+    a.t = a.t * (1.0f - alpha);
+  else
+    a.t = a.t - contrib;
+  if (blended) ++*blended;
   return a.t < f.t_threshold;
 }
 
+struct RasterCounters {
+  uint32_t checked, blended;
+};
+
 // Blend samples [s0, s1) of the tile into `a` (block-cooperative; every thread
 // of the block must call it). `done` marks pixels that take no more samples.
-template <class M>
+// With STATS, `cnt` receives the reference's per-pixel counters: samples
+// examined until done (TileRasterizer.ts:617) and samples blended (:702).
+template <class M, bool PERIODIC, bool STATS>
 __device__ __forceinline__ void blend_range(uint32_t begin, uint32_t source_count, uint32_t raster_count,
                                             uint32_t s0, uint32_t s1, bool capped, const uint32_t* __restrict__ ids,
                                             const float4* __restrict__ mean, const float4* __restrict__ conic,
                                             const float4* __restrict__ color, const RasterFrame& f, float tile_x0,
-                                            float tile_y0, float pxc, float pyc, bool done, PixelAcc& a, Batch& sb) {
+                                            float tile_y0, float pxc, float pyc, bool done, PixelAcc& a, Batch& sb,
+                                            RasterCounters& cnt) {
   const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
+  const bool counting = STATS && !done;
+  uint32_t stop = s1;  // sample index after which this pixel stopped
   for (uint32_t b = s0; b < s1; b += kBlock) {
     if (!__syncthreads_or(!done)) break;
     const uint32_t i = b + t;
@@ -167,8 +216,14 @@ __device__ __forceinline__ void blend_range(uint32_t begin, uint32_t source_coun
       const float4 m = __ldg(mean + g);
       const float4 c = __ldg(conic + g);
       const float thr = M::log(m.w * 255.0f);
-      sb.geo[t] = make_float4(m.x, m.y, m.w, thr);
-      sb.con[t] = make_float4(c.x, c.y, c.z, m.z);
+      if (M::kExact) {
+        sb.geo[t] = make_float4(m.x, m.y, m.w, thr);
+        sb.con[t] = make_float4(c.x, c.y, c.z, m.z);
+      } else {
+        sb.geo[t] = make_float4(m.x, m.y, m.w, thr * kLog2e);
+        sb.con[t] = make_float4(-0.5f * kLog2e * c.x, -kLog2e * c.y, -0.5f * kLog2e * c.z, m.z);
+        if (PERIODIC) sb.raw[t] = c;
+      }
       sb.col[t] = __ldg(color + g);
       sb.mask[t] = (uint8_t)patch_mask(m.x, m.y, c.x, c.y, c.z, thr, tile_x0, tile_y0, f.axis);
     }
@@ -181,11 +236,15 @@ __device__ __forceinline__ void blend_range(uint32_t begin, uint32_t source_coun
       while (bits) {
         const uint32_t j = c0 + (uint32_t)(__ffs(bits) - 1);
         bits &= bits - 1u;
-        if (!done) done = blend_one<M>(sb, j, pxc, pyc, f, a);
+        if (!done) {
+          done = blend_one<M, PERIODIC>(sb, j, pxc, pyc, f, a, STATS ? &cnt.blended : nullptr);
+          if (STATS && done) stop = b + j + 1;
+        }
       }
     }
   }
   __syncthreads();  // shared batch buffers are free again
+  if (counting) cnt.checked += stop - s0;
 }
 
 __device__ __forceinline__ bool finite_r(float v) { return v == v && fabsf(v) <= 3.402823e+38f; }
@@ -212,24 +271,27 @@ __device__ __forceinline__ float finalize_depth(float wd, float trans, const Pas
   return dev;
 }
 
-// One block per tile of the batch; the tile's view supplies its viewport and
-// targets.
-template <class M>
+// One block per tile of the batch (in work-list order); the tile's view
+// supplies its viewport and targets.
+template <class M, bool PERIODIC, bool STATS>
 __global__ void __launch_bounds__(kBlock) k_raster(const uint32_t* __restrict__ tile_offsets,
+                                                   const uint32_t* __restrict__ order,
                                                    const uint32_t* __restrict__ ids,
                                                    const float4* __restrict__ mean,
                                                    const float4* __restrict__ conic,
                                                    const float4* __restrict__ color, BatchView bv, PassOptions o,
-                                                   const Control* __restrict__ ctl) {
+                                                   Control* __restrict__ ctl) {
   // Overflow: the reference zeroes the raster dispatch, so nothing is written.
   if (ctl->state[3] != 0u) return;
   __shared__ Batch sb;
   __shared__ uint32_t s_view;
-  if (threadIdx.x == 0) s_view = find_view(bv.tile_base, bv.nviews, blockIdx.x);
+  __shared__ unsigned long long s_stats[4];
+  const uint32_t tile = order ? order[blockIdx.x] : blockIdx.x;
+  if (threadIdx.x == 0) s_view = find_view(bv.tile_base, bv.nviews, tile);
+  if (STATS && threadIdx.x < 4) s_stats[threadIdx.x] = 0ull;
   __syncthreads();
   const ViewDesc& v = bv.views[s_view];
   const RasterFrame f = {v.vw, v.vh, o.t_threshold, o.axis};
-  const uint32_t tile = blockIdx.x;
   const uint32_t local = tile - v.tile_base;
   const uint32_t tx = local % v.tiles_x, ty = local / v.tiles_x;
   const uint32_t lx = morton_compact(threadIdx.x), ly = morton_compact(threadIdx.x >> 1);
@@ -245,9 +307,10 @@ __global__ void __launch_bounds__(kBlock) k_raster(const uint32_t* __restrict__ 
   const float pxc = (float)px + 0.5f, pyc = (float)py + 0.5f;
   const float tile_x0 = (float)(tx * kTileSize), tile_y0 = (float)(ty * kTileSize);
   PixelAcc a = {0.0f, 0.0f, 0.0f, 1.0f, 0.0f};
+  RasterCounters cnt = {0u, 0u};
   if (!chunked) {
-    blend_range<M>(begin, source_count, raster_count, 0, raster_count, capped, ids, mean, conic, color, f, tile_x0,
-                   tile_y0, pxc, pyc, !active, a, sb);
+    blend_range<M, PERIODIC, STATS>(begin, source_count, raster_count, 0, raster_count, capped, ids, mean, conic,
+                                    color, f, tile_x0, tile_y0, pxc, pyc, !active, a, sb, cnt);
   } else {
     const uint32_t nchunk = (raster_count + chunk - 1) / chunk;
     bool finished = !active;
@@ -256,8 +319,8 @@ __global__ void __launch_bounds__(kBlock) k_raster(const uint32_t* __restrict__ 
       const uint32_t s0 = ch * chunk;
       const uint32_t s1 = min(s0 + chunk, raster_count);
       PixelAcc p = {0.0f, 0.0f, 0.0f, 1.0f, 0.0f};
-      blend_range<M>(begin, source_count, raster_count, s0, s1, capped, ids, mean, conic, color, f, tile_x0, tile_y0,
-                     pxc, pyc, finished, p, sb);
+      blend_range<M, PERIODIC, STATS>(begin, source_count, raster_count, s0, s1, capped, ids, mean, conic, color, f,
+                                      tile_x0, tile_y0, pxc, pyc, finished, p, sb, cnt);
       if (!finished) {
         a.r = a.r + p.r * a.t;
         a.g = a.g + p.g * a.t;
@@ -267,6 +330,19 @@ __global__ void __launch_bounds__(kBlock) k_raster(const uint32_t* __restrict__ 
         if (a.t < f.t_threshold) finished = true;
       }
     }
+  }
+  if (STATS) {
+    // TileRasterizer.ts:749-768: checked, blended, pixels, alpha-stopped.
+    if (active) {
+      atomicAdd(&s_stats[0], (unsigned long long)cnt.checked);
+      atomicAdd(&s_stats[1], (unsigned long long)cnt.blended);
+      if (raster_count > 0) {
+        atomicAdd(&s_stats[2], 1ull);
+        if (a.t < f.t_threshold) atomicAdd(&s_stats[3], 1ull);
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x < 4 && s_stats[threadIdx.x]) atomicAdd(&ctl->raster_stats[threadIdx.x], s_stats[threadIdx.x]);
   }
   if (!active) return;
   const float bga = rclamp(o.background[3], 0.0f, 1.0f);
@@ -286,6 +362,22 @@ __global__ void __launch_bounds__(kBlock) k_raster(const uint32_t* __restrict__ 
     reinterpret_cast<float4*>(v.color)[off] = make_float4(r, g, b, alpha);
   }
   if (v.depth) v.depth[off] = finalize_depth(a.d, a.t, o, v.vnear, v.vfar);
+}
+
+template <class M>
+void launch_raster_policy(const uint32_t* tile_offsets, const uint32_t* order, const uint32_t* ids,
+                          const float4* mean, const float4* conic, const float4* color, const BatchView& b,
+                          const PassOptions& o, Control* ctl, bool stats, cudaStream_t st) {
+  if (b.total_tiles == 0) return;
+  const bool periodic = o.axis != 0u;
+#define GS_RASTER(P, S) \
+  k_raster<M, P, S><<<b.total_tiles, kBlock, 0, st>>>(tile_offsets, order, ids, mean, conic, color, b, o, ctl)
+  if (periodic) {
+    if (stats) GS_RASTER(true, true); else GS_RASTER(true, false);
+  } else {
+    if (stats) GS_RASTER(false, true); else GS_RASTER(false, false);
+  }
+#undef GS_RASTER
 }
 
 }  // namespace gs

@@ -108,6 +108,7 @@ typedef struct gs3d_pipeline_desc {
   uint32_t boundary_policy;       /* gs3d_boundary_policy, default clip */
   uint32_t raster_precision;      /* gs3d_raster_precision, default FP32 */
   uint32_t depth_encoding;        /* 0: default device depth node; 1: raw alpha-weighted depth */
+  uint32_t raster_stats;          /* rasterStats (types.ts:283): per-pixel work counters, default 0 */
 } gs3d_pipeline_desc;
 
 /* Per-frame camera state: what FrameUniforms.update and ObjectFrameState.update
@@ -139,6 +140,13 @@ typedef struct gs3d_stats {
   uint64_t intersection_capacity;
   uint32_t device_error;            /* nonzero: a bounded device wait expired */
   uint32_t reserved;
+  /* rasterStats counters (TileRasterizer.ts:904-927), zero unless enabled:
+   * samples examined and blended by all pixels, in-bounds pixels of nonempty
+   * tiles, and those whose transmittance fell below the threshold. */
+  uint64_t raster_checked;
+  uint64_t raster_blended;
+  uint64_t raster_pixels;
+  uint64_t raster_alpha_stopped;
 } gs3d_stats;
 
 /* getResources() (TiledGaussianPipeline.ts:391-406, types.ts:174-193).

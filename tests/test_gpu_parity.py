@@ -218,3 +218,24 @@ def test_batched_views_match_single_view_renders():
         assert np.array_equal(g["tile_offsets"], o["tile_offsets"])
         assert np.array_equal(g["rgba"].view(np.uint32), o["rgba"].view(np.uint32))
         assert np.array_equal(g["depth"].view(np.uint32), o["depth"].view(np.uint32))
+
+
+@pytest.mark.parametrize("name", ["default", "chunked", "capped"])
+def test_raster_stats_match_reference_counters(name):
+    # rasterStats (TileRasterizer.ts:545-546,617,702,749-768): samples examined
+    # until each pixel is done, and samples blended, summed over pixels.
+    scene, frame = CASES[name]()
+    o = oracle.render(scene, frame, 0)
+    run = GpuRun(scene, frame, "exact", capacity=max(int(o["state"][1]), 1))
+    run.pipe.dispose()
+    import importlib
+    P = importlib.import_module("3dgs_tile_webgpu_gb300")
+    from gpu_harness import pipeline_options
+    run.pipe = P.TiledGaussianPipeline(run.ds.data(), dict(pipeline_options(frame, "exact", max(int(o["state"][1]), 1)),
+                                                           raster_stats=True))
+    g = run.render(frame)
+    run.close()
+    work = g["stats"]["rasterWork"]
+    assert work["checked"] == o["checked"]
+    assert work["blended"] == o["blended"]
+    assert_bit_exact(g, o)
