@@ -249,7 +249,7 @@ constexpr uint32_t kSortTile = 4096;  // items per onesweep block
 // Raster work list: every tile of the batch, heaviest load class first.
 void launch_tile_order(const uint32_t* tile_offsets, uint32_t ntile, Control* ctl, uint32_t* order, int sms,
                        cudaStream_t st);
-// Rasterizer over every tile of the batch (precision: 0 fp32, 1 exact).
+// Rasterizer over every tile of the batch (precision: 0 fp32, 1 exact, 2 half2).
 void launch_raster(int precision, const uint32_t* tile_offsets, const uint32_t* order, const uint32_t* sorted_ids,
                    const float4* mean, const float4* conic, const float4* color, const BatchView& b,
                    const PassOptions& o, Control* ctl, bool stats, cudaStream_t st);

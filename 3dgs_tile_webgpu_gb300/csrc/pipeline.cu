@@ -128,7 +128,6 @@ gs3d_status validate_desc(gs3d_pipeline* p, const gs3d_pipeline_desc& d) {
   if (d.boundary_policy > 2) return fail(p, GS3D_ERROR_INVALID_ARGUMENT, "boundaryPolicy must be clip, repeat-x or repeat-y");
   if (d.raster_precision > 2) return fail(p, GS3D_ERROR_INVALID_ARGUMENT, "unknown raster precision");
   if (d.depth_encoding > 1) return fail(p, GS3D_ERROR_INVALID_ARGUMENT, "unknown depth encoding");
-  if (d.raster_precision == GS3D_RASTER_HALF2) return fail(p, GS3D_ERROR_UNSUPPORTED, "half2 raster not built");
   // GaussianPass.ts:178-192,231-255
   if (d.intersection_capacity == 0 || d.intersection_capacity > 0x7fffffffull)
     return fail(p, GS3D_ERROR_RANGE, "intersectionCapacity must be a positive integer below 2^31");

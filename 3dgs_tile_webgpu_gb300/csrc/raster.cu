@@ -1,6 +1,7 @@
 // FP32 rasterizer with hardware exp2 and multiply-add contraction: the
 // production form of the reference's direct tile rasterizer
 // (src/renderer/pipeline/TileRasterizer.ts:414-805); and the raster work list.
+#include "raster_half2.cuh"
 #include "raster_impl.cuh"
 
 namespace gs {
@@ -61,6 +62,10 @@ void launch_raster(int precision, const uint32_t* tile_offsets, const uint32_t* 
                    const PassOptions& o, Control* ctl, bool stats, cudaStream_t st) {
   if (precision == 1) {
     launch_raster_exact(tile_offsets, order, ids, mean, conic, color, b, o, ctl, stats, st);
+    return;
+  }
+  if (precision == 2) {
+    launch_raster_half2(tile_offsets, order, ids, mean, conic, color, b, o, ctl, stats, st);
     return;
   }
   launch_raster_policy<FastMath>(tile_offsets, order, ids, mean, conic, color, b, o, ctl, stats, st);

@@ -1,0 +1,278 @@
+// Packed-half2 form of the tile rasterizer (the reference's direct rasterizer,
+// src/renderer/pipeline/TileRasterizer.ts:414-805, with the same chunk, cap,
+// boundary, background and depth semantics as raster_impl.cuh).
+//
+// 128 threads per 16x16 tile; each thread owns two pixels of one column,
+// (x, y) and (x, y + 4), so warp w owns the 8x8 patch at (8 (w & 1), 8 (w >> 1)).
+// The two pixels share dx and the x-only terms of the quadratic, the record
+// loads, the culling test and the loop. Per record and pixel pair:
+//   FP32   dx, dy0, dy1 and the base-2 exponent of each pixel (the conic is
+//          pre-scaled by -1/2 log2 e while staging)
+//   half2  exp2 of both exponents (ex2.approx.f16x2) and alpha = min(op e, 0.99)
+//   FP32   transmittance and colour/depth accumulation
+// A pixel blends a record only when its exponent clears the 1/255 threshold.
+#pragma once
+
+#include <cuda_fp16.h>
+
+#include "raster_impl.cuh"
+
+namespace gs {
+
+constexpr int kHalfThreads = 128;
+
+__device__ __forceinline__ __half2 h2ex2_approx(__half2 x) {
+  uint32_t in = *reinterpret_cast<uint32_t*>(&x), out;
+  asm("ex2.approx.f16x2 %0, %1;" : "=r"(out) : "r"(in));
+  return *reinterpret_cast<__half2*>(&out);
+}
+
+struct HalfBatch {
+  float4 geo[kBlock];  // cx, cy, opacity, threshold * log2 e
+  float4 con[kBlock];  // -a/2 log2 e, -b log2 e, -c/2 log2 e, depth
+  float4 col[kBlock];
+  float4 raw[kBlock];  // conic (a, b, c) for periodic boundaries
+  uint8_t mask[kBlock];
+};
+
+// Which of the tile's four 8x8 warp patches can hold a pixel centre inside the
+// splat's support (same conservative box as patch_mask).
+__device__ __forceinline__ uint32_t patch_mask8(float cx, float cy, float ca, float cb, float cc, float thr,
+                                                float tile_x0, float tile_y0, uint32_t axis) {
+  if (axis != 0u) return 0xfu;
+  const float det = ca * cc - cb * cb;
+  const float tr = ca + cc;
+  if (!(det > 0.0f) || !(tr * tr <= 4e4f * det) || !(thr >= 0.0f)) return 0xfu;
+  const float q = 2.0f * thr;
+  const float hx = sqrtf(q * cc / det) * 1.05f + 0.25f;
+  const float hy = sqrtf(q * ca / det) * 1.05f + 0.25f;
+  if (!(hx < 1e30f) || !(hy < 1e30f)) return 0xfu;
+  uint32_t m = 0;
+#pragma unroll
+  for (uint32_t w = 0; w < 4; ++w) {
+    const float x0 = tile_x0 + (float)(8u * (w & 1u)) + 0.5f;
+    const float y0 = tile_y0 + (float)(8u * (w >> 1)) + 0.5f;
+    const bool hit = cx + hx >= x0 && cx - hx <= x0 + 7.0f && cy + hy >= y0 && cy - hy <= y0 + 7.0f;
+    m |= hit ? (1u << w) : 0u;
+  }
+  return m;
+}
+
+__device__ __forceinline__ void blend_pixel(float alpha, const float4& col, float depth, PixelAcc& a) {
+  const float contrib = a.t * alpha;
+  a.r = a.r + col.x * contrib;
+  a.g = a.g + col.y * contrib;
+  a.b = a.b + col.z * contrib;
+  a.d = a.d + depth * contrib;
+  a.t = a.t - contrib;
+}
+
+template <bool PERIODIC, bool STATS>
+__device__ __forceinline__ void blend_range_h2(uint32_t begin, uint32_t source_count, uint32_t raster_count,
+                                               uint32_t s0, uint32_t s1, bool capped,
+                                               const uint32_t* __restrict__ ids, const float4* __restrict__ mean,
+                                               const float4* __restrict__ conic, const float4* __restrict__ color,
+                                               const RasterFrame& f, float tile_x0, float tile_y0, float pxc,
+                                               float pyc0, bool done0, bool done1, PixelAcc& a0, PixelAcc& a1,
+                                               HalfBatch& sb, RasterCounters& c0n, RasterCounters& c1n) {
+  const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
+  const bool count0 = STATS && !done0, count1 = STATS && !done1;
+  uint32_t stop0 = s1, stop1 = s1;
+  const float pyc1 = pyc0 + 4.0f;
+  const __half2 cap = __float2half2_rn(0.99f);
+  for (uint32_t b = s0; b < s1; b += kBlock) {
+    if (!__syncthreads_or(!(done0 && done1))) break;
+#pragma unroll
+    for (uint32_t h = 0; h < 2; ++h) {
+      const uint32_t slot = t + h * kHalfThreads;
+      const uint32_t i = b + slot;
+      if (i < s1) {
+        uint32_t src = i;
+        if (capped) src = (uint32_t)floorf((((float)i + 0.5f) * (float)source_count) / (float)raster_count);
+        const uint32_t g = __ldg(ids + begin + src);
+        const float4 m = __ldg(mean + g);
+        const float4 c = __ldg(conic + g);
+        const float thr = __logf(m.w * 255.0f);
+        sb.geo[slot] = make_float4(m.x, m.y, m.w, thr * kLog2e);
+        sb.con[slot] = make_float4(-0.5f * kLog2e * c.x, -kLog2e * c.y, -0.5f * kLog2e * c.z, m.z);
+        if (PERIODIC) sb.raw[slot] = c;
+        sb.col[slot] = __ldg(color + g);
+        sb.mask[slot] = (uint8_t)patch_mask8(m.x, m.y, c.x, c.y, c.z, thr, tile_x0, tile_y0, f.axis);
+      }
+    }
+    __syncthreads();
+    const uint32_t n = min((uint32_t)kBlock, s1 - b);
+    for (uint32_t base = 0; base < n; base += 32) {
+      if (__all_sync(0xffffffffu, done0 && done1)) break;
+      const uint32_t k = base + lane;
+      uint32_t bits = __ballot_sync(0xffffffffu, k < n && ((sb.mask[k] >> warp) & 1u));
+      while (bits) {
+        const uint32_t j = base + (uint32_t)(__ffs(bits) - 1);
+        bits &= bits - 1u;
+        if (done0 && done1) continue;
+        const float4 g = sb.geo[j];
+        const float4 c = sb.con[j];
+        float p0, p1;
+        if (PERIODIC) {
+          const float4 r = sb.raw[j];
+          float dx0, dy0, dx1, dy1;
+          boundary_delta<true>(pxc, pyc0, g.x, g.y, r.x, r.y, r.z, f, &dx0, &dy0);
+          boundary_delta<true>(pxc, pyc1, g.x, g.y, r.x, r.y, r.z, f, &dx1, &dy1);
+          p0 = fmaf(c.x * dx0, dx0, fmaf(c.y * dx0, dy0, (c.z * dy0) * dy0));
+          p1 = fmaf(c.x * dx1, dx1, fmaf(c.y * dx1, dy1, (c.z * dy1) * dy1));
+        } else {
+          const float dx = pxc - g.x;
+          const float dy0 = pyc0 - g.y, dy1 = pyc1 - g.y;
+          const float bdx = c.y * dx, xx = (c.x * dx) * dx;
+          p0 = fmaf(fmaf(c.z, dy0, bdx), dy0, xx);
+          p1 = fmaf(fmaf(c.z, dy1, bdx), dy1, xx);
+        }
+        const bool use0 = !done0 && p0 >= -g.w;
+        const bool use1 = !done1 && p1 >= -g.w;
+        if (!(use0 || use1)) continue;
+        const __half2 e = h2ex2_approx(__floats2half2_rn(fminf(p0, 0.0f), fminf(p1, 0.0f)));
+        const float2 al = __half22float2(__hmin2(__hmul2(__float2half2_rn(g.z), e), cap));
+        const float4 col = sb.col[j];
+        if (use0) {
+          blend_pixel(al.x, col, c.w, a0);
+          if (STATS) ++c0n.blended;
+          if (a0.t < f.t_threshold) {
+            done0 = true;
+            if (STATS) stop0 = b + j + 1;
+          }
+        }
+        if (use1) {
+          blend_pixel(al.y, col, c.w, a1);
+          if (STATS) ++c1n.blended;
+          if (a1.t < f.t_threshold) {
+            done1 = true;
+            if (STATS) stop1 = b + j + 1;
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();
+  if (count0) c0n.checked += stop0 - s0;
+  if (count1) c1n.checked += stop1 - s0;
+}
+
+__device__ __forceinline__ void store_pixel(const ViewDesc& v, const PassOptions& o, uint32_t px, uint32_t py,
+                                            const PixelAcc& a) {
+  const uint32_t W = (uint32_t)v.vw;
+  const float bga = rclamp(o.background[3], 0.0f, 1.0f);
+  const float r = a.r + (o.background[0] * a.t) * bga;
+  const float g = a.g + (o.background[1] * a.t) * bga;
+  const float b = a.b + (o.background[2] * a.t) * bga;
+  const float alpha = 1.0f - a.t * (1.0f - bga);
+  const size_t off = (size_t)py * W + px;
+  if (v.color_half) {
+    __half2 lo = __floats2half2_rn(r, g);
+    __half2 hi = __floats2half2_rn(b, alpha);
+    uint2 w;
+    w.x = *reinterpret_cast<uint32_t*>(&lo);
+    w.y = *reinterpret_cast<uint32_t*>(&hi);
+    reinterpret_cast<uint2*>(v.color)[off] = w;
+  } else {
+    reinterpret_cast<float4*>(v.color)[off] = make_float4(r, g, b, alpha);
+  }
+  if (v.depth) v.depth[off] = finalize_depth(a.d, a.t, o, v.vnear, v.vfar);
+}
+
+template <bool PERIODIC, bool STATS>
+__global__ void __launch_bounds__(kHalfThreads) k_raster_h2(const uint32_t* __restrict__ tile_offsets,
+                                                           const uint32_t* __restrict__ order,
+                                                           const uint32_t* __restrict__ ids,
+                                                           const float4* __restrict__ mean,
+                                                           const float4* __restrict__ conic,
+                                                           const float4* __restrict__ color, BatchView bv,
+                                                           PassOptions o, Control* __restrict__ ctl) {
+  if (ctl->state[3] != 0u) return;  // overflow: nothing is published
+  __shared__ HalfBatch sb;
+  __shared__ uint32_t s_view;
+  __shared__ unsigned long long s_stats[4];
+  const uint32_t tile = order ? order[blockIdx.x] : blockIdx.x;
+  if (threadIdx.x == 0) s_view = find_view(bv.tile_base, bv.nviews, tile);
+  if (STATS && threadIdx.x < 4) s_stats[threadIdx.x] = 0ull;
+  __syncthreads();
+  const ViewDesc& v = bv.views[s_view];
+  const RasterFrame f = {v.vw, v.vh, o.t_threshold, o.axis};
+  const uint32_t local = tile - v.tile_base;
+  const uint32_t tx = local % v.tiles_x, ty = local / v.tiles_x;
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+  const uint32_t px = tx * kTileSize + 8u * (warp & 1u) + morton_compact(lane);
+  const uint32_t py0 = ty * kTileSize + 8u * (warp >> 1) + morton_compact(lane >> 1);
+  const uint32_t py1 = py0 + 4u;
+  const uint32_t W = (uint32_t)v.vw, H = (uint32_t)v.vh;
+  const bool active0 = px < W && py0 < H, active1 = px < W && py1 < H;
+  const uint32_t begin = tile_offsets[tile], end = tile_offsets[tile + 1];
+  const uint32_t source_count = end - begin;
+  const bool capped = o.max_per_tile != 0u;
+  const uint32_t raster_count = capped ? min(source_count, o.max_per_tile) : source_count;
+  const uint32_t chunk = o.chunk;
+  const bool chunked = chunk != 0u && raster_count > chunk;
+  const float pxc = (float)px + 0.5f, pyc0 = (float)py0 + 0.5f;
+  const float tile_x0 = (float)(tx * kTileSize), tile_y0 = (float)(ty * kTileSize);
+  PixelAcc a0 = {0.0f, 0.0f, 0.0f, 1.0f, 0.0f}, a1 = a0;
+  RasterCounters n0 = {0u, 0u}, n1 = {0u, 0u};
+  if (!chunked) {
+    blend_range_h2<PERIODIC, STATS>(begin, source_count, raster_count, 0, raster_count, capped, ids, mean, conic,
+                                    color, f, tile_x0, tile_y0, pxc, pyc0, !active0, !active1, a0, a1, sb, n0, n1);
+  } else {
+    const uint32_t nchunk = (raster_count + chunk - 1) / chunk;
+    bool fin0 = !active0, fin1 = !active1;
+    for (uint32_t ch = 0; ch < nchunk; ++ch) {
+      if (!__syncthreads_or(!(fin0 && fin1))) break;
+      const uint32_t s0 = ch * chunk, s1 = min(s0 + chunk, raster_count);
+      PixelAcc p0 = {0.0f, 0.0f, 0.0f, 1.0f, 0.0f}, p1 = p0;
+      blend_range_h2<PERIODIC, STATS>(begin, source_count, raster_count, s0, s1, capped, ids, mean, conic, color,
+                                      f, tile_x0, tile_y0, pxc, pyc0, fin0, fin1, p0, p1, sb, n0, n1);
+      if (!fin0) {
+        a0.r = a0.r + p0.r * a0.t; a0.g = a0.g + p0.g * a0.t; a0.b = a0.b + p0.b * a0.t;
+        a0.d = a0.d + p0.d * a0.t; a0.t = a0.t * p0.t;
+        if (a0.t < f.t_threshold) fin0 = true;
+      }
+      if (!fin1) {
+        a1.r = a1.r + p1.r * a1.t; a1.g = a1.g + p1.g * a1.t; a1.b = a1.b + p1.b * a1.t;
+        a1.d = a1.d + p1.d * a1.t; a1.t = a1.t * p1.t;
+        if (a1.t < f.t_threshold) fin1 = true;
+      }
+    }
+  }
+  if (STATS) {
+    for (int q = 0; q < 2; ++q) {
+      const bool act = q == 0 ? active0 : active1;
+      const RasterCounters& cn = q == 0 ? n0 : n1;
+      const PixelAcc& aq = q == 0 ? a0 : a1;
+      if (act) {
+        atomicAdd(&s_stats[0], (unsigned long long)cn.checked);
+        atomicAdd(&s_stats[1], (unsigned long long)cn.blended);
+        if (raster_count > 0) {
+          atomicAdd(&s_stats[2], 1ull);
+          if (aq.t < f.t_threshold) atomicAdd(&s_stats[3], 1ull);
+        }
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x < 4 && s_stats[threadIdx.x]) atomicAdd(&ctl->raster_stats[threadIdx.x], s_stats[threadIdx.x]);
+  }
+  if (active0) store_pixel(v, o, px, py0, a0);
+  if (active1) store_pixel(v, o, px, py1, a1);
+}
+
+inline void launch_raster_half2(const uint32_t* tile_offsets, const uint32_t* order, const uint32_t* ids,
+                                const float4* mean, const float4* conic, const float4* color, const BatchView& b,
+                                const PassOptions& o, Control* ctl, bool stats, cudaStream_t st) {
+  if (b.total_tiles == 0) return;
+#define GS_RASTER_H2(P, S)                                                                                     \
+  k_raster_h2<P, S><<<b.total_tiles, kHalfThreads, 0, st>>>(tile_offsets, order, ids, mean, conic, color, b, o, \
+                                                            ctl)
+  if (o.axis != 0u) {
+    if (stats) GS_RASTER_H2(true, true); else GS_RASTER_H2(true, false);
+  } else {
+    if (stats) GS_RASTER_H2(false, true); else GS_RASTER_H2(false, false);
+  }
+#undef GS_RASTER_H2
+}
+
+}  // namespace gs

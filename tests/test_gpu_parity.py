@@ -21,6 +21,7 @@ pytestmark = pytest.mark.gpu
 sc = scenes()
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "small_scene.npz")
 FP32_MAX_ABS = 4e-3
+HALF2_MAX_ABS = 2e-2
 MIN_PSNR_DB = 50.0
 
 
@@ -95,6 +96,21 @@ def test_fp32_raster_tolerance(name):
     run.close()
     assert_bit_exact(g, o, image=False)
     assert np.abs(g["rgba"] - o["rgba"]).max() <= FP32_MAX_ABS
+    assert psnr(g["rgba"][..., :3], o64["rgba"][..., :3]) >= MIN_PSNR_DB
+
+
+@pytest.mark.parametrize("name", ["default", "chunked", "repeat_x", "repeat_y", "background_depth_raw", "capped"])
+def test_half2_raster_tolerance(name):
+    # Packed-half2 evaluation with FP32 accumulation: integer stages unchanged,
+    # image within HALF2_MAX_ABS of the FP32 oracle and >= 50 dB vs FP64.
+    scene, frame = CASES[name]()
+    o = oracle.render(scene, frame, 0)
+    o64 = oracle.render(scene, frame, 1)
+    run = GpuRun(scene, frame, "half2", capacity=max(int(o["state"][1]), 1))
+    g = run.render(frame)
+    run.close()
+    assert_bit_exact(g, o, image=False)
+    assert np.abs(g["rgba"] - o["rgba"]).max() <= HALF2_MAX_ABS
     assert psnr(g["rgba"][..., :3], o64["rgba"][..., :3]) >= MIN_PSNR_DB
 
 
