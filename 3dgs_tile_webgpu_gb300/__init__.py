@@ -192,6 +192,36 @@ class TiledGaussianPipeline:
                                                   C.c_void_p(int(stream)))
         _raise(self._lib, st, self._p)
 
+    def _views_array(self, views: list):
+        arr = (View * len(views))()
+        keep = []
+        for i, (data, cam, w, h, color_ptr, depth_ptr, fmt) in enumerate(views):
+            arr[i].data = C.pointer(data)
+            arr[i].camera = C.pointer(cam)
+            arr[i].width, arr[i].height = int(w), int(h)
+            arr[i].targets.color = int(color_ptr)
+            arr[i].targets.color_format = {"rgba16f": 0, "rgba32f": 1}[fmt]
+            arr[i].targets.depth = (C.cast(C.c_void_p(int(depth_ptr)), C.POINTER(C.c_float))
+                                    if depth_ptr else None)
+            keep.append((data, cam))
+        return arr, keep
+
+    def capture_graph(self, views: list, stream: int) -> None:
+        """Capture the batched pass for these views into CUDA graphs (same
+        tuple layout as render_batch); launch_graph replays it with new
+        cameras. ``stream`` must be a non-default CUDA stream handle."""
+        arr, keep = self._views_array(views)
+        self._graph_keep = (arr, keep)  # the library keeps pointers to the GaussianData structs
+        _raise(self._lib, self._lib.gs3d_pipeline_capture_graph(self._p, arr, len(views), C.c_void_p(int(stream))),
+               self._p)
+
+    def launch_graph(self, cameras: list, attempt: int = 1, reset_valid: bool = False, stream: int = 0) -> None:
+        arr = (Camera * len(cameras))(*cameras)
+        self._graph_cams = (arr, [getattr(c, "_table", None) for c in cameras])
+        st = self._lib.gs3d_pipeline_launch_graph(self._p, arr, len(cameras), int(attempt), 1 if reset_valid else 0,
+                                                  C.c_void_p(int(stream)))
+        _raise(self._lib, st, self._p)
+
     def batch_layout(self) -> tuple[list, list]:
         """(item_base, tile_base) of the last render, one entry per view plus the total."""
         n = C.c_uint32()

@@ -81,6 +81,8 @@ SIGNATURES = {
     "gs3d_pipeline_prepare_frame": (C.c_int, [_P, C.c_uint32, C.c_uint32]),
     "gs3d_pipeline_render": (C.c_int, [_P, C.POINTER(Camera), C.c_uint32, C.c_int, C.POINTER(Targets), _P]),
     "gs3d_pipeline_render_batch": (C.c_int, [_P, C.POINTER(View), C.c_uint32, C.c_uint32, C.c_int, _P]),
+    "gs3d_pipeline_capture_graph": (C.c_int, [_P, C.POINTER(View), C.c_uint32, _P]),
+    "gs3d_pipeline_launch_graph": (C.c_int, [_P, C.POINTER(Camera), C.c_uint32, C.c_uint32, C.c_int, _P]),
     "gs3d_pipeline_batch_layout": (C.c_int, [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.c_uint32,
                                              C.POINTER(C.c_uint32)]),
     "gs3d_pipeline_read_stats": (C.c_int, [_P, C.POINTER(Stats)]),

@@ -50,12 +50,14 @@ struct PassOptions {
 };
 
 // The batch table in device memory: three ascending base arrays (nviews + 1
-// entries each, the last one the total) followed by the view descriptors.
+// entries each, the last one the total) followed by the view descriptors and
+// the per-frame parameters (attempt, reset_valid).
 struct BatchView {
   const uint32_t* item_base;
   const uint32_t* tile_base;
   const uint32_t* block_base;
   const ViewDesc* views;
+  const uint32_t* frame_params;  // attempt, reset_valid
   uint32_t nviews;
   uint32_t total_items;
   uint32_t total_tiles;
@@ -91,7 +93,18 @@ enum Ticket { kTicketCompact = 0, kTicketScan = 1, kTicketSortBase = 2 };
 // ---------------------------------------------------------------------------
 // Decoupled look-back status words: [63:34] epoch, [33:32] flag, [31:0] value.
 // A word whose epoch differs from the launch's epoch is "not yet published",
-// so the status array never needs clearing between launches.
+// so the status array never needs clearing between launches. A frame's
+// launches use epochs base + 1 .. base + kEpochsPerFrame, where base is a
+// device-side counter advanced by k_epoch_begin at the start of every frame,
+// so a replayed CUDA graph never reuses an epoch.
+constexpr uint32_t kEpochsPerFrame = 16;
+
+// The epoch of look-back launch `index` of the current frame.
+struct Epoch {
+  const uint32_t* base;  // device counter, or null for a host-chosen epoch
+  uint32_t add;
+  __device__ __forceinline__ uint32_t get() const { return (base ? *base : 0u) + add; }
+};
 constexpr unsigned long long kFlagAggregate = 1ull;
 constexpr unsigned long long kFlagInclusive = 2ull;
 constexpr uint32_t kSpinLimit = 1u << 22;  // polls before a wait is declared expired
@@ -229,11 +242,12 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* s
 // Launch wrappers implemented in the .cu files.
 void launch_project(const BatchView& b, const PassOptions& o, float4* mean, float4* conic, float4* color,
                     uint32_t* counts, uint32_t* keys, int max_degree, cudaStream_t st);
+void launch_epoch_begin(uint32_t* epoch_base, cudaStream_t st);
 void launch_compact(const uint32_t* keys, uint32_t n, uint32_t* vis_off, uint32_t* keys_out, uint32_t* vals_out,
-                    Control* ctl, unsigned long long* status, uint32_t epoch, int depth_passes, cudaStream_t st);
+                    Control* ctl, unsigned long long* status, Epoch epoch, int depth_passes, cudaStream_t st);
 void launch_scan_counts(const uint32_t* sorted_ids, const uint32_t* tile_counts, uint32_t n_max,
                         uint32_t* ordered, uint32_t* offsets, Control* ctl, unsigned long long* status,
-                        uint32_t epoch, uint32_t capacity, uint32_t attempt, int reset_valid, uint32_t* output_state,
+                        Epoch epoch, uint32_t capacity, const uint32_t* frame_params, uint32_t* output_state,
                         cudaStream_t st);
 void launch_emit(const uint32_t* sorted_ids, uint32_t n_max, const float4* mean, const float4* conic,
                  const uint32_t* ordered, const uint32_t* offsets, const BatchView& b, const PassOptions& o,
@@ -244,8 +258,11 @@ void launch_tile_ranges(const uint32_t* sorted_tiles, Control* ctl, uint32_t nti
 // Onesweep LSD pass. n is read from *n_ptr on the device.
 void launch_onesweep(int bits, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
                      uint32_t* vals_out, const uint32_t* n_ptr, uint32_t n_max, int shift, const uint32_t* hist,
-                     unsigned long long* status, uint32_t* ticket, uint32_t epoch, uint32_t* err, cudaStream_t st);
+                     unsigned long long* status, uint32_t* ticket, Epoch epoch, uint32_t* err, cudaStream_t st);
 constexpr uint32_t kSortTile = 4096;  // items per onesweep block
+// Opt every onesweep instantiation into its shared-memory size (once per
+// device; call before any stream capture).
+void prepare_sort_kernels();
 // Raster work list: every tile of the batch, heaviest load class first.
 void launch_tile_order(const uint32_t* tile_offsets, uint32_t ntile, Control* ctl, uint32_t* order, int sms,
                        cudaStream_t st);

@@ -158,8 +158,9 @@ constexpr uint32_t kScanTile = kBlock * kItems;  // 2048 items per tile
 __global__ void __launch_bounds__(kBlock) k_compact(const uint32_t* __restrict__ keys, uint32_t n,
                                                     uint32_t* __restrict__ vis_off, uint32_t* __restrict__ keys_out,
                                                     uint32_t* __restrict__ vals_out, Control* __restrict__ ctl,
-                                                    unsigned long long* __restrict__ status, uint32_t epoch,
+                                                    unsigned long long* __restrict__ status, Epoch ep,
                                                     int passes) {
+  const uint32_t epoch = ep.get();
   __shared__ uint32_t s_tile, s_prefix;
   __shared__ uint32_t s_warp[kBlock / 32];
   __shared__ uint32_t s_hist[4][256];
@@ -226,8 +227,16 @@ __global__ void __launch_bounds__(kBlock) k_compact(const uint32_t* __restrict__
       if (s_hist[p][d]) atomicAdd(&ctl->depth_hist[p][d], s_hist[p][d]);
 }
 
+__global__ void k_epoch_begin(uint32_t* base) {
+  // Leaves room for kEpochsPerFrame launches; status words are 30-bit epochs.
+  const uint32_t next = (*base + kEpochsPerFrame) & ((1u << 30) - 1u);
+  *base = next < kEpochsPerFrame ? kEpochsPerFrame : next;
+}
+
+void launch_epoch_begin(uint32_t* epoch_base, cudaStream_t st) { k_epoch_begin<<<1, 1, 0, st>>>(epoch_base); }
+
 void launch_compact(const uint32_t* keys, uint32_t n, uint32_t* vis_off, uint32_t* keys_out, uint32_t* vals_out,
-                    Control* ctl, unsigned long long* status, uint32_t epoch, int passes, cudaStream_t st) {
+                    Control* ctl, unsigned long long* status, Epoch epoch, int passes, cudaStream_t st) {
   const uint32_t grid = n == 0 ? 1u : (n + kScanTile - 1) / kScanTile;
   k_compact<<<grid, kBlock, 0, st>>>(keys, n, vis_off, keys_out, vals_out, ctl, status, epoch, passes);
 }
@@ -240,9 +249,10 @@ __global__ void __launch_bounds__(kBlock) k_scan_counts(const uint32_t* __restri
                                                         const uint32_t* __restrict__ tile_counts,
                                                         uint32_t* __restrict__ ordered,
                                                         uint32_t* __restrict__ offsets, Control* __restrict__ ctl,
-                                                        unsigned long long* __restrict__ status, uint32_t epoch,
-                                                        uint32_t capacity, uint32_t attempt, int reset_valid,
+                                                        unsigned long long* __restrict__ status, Epoch ep,
+                                                        uint32_t capacity, const uint32_t* __restrict__ frame_params,
                                                         uint32_t* __restrict__ output_state) {
+  const uint32_t epoch = ep.get();
   __shared__ uint32_t s_tile, s_prefix;
   __shared__ uint32_t s_warp[kBlock / 32];
   const uint32_t tid = threadIdx.x;
@@ -280,7 +290,8 @@ __global__ void __launch_bounds__(kBlock) k_scan_counts(const uint32_t* __restri
       ctl->state[1] = all;
       ctl->state[2] = (uint32_t)(((uint64_t)count + 1023u) / 1024u);
       ctl->state[3] = overflow ? 1u : 0u;
-      const uint32_t last_version = reset_valid ? 0u : output_state[1];
+      const uint32_t attempt = frame_params[0];
+      const uint32_t last_version = frame_params[1] ? 0u : output_state[1];
       output_state[0] = attempt;
       output_state[1] = overflow ? last_version : attempt;
       output_state[2] = all;
@@ -301,12 +312,11 @@ __global__ void __launch_bounds__(kBlock) k_scan_counts(const uint32_t* __restri
 }
 
 void launch_scan_counts(const uint32_t* ids, const uint32_t* tile_counts, uint32_t n_max, uint32_t* ordered,
-                        uint32_t* offsets, Control* ctl, unsigned long long* status, uint32_t epoch,
-                        uint32_t capacity, uint32_t attempt, int reset_valid, uint32_t* output_state,
-                        cudaStream_t st) {
+                        uint32_t* offsets, Control* ctl, unsigned long long* status, Epoch epoch,
+                        uint32_t capacity, const uint32_t* frame_params, uint32_t* output_state, cudaStream_t st) {
   const uint32_t grid = n_max == 0 ? 1u : (n_max + kScanTile - 1) / kScanTile;
-  k_scan_counts<<<grid, kBlock, 0, st>>>(ids, tile_counts, ordered, offsets, ctl, status, epoch, capacity, attempt,
-                                         reset_valid, output_state);
+  k_scan_counts<<<grid, kBlock, 0, st>>>(ids, tile_counts, ordered, offsets, ctl, status, epoch, capacity,
+                                         frame_params, output_state);
 }
 
 // ---------------------------------------------------------------------------

@@ -73,6 +73,21 @@ struct gs3d_pipeline {
   // Layout of the last batch.
   std::vector<uint32_t> item_bases, tile_bases;
   uint32_t total_items = 0, total_tiles = 0;
+  // Device epoch counter of the look-back protocol and frames since the last
+  // status reset.
+  uint32_t* epoch_dev = nullptr;
+  uint64_t frames_since_reset = 0;
+  // Captured CUDA graphs (two, alternating staging buffers).
+  cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};
+  unsigned char* graph_pinned[2] = {nullptr, nullptr};
+  unsigned char* graph_dev[2] = {nullptr, nullptr};
+  cudaEvent_t graph_ev[2] = {nullptr, nullptr};
+  bool graph_ev_used[2] = {false, false};
+  size_t graph_stage_bytes = 0;
+  std::vector<gs3d_view> graph_views;
+  std::vector<gs3d_camera> graph_cameras;
+  uint32_t graph_launches = 0;
+  uint32_t graph_next = 0;
   // Frame.
   bool prepared = false;
   uint32_t width = 0, height = 0, tiles_x = 0, tiles_y = 0;
@@ -241,14 +256,14 @@ gs3d_status ensure_tiles(gs3d_pipeline* p, uint64_t tiles) {
   return GS3D_OK;
 }
 
-uint32_t next_epoch(gs3d_pipeline* p, cudaStream_t st) {
-  p->epoch = (p->epoch + 1u) & kEpochMask;
-  if (p->epoch == 0) {
-    // Wrapped: clear the status words so no stale word can match.
-    cudaMemsetAsync(p->status, 0, p->status_words * sizeof(unsigned long long), st);
-    p->epoch = 1;
-  }
-  return p->epoch;
+// Status words hold 30-bit epochs and every frame consumes kEpochsPerFrame of
+// them; well before the counter wraps, clear the words and the counter
+// (stream-ordered, outside any captured graph).
+void maybe_reset_epochs(gs3d_pipeline* p, cudaStream_t st) {
+  if (++p->frames_since_reset < (1ull << 25)) return;
+  cudaMemsetAsync(p->status, 0, p->status_words * sizeof(unsigned long long), st);
+  cudaMemsetAsync(p->epoch_dev, 0, sizeof(uint32_t), st);
+  p->frames_since_reset = 1;
 }
 
 // Event marking the start of `stage` (stage == GS3D_STAGE_COUNT: end) of the
@@ -264,7 +279,24 @@ void mark(gs3d_pipeline* p, uint32_t stage, cudaStream_t st) {
   cudaEventRecord(p->events[idx], st);
 }
 
+void release_graphs(gs3d_pipeline* p) {
+  for (int g = 0; g < 2; ++g) {
+    if (p->graph_ev_used[g]) cudaEventSynchronize(p->graph_ev[g]);
+    if (p->graph_exec[g]) cudaGraphExecDestroy(p->graph_exec[g]);
+    p->graph_exec[g] = nullptr;
+    if (p->graph_pinned[g]) cudaFreeHost(p->graph_pinned[g]);
+    p->graph_pinned[g] = nullptr;
+    dfree(p->graph_dev[g]);
+    if (p->graph_ev[g]) cudaEventDestroy(p->graph_ev[g]);
+    p->graph_ev[g] = nullptr;
+    p->graph_ev_used[g] = false;
+  }
+  p->graph_views.clear();
+  p->graph_cameras.clear();
+}
+
 void release_all(gs3d_pipeline* p) {
+  release_graphs(p);
   for (cudaEvent_t e : p->events) cudaEventDestroy(e);
   p->events.clear();
   for (uint32_t i = 0; i < kObjectRing; ++i) {
@@ -276,7 +308,7 @@ void release_all(gs3d_pipeline* p) {
   dfree(p->mean); dfree(p->conic); dfree(p->color); dfree(p->counts); dfree(p->keys); dfree(p->vis_off);
   dfree(p->dk[0]); dfree(p->dk[1]); dfree(p->dv[0]); dfree(p->dv[1]); dfree(p->ordered); dfree(p->ioff);
   dfree(p->tk[0]); dfree(p->tk[1]); dfree(p->tv[0]); dfree(p->tv[1]);
-  dfree(p->tile_offsets); dfree(p->tile_order); dfree(p->ctl); dfree(p->output_state); dfree(p->status);
+  dfree(p->tile_offsets); dfree(p->tile_order); dfree(p->ctl); dfree(p->epoch_dev); dfree(p->output_state); dfree(p->status);
 }
 
 }  // namespace
@@ -340,7 +372,7 @@ gs3d_status gs3d_pipeline_create(const gs3d_pipeline_desc* desc, const gs3d_gaus
   }
   cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, p->device);
   for (uint32_t i = 0; i < kObjectRing; ++i) cudaEventCreateWithFlags(&p->stage_ev[i], cudaEventDisableTiming);
-  if ((e = dalloc(p->ctl, 1)) || (e = dalloc(p->output_state, 4))) {
+  if ((e = dalloc(p->ctl, 1)) || (e = dalloc(p->output_state, 4)) || (e = dalloc(p->epoch_dev, 1))) {
     s = cuda_fail(p, e, "allocating control block");
     release_all(p);
     delete p;
@@ -348,6 +380,8 @@ gs3d_status gs3d_pipeline_create(const gs3d_pipeline_desc* desc, const gs3d_gaus
   }
   cudaMemset(p->output_state, 0, 4 * sizeof(uint32_t));
   cudaMemset(p->ctl, 0, sizeof(Control));
+  cudaMemset(p->epoch_dev, 0, sizeof(uint32_t));
+  prepare_sort_kernels();
   if ((s = ensure_slots(p, data->count)) != GS3D_OK || (s = ensure_capacity(p, desc->intersection_capacity)) != GS3D_OK ||
       (s = ensure_stage(p, 16384)) != GS3D_OK) {
     release_all(p);
@@ -372,6 +406,7 @@ gs3d_status gs3d_pipeline_update_data(gs3d_pipeline* p, const gs3d_gaussian_data
   if (s != GS3D_OK) return s;
   cudaSetDevice(p->device);
   if (p->last_stream) cudaStreamSynchronize(p->last_stream);
+  release_graphs(p);
   if ((s = ensure_slots(p, data->count)) != GS3D_OK) return s;
   p->data = *data;
   return GS3D_OK;
@@ -383,6 +418,7 @@ gs3d_status gs3d_pipeline_resize_intersections(gs3d_pipeline* p, uint64_t capaci
     return fail(p, GS3D_ERROR_RANGE, "intersection capacity must be a positive integer below 2^31");
   cudaSetDevice(p->device);
   if (p->last_stream) cudaStreamSynchronize(p->last_stream);
+  release_graphs(p);
   return ensure_capacity(p, capacity);
 }
 
@@ -410,11 +446,16 @@ namespace {
 
 size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
 
-// Validate, lay out and enqueue a batch of views: the whole pass of
-// TiledGaussianPipeline.render (TiledGaussianPipeline.ts:324-341) for every view
-// in one launch sequence.
-gs3d_status enqueue(gs3d_pipeline* p, const gs3d_view* views, uint32_t n, uint32_t attempt, int reset_valid,
-                    cudaStream_t st) {
+struct Plan {
+  uint32_t n = 0;
+  uint32_t items = 0, tiles = 0, blocks = 0;
+  size_t objects = 0;
+  size_t views_off = 0, objects_off = 0, stage_bytes = 0;
+};
+
+// Validate a batch, grow every workspace it needs and lay out its batch
+// table. Not capturable (it may allocate).
+gs3d_status plan_batch(gs3d_pipeline* p, const gs3d_view* views, uint32_t n, Plan* out) {
   if (n == 0 || n > kMaxViews) return fail(p, GS3D_ERROR_RANGE, "a batch holds 1 to 4096 views");
   uint64_t items = 0, tiles = 0, blocks = 0;
   size_t objects = 0;
@@ -439,7 +480,6 @@ gs3d_status enqueue(gs3d_pipeline* p, const gs3d_view* views, uint32_t n, uint32
     objects += v.camera->object_count;
   }
   if (items >= 0xffffffffull || tiles >= 0x7fffffffull) return fail(p, GS3D_ERROR_RANGE, "batch too large");
-
   // Workspaces (grow only; synchronise before freeing buffers a queued frame may use).
   if (items > p->slot_cap || tiles + 1 > p->tile_cap ||
       status_words_needed((uint32_t)items, p->capacity) > p->status_words) {
@@ -449,22 +489,32 @@ gs3d_status enqueue(gs3d_pipeline* p, const gs3d_view* views, uint32_t n, uint32
   if (s != GS3D_OK) return s;
   if ((s = ensure_status(p)) != GS3D_OK) return s;
   if ((s = ensure_tiles(p, tiles)) != GS3D_OK) return s;
+  out->n = n;
+  out->items = (uint32_t)items;
+  out->tiles = (uint32_t)tiles;
+  out->blocks = (uint32_t)blocks;
+  out->objects = objects;
+  const size_t header = 16 + align16(3 * (size_t)(n + 1) * sizeof(uint32_t));
+  out->views_off = header;
+  out->objects_off = align16(header + (size_t)n * sizeof(ViewDesc));
+  out->stage_bytes = out->objects_off + objects * 40 * sizeof(float);
+  return GS3D_OK;
+}
 
-  // Batch table: bases, view descriptors, object tables; one H2D copy.
-  const size_t bases_bytes = align16(3 * (size_t)(n + 1) * sizeof(uint32_t));
-  const size_t views_off = bases_bytes;
-  const size_t objects_off = align16(views_off + (size_t)n * sizeof(ViewDesc));
-  const size_t stage_bytes = objects_off + objects * 40 * sizeof(float);
-  if ((s = ensure_stage(p, stage_bytes)) != GS3D_OK) return s;
-  const uint32_t slot = p->frame_index++ % kObjectRing;
-  if (p->stage_ev_used[slot]) cudaEventSynchronize(p->stage_ev[slot]);
-  unsigned char* host = p->stage_pinned[slot];
-  unsigned char* dev = p->stage_dev[slot];
-  uint32_t* h_item = (uint32_t*)host;
+// Fill a host copy of the batch table whose device copy will live at `dev`:
+// frame parameters, the three base arrays, view descriptors, object tables.
+void stage_batch(gs3d_pipeline* p, const gs3d_view* views, const Plan& pl, uint32_t attempt, int reset_valid,
+                 unsigned char* host, unsigned char* dev) {
+  const uint32_t n = pl.n;
+  uint32_t* params = (uint32_t*)host;
+  params[0] = attempt;
+  params[1] = reset_valid ? 1u : 0u;
+  params[2] = params[3] = 0u;
+  uint32_t* h_item = params + 4;
   uint32_t* h_tile = h_item + (n + 1);
   uint32_t* h_block = h_tile + (n + 1);
-  ViewDesc* h_views = (ViewDesc*)(host + views_off);
-  float* h_obj = (float*)(host + objects_off);
+  ViewDesc* h_views = (ViewDesc*)(host + pl.views_off);
+  float* h_obj = (float*)(host + pl.objects_off);
   uint32_t item = 0, tile = 0, block = 0;
   size_t obj = 0;
   p->item_bases.assign(n + 1, 0);
@@ -478,7 +528,7 @@ gs3d_status enqueue(gs3d_pipeline* p, const gs3d_view* views, uint32_t n, uint32
     w.shape = (const uint2*)d.scales_opacity;
     w.rot = (const uint32_t*)d.rotations;
     w.sh = (const uint32_t*)d.sh_coefficients;
-    w.objects = (const float*)(dev + objects_off) + obj * 40;
+    w.objects = (const float*)(dev + pl.objects_off) + obj * 40;
     w.color = v.targets.color;
     w.depth = v.targets.depth;
     w.count = d.count;
@@ -517,17 +567,22 @@ gs3d_status enqueue(gs3d_pipeline* p, const gs3d_view* views, uint32_t n, uint32
   p->tile_bases[n] = tile;
   p->total_items = item;
   p->total_tiles = tile;
-  cudaMemcpyAsync(dev, host, stage_bytes, cudaMemcpyHostToDevice, st);
+}
 
+// Enqueue the pass over a staged batch table at `dev` (capturable: launches
+// and memsets only).
+void record_batch(gs3d_pipeline* p, const Plan& pl, unsigned char* dev, cudaStream_t st) {
+  const uint32_t n = pl.n;
   BatchView bv;
-  bv.item_base = (const uint32_t*)dev;
+  bv.frame_params = (const uint32_t*)dev;
+  bv.item_base = bv.frame_params + 4;
   bv.tile_base = bv.item_base + (n + 1);
   bv.block_base = bv.tile_base + (n + 1);
-  bv.views = (const ViewDesc*)(dev + views_off);
+  bv.views = (const ViewDesc*)(dev + pl.views_off);
   bv.nviews = n;
-  bv.total_items = item;
-  bv.total_tiles = tile;
-  bv.total_blocks = block;
+  bv.total_items = pl.items;
+  bv.total_tiles = pl.tiles;
+  bv.total_blocks = pl.blocks;
 
   PassOptions o;
   memset(&o, 0, sizeof(o));
@@ -544,27 +599,32 @@ gs3d_status enqueue(gs3d_pipeline* p, const gs3d_view* views, uint32_t n, uint32
   o.depth_alpha_threshold = p->desc.depth_alpha_threshold;
   o.invalid_depth = p->desc.invalid_depth_value;
 
-  const uint32_t N = item;
+  const uint32_t N = pl.items;
+  const uint32_t tile = pl.tiles;
   uint32_t launches = 0;
   Control* ctl = p->ctl;
+  uint32_t ep = 0;  // look-back launch index within the frame
+  auto epoch = [&]() { return Epoch{p->epoch_dev, ++ep}; };
+  launch_epoch_begin(p->epoch_dev, st);
   cudaMemsetAsync(ctl, 0, sizeof(Control), st);
+  launches += 1;
 
   // K1: projection.
   mark(p, GS3D_STAGE_PROJECT, st);
   launch_project(bv, o, p->mean, p->conic, p->color, p->counts, p->keys, 3, st);
-  launches += block ? 1 : 0;
+  launches += pl.blocks ? 1 : 0;
   // Visibility compaction.
   mark(p, GS3D_STAGE_COMPACT, st);
   const int depth_passes = p->desc.depth_sort_mode == GS3D_DEPTH_FLOAT32 ? 4 : 2;
-  launch_compact(p->keys, N, p->vis_off, p->dk[0], p->dv[0], ctl, p->status, next_epoch(p, st), depth_passes, st);
+  launch_compact(p->keys, N, p->vis_off, p->dk[0], p->dv[0], ctl, p->status, epoch(), depth_passes, st);
   ++launches;
   // Depth sort.
   mark(p, GS3D_STAGE_DEPTH_SORT, st);
   int cur = 0;
   for (int pass = 0; pass < depth_passes; ++pass) {
     launch_onesweep(8, p->dk[cur], p->dv[cur], p->dk[cur ^ 1], p->dv[cur ^ 1], &ctl->visible_state[0], N, 8 * pass,
-                    ctl->depth_hist[pass], p->status, &ctl->tickets[kTicketSortBase + pass], next_epoch(p, st),
-                    &ctl->error, st);
+                    ctl->depth_hist[pass], p->status, &ctl->tickets[kTicketSortBase + pass], epoch(), &ctl->error,
+                    st);
     cur ^= 1;
     ++launches;
   }
@@ -572,8 +632,8 @@ gs3d_status enqueue(gs3d_pipeline* p, const gs3d_view* views, uint32_t n, uint32
   // Ordered counts + saturating scan + dispatch/output state.
   mark(p, GS3D_STAGE_SCAN, st);
   const uint32_t cap32 = (uint32_t)p->capacity;
-  launch_scan_counts(p->dv[cur], p->counts, N, p->ordered, p->ioff, ctl, p->status, next_epoch(p, st), cap32,
-                     attempt, reset_valid, p->output_state, st);
+  launch_scan_counts(p->dv[cur], p->counts, N, p->ordered, p->ioff, ctl, p->status, epoch(), cap32,
+                     bv.frame_params, p->output_state, st);
   ++launches;
   // Emission + tile-sort histograms.
   mark(p, GS3D_STAGE_EMIT, st);
@@ -588,13 +648,13 @@ gs3d_status enqueue(gs3d_pipeline* p, const gs3d_view* views, uint32_t n, uint32
   int tcur = 0;
   for (int pass = 0; pass < tile_passes; ++pass) {
     launch_onesweep(digit_bits, p->tk[tcur], p->tv[tcur], p->tk[tcur ^ 1], p->tv[tcur ^ 1], &ctl->state[0], cap32,
-                    digit_bits * pass, ctl->tile_hist[pass], p->status,
-                    &ctl->tickets[kTicketSortBase + 4 + pass], next_epoch(p, st), &ctl->error, st);
+                    digit_bits * pass, ctl->tile_hist[pass], p->status, &ctl->tickets[kTicketSortBase + 4 + pass],
+                    epoch(), &ctl->error, st);
     tcur ^= 1;
     ++launches;
   }
   p->tile_final = tcur;
-  // Tile ranges.
+  // Tile ranges and the raster work list.
   mark(p, GS3D_STAGE_RANGES, st);
   launch_tile_ranges(p->tk[tcur], ctl, tile, p->tile_offsets, p->sms, st);
   ++launches;
@@ -605,13 +665,28 @@ gs3d_status enqueue(gs3d_pipeline* p, const gs3d_view* views, uint32_t n, uint32
   launch_raster((int)p->desc.raster_precision, p->tile_offsets, p->tile_order, p->tv[tcur], p->mean, p->conic,
                 p->color, bv, o, ctl, p->desc.raster_stats != 0, st);
   ++launches;
-
   mark(p, GS3D_STAGE_COUNT, st);
   if (p->profiling) ++p->profiled;
+  p->last_launches = launches;
+}
+
+// The whole pass of TiledGaussianPipeline.render (TiledGaussianPipeline.ts:324-341)
+// for every view of a batch in one launch sequence.
+gs3d_status enqueue(gs3d_pipeline* p, const gs3d_view* views, uint32_t n, uint32_t attempt, int reset_valid,
+                    cudaStream_t st) {
+  Plan pl;
+  gs3d_status s = plan_batch(p, views, n, &pl);
+  if (s != GS3D_OK) return s;
+  if ((s = ensure_stage(p, pl.stage_bytes)) != GS3D_OK) return s;
+  const uint32_t slot = p->frame_index++ % kObjectRing;
+  if (p->stage_ev_used[slot]) cudaEventSynchronize(p->stage_ev[slot]);
+  stage_batch(p, views, pl, attempt, reset_valid, p->stage_pinned[slot], p->stage_dev[slot]);
+  maybe_reset_epochs(p, st);
+  cudaMemcpyAsync(p->stage_dev[slot], p->stage_pinned[slot], pl.stage_bytes, cudaMemcpyHostToDevice, st);
+  record_batch(p, pl, p->stage_dev[slot], st);
   cudaEventRecord(p->stage_ev[slot], st);
   p->stage_ev_used[slot] = true;
   p->last_stream = st;
-  p->last_launches = launches;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(p, e, "launching the pass");
   return GS3D_OK;
@@ -643,6 +718,85 @@ gs3d_status gs3d_pipeline_render_batch(gs3d_pipeline* p, const gs3d_view* views,
   cudaSetDevice(p->device);
   p->prepared = true;
   return enqueue(p, views, count, attempt, reset_valid, (cudaStream_t)stream);
+}
+
+gs3d_status gs3d_pipeline_capture_graph(gs3d_pipeline* p, const gs3d_view* views, uint32_t count, void* stream) {
+  if (!p || !views) return GS3D_ERROR_INVALID_ARGUMENT;
+  if (p->profiling) return fail(p, GS3D_ERROR_UNSUPPORTED, "disable profiling before capturing a graph");
+  cudaSetDevice(p->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (!st) return fail(p, GS3D_ERROR_INVALID_ARGUMENT, "graph capture needs a non-default stream");
+  if (p->last_stream) cudaStreamSynchronize(p->last_stream);
+  release_graphs(p);
+  Plan pl;
+  gs3d_status s = plan_batch(p, views, count, &pl);
+  if (s != GS3D_OK) return s;
+  for (int g = 0; g < 2; ++g) {
+    cudaError_t e = cudaMallocHost((void**)&p->graph_pinned[g], pl.stage_bytes);
+    if (e == cudaSuccess) e = dalloc(p->graph_dev[g], pl.stage_bytes);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->graph_ev[g], cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+      release_graphs(p);
+      return cuda_fail(p, e, "allocating graph staging");
+    }
+    cudaGraph_t graph = nullptr;
+    e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+      release_graphs(p);
+      return cuda_fail(p, e, "beginning stream capture");
+    }
+    record_batch(p, pl, p->graph_dev[g], st);
+    e = cudaStreamEndCapture(st, &graph);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&p->graph_exec[g], graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+      release_graphs(p);
+      return cuda_fail(p, e, "capturing the pass");
+    }
+  }
+  p->graph_stage_bytes = pl.stage_bytes;
+  p->prepared = true;
+  p->graph_views.assign(views, views + count);
+  p->graph_cameras.resize(count);
+  p->graph_launches = p->last_launches;
+  p->graph_next = 0;
+  return GS3D_OK;
+}
+
+gs3d_status gs3d_pipeline_launch_graph(gs3d_pipeline* p, const gs3d_camera* cameras, uint32_t count,
+                                       uint32_t attempt, int reset_valid, void* stream) {
+  if (!p || !cameras) return GS3D_ERROR_INVALID_ARGUMENT;
+  if (!p->graph_exec[0]) return fail(p, GS3D_ERROR_NOT_PREPARED, "no captured graph");
+  if (count != p->graph_views.size()) return fail(p, GS3D_ERROR_INVALID_ARGUMENT, "camera count differs from the capture");
+  cudaSetDevice(p->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  for (uint32_t i = 0; i < count; ++i) {
+    if (cameras[i].object_count != p->graph_views[i].camera->object_count)
+      return fail(p, GS3D_ERROR_INVALID_ARGUMENT, "object count differs from the capture");
+    p->graph_cameras[i] = cameras[i];
+    p->graph_views[i].camera = &p->graph_cameras[i];
+  }
+  const int g = (int)(p->graph_next++ & 1u);
+  if (p->graph_ev_used[g]) cudaEventSynchronize(p->graph_ev[g]);
+  Plan pl;
+  pl.n = count;
+  pl.items = 0;
+  size_t objects = 0;
+  for (uint32_t i = 0; i < count; ++i) objects += cameras[i].object_count;
+  const size_t header = 16 + align16(3 * (size_t)(count + 1) * sizeof(uint32_t));
+  pl.views_off = header;
+  pl.objects_off = align16(header + (size_t)count * sizeof(ViewDesc));
+  pl.stage_bytes = pl.objects_off + objects * 40 * sizeof(float);
+  stage_batch(p, p->graph_views.data(), pl, attempt, reset_valid, p->graph_pinned[g], p->graph_dev[g]);
+  maybe_reset_epochs(p, st);
+  cudaMemcpyAsync(p->graph_dev[g], p->graph_pinned[g], pl.stage_bytes, cudaMemcpyHostToDevice, st);
+  cudaError_t e = cudaGraphLaunch(p->graph_exec[g], st);
+  cudaEventRecord(p->graph_ev[g], st);
+  p->graph_ev_used[g] = true;
+  p->last_stream = st;
+  p->last_launches = p->graph_launches;
+  if (e != cudaSuccess) return cuda_fail(p, e, "launching the graph");
+  return GS3D_OK;
 }
 
 gs3d_status gs3d_pipeline_batch_layout(gs3d_pipeline* p, uint32_t* item_base, uint32_t* tile_base,

@@ -55,7 +55,7 @@ __global__ void __launch_bounds__(kBlock, 3)
     k_onesweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
                uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, const uint32_t* __restrict__ n_ptr,
                int shift, const uint32_t* __restrict__ hist, unsigned long long* __restrict__ status,
-               uint32_t* __restrict__ ticket, uint32_t epoch, uint32_t* __restrict__ err) {
+               uint32_t* __restrict__ ticket, Epoch ep, uint32_t* __restrict__ err) {
   constexpr uint32_t RADIX = 1u << BITS;
   constexpr uint32_t MASK = RADIX - 1u;
   __shared__ uint32_t s_warp_hist[kSortWarps][RADIX];
@@ -77,6 +77,7 @@ __global__ void __launch_bounds__(kBlock, 3)
   const uint32_t tile = s_tile;
   const uint32_t base = tile * kSortTile;
   if (base >= n) return;
+  const uint32_t epoch = ep.get();
   const uint32_t wbase = base + warp * 32u * kSortItems;
 
   // Keys into registers (warp-striped: item j*32+lane of the warp's
@@ -183,21 +184,24 @@ constexpr size_t kSortDynSmem = 3 * kSortTile * sizeof(uint32_t);
 template <int B>
 void launch_bits(uint32_t grid, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
                  uint32_t* vals_out, const uint32_t* n_ptr, int shift, const uint32_t* hist,
-                 unsigned long long* status, uint32_t* ticket, uint32_t epoch, uint32_t* err, cudaStream_t st) {
-  static bool configured[64] = {};  // opt-in to >48 KB shared memory, once per device
-  int dev = 0;
-  cudaGetDevice(&dev);
-  if (dev < 0 || dev >= 64 || !configured[dev]) {
-    cudaFuncSetAttribute(k_onesweep<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSortDynSmem);
-    if (dev >= 0 && dev < 64) configured[dev] = true;
-  }
+                 unsigned long long* status, uint32_t* ticket, Epoch epoch, uint32_t* err, cudaStream_t st) {
   k_onesweep<B><<<grid, kBlock, kSortDynSmem, st>>>(keys_in, vals_in, keys_out, vals_out, n_ptr, shift, hist, status,
                                                     ticket, epoch, err);
 }
 
+template <int B>
+void configure_bits() {
+  cudaFuncSetAttribute(k_onesweep<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSortDynSmem);
+}
+
+void prepare_sort_kernels() {
+  configure_bits<1>(); configure_bits<2>(); configure_bits<3>(); configure_bits<4>();
+  configure_bits<5>(); configure_bits<6>(); configure_bits<7>(); configure_bits<8>();
+}
+
 void launch_onesweep(int bits, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
                      uint32_t* vals_out, const uint32_t* n_ptr, uint32_t n_max, int shift, const uint32_t* hist,
-                     unsigned long long* status, uint32_t* ticket, uint32_t epoch, uint32_t* err, cudaStream_t st) {
+                     unsigned long long* status, uint32_t* ticket, Epoch epoch, uint32_t* err, cudaStream_t st) {
   const uint32_t grid = n_max == 0 ? 1u : (uint32_t)(((uint64_t)n_max + kSortTile - 1) / kSortTile);
 #define GS_SWEEP(B)                                                                                      \
   case B:                                                                                                \

@@ -220,6 +220,17 @@ typedef struct gs3d_view {
  * is published and the output state reports the batch's demand. */
 gs3d_status gs3d_pipeline_render_batch(gs3d_pipeline* pipeline, const gs3d_view* views, uint32_t count,
                                        uint32_t attempt, int reset_valid, void* stream);
+/* Capture the batched pass for these views (scenes, sizes, targets and object
+ * counts fixed) into CUDA graphs; gs3d_pipeline_launch_graph then replays it
+ * with new cameras: one graph launch per frame instead of ~20 launches.
+ * `stream` must be a non-default stream; profiling must be off. Any
+ * update_data/resize_intersections drops the graphs. Two graph instances
+ * alternate over two staging buffers, so the host prepares frame N+1 while
+ * frame N runs. */
+gs3d_status gs3d_pipeline_capture_graph(gs3d_pipeline* pipeline, const gs3d_view* views, uint32_t count,
+                                        void* stream);
+gs3d_status gs3d_pipeline_launch_graph(gs3d_pipeline* pipeline, const gs3d_camera* cameras, uint32_t count,
+                                       uint32_t attempt, int reset_valid, void* stream);
 /* item_base/tile_base of the last render (count + 1 entries each). */
 gs3d_status gs3d_pipeline_batch_layout(gs3d_pipeline* pipeline, uint32_t* item_base, uint32_t* tile_base,
                                        uint32_t capacity, uint32_t* count);
