@@ -275,8 +275,9 @@ def main() -> None:
             launches += plain.last_launch_count()
         return launches
 
-    def timed(step, pipe_for_stages):
+    def timed(step, pipe_for_stages, stream_for_timing=None):
         """Device time of exactly `steps` steps, per-stage events on."""
+        stream_for_timing = stream_for_timing or torch.cuda.current_stream()
         for _ in range(max(args.warmup, 3)):
             step()
         torch.cuda.synchronize()
@@ -287,11 +288,11 @@ def main() -> None:
         torch.cuda.synchronize()
         clocks.start()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
+        e0.record(stream_for_timing)
         nl = 0
         for _ in range(args.steps):
             nl += step()
-        e1.record()
+        e1.record(stream_for_timing)
         torch.cuda.synchronize()
         ck = clocks.stop()
         barrier()
@@ -311,12 +312,32 @@ def main() -> None:
     batched = P.TiledGaussianPipeline(ds.data(), {"raster_precision": args.precision,
                                                   "intersection_capacity": int(demand * 1.25 * ncam) + 256})
     views = [(data, cam, W, H, colors[i].data_ptr(), 0, "rgba16f") for i, cam in enumerate(cams)]
+    gstream = torch.cuda.Stream()
+    batched.render_batch(views)  # size the workspaces, then capture the pass as a graph
+    torch.cuda.synchronize()
+    batched.capture_graph(views, gstream.cuda_stream)
 
     def step_batched():
         batched.render_batch(views)
         return batched.last_launch_count()
 
+    def step_graph():
+        with torch.cuda.stream(gstream):
+            batched.launch_graph(cams, stream=gstream.cuda_stream)
+        return batched.last_launch_count()
+
     ms_total, stage_ms, profiled, launches, clock_info = timed(step_batched, batched)
+    # Same batches replayed from the captured graph (no per-stage events).
+    for _ in range(3):
+        step_graph()
+    torch.cuda.synchronize()
+    g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    g0.record(gstream)
+    for _ in range(args.steps):
+        step_graph()
+    g1.record(gstream)
+    torch.cuda.synchronize()
+    fps_graph = args.steps * ncam * world / (g0.elapsed_time(g1) / 1000.0)
     fps = args.steps * ncam * world / (ms_total / 1000.0)
     bstats = batched.read_stats()
 
@@ -336,7 +357,11 @@ def main() -> None:
 
     p50_plain, p99_plain = latencies(lambda i: plain.render(cams[i % ncam], colors[0].data_ptr(), 0,
                                                             color_format="rgba16f"), args.latency_frames)
-    p50, p99 = latencies(lambda i: batched.render_batch(views), max(20, args.latency_frames // ncam))
+    def batch_once(i):
+        with torch.cuda.stream(gstream):
+            batched.launch_graph(cams, stream=gstream.cuda_stream)
+
+    p50, p99 = latencies(batch_once, max(20, args.latency_frames // ncam))
 
     # End to end through the public API (batched form): camera/object tables
     # from host memory in, every rendered rgba16f image back to pinned host
@@ -345,9 +370,10 @@ def main() -> None:
     barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        batched.render_batch(views)
-        for c in colors:
-            host.copy_(c, non_blocking=True)
+        with torch.cuda.stream(gstream):
+            batched.launch_graph(cams, stream=gstream.cuda_stream)
+            for c in colors:
+                host.copy_(c, non_blocking=True)
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     if world > 1:
@@ -413,6 +439,7 @@ def main() -> None:
                    "visible_mean": v, "intersections_mean": inter},
         "p50_ms": p50, "p99_ms": p99, "psnr_db_vs_fp64": psnr_db,
         "forms": {"batched": {"precision": args.precision, "frames_per_s": fps, "views_per_batch": ncam,
+                              "graph_replay_frames_per_s": fps_graph,
                               "p50_batch_ms": p50, "p99_batch_ms": p99, "psnr_db": psnr_db,
                               "stats": bstats},
                   "plain": {"precision": args.plain_precision, "frames_per_s": fps_plain,
