@@ -5,12 +5,21 @@
 // 128 threads per 16x16 tile; each thread owns two pixels of one column,
 // (x, y) and (x, y + 4), so warp w owns the 8x8 patch at (8 (w & 1), 8 (w >> 1)).
 // The two pixels share dx and the x-only terms of the quadratic, the record
-// loads, the culling test and the loop. Per record and pixel pair:
-//   FP32   dx, dy0, dy1 and the base-2 exponent of each pixel (the conic is
-//          pre-scaled by -1/2 log2 e while staging)
-//   half2  exp2 of both exponents (ex2.approx.f16x2) and alpha = min(op e, 0.99)
+// loads, the culling test and the loop.
+//
+// Per record the staging thread folds the opacity into the exponent:
+//   p' = log2(opacity) - (a dx^2 + 2 b dx dy + c dy^2) / 2 * log2(e)
+// so alpha = min(opacity e^power, 0.99) = 2^min(p', L), L = min(log2 opacity,
+// log2 0.99), and the reference's alpha >= 1/255 test is p' >= log2(1/255).
+// Per record and pixel pair:
+//   FP32   dx, dy0, dy1, p'0, p'1 and the two threshold compares
+//   half2  min(p', L) and its exp2 (ex2.approx.f16x2)
 //   FP32   transmittance and colour/depth accumulation
-// A pixel blends a record only when its exponent clears the 1/255 threshold.
+// Each warp walks a compacted list of the records whose support can reach
+// its 8x8 patch. A pixel's transmittance is tested against the threshold once
+// per 32 listed records; a pixel found done stops blending from there on (its
+// threshold becomes +inf), so it may blend up to 31 records more than the
+// reference, whose contributions sum to less than the threshold.
 #pragma once
 
 #include <cuda_fp16.h>
@@ -20,6 +29,8 @@
 namespace gs {
 
 constexpr int kHalfThreads = 128;
+constexpr float kLog2MinAlpha = -7.99435329f;  // log2(1/255)
+constexpr float kLog2MaxAlpha = -0.01449957f;  // log2(0.99)
 
 __device__ __forceinline__ __half2 h2ex2_approx(__half2 x) {
   uint32_t in = *reinterpret_cast<uint32_t*>(&x), out;
@@ -28,24 +39,28 @@ __device__ __forceinline__ __half2 h2ex2_approx(__half2 x) {
 }
 
 struct HalfBatch {
-  float4 geo[kBlock];  // cx, cy, opacity, threshold * log2 e
-  float4 con[kBlock];  // -a/2 log2 e, -b log2 e, -c/2 log2 e, depth
+  float4 geo[kBlock];  // cx, cy, -a/2 log2 e, -b log2 e
+  float4 con[kBlock];  // -c/2 log2 e, log2 opacity, L as half2 bits, depth
   float4 col[kBlock];
   float4 raw[kBlock];  // conic (a, b, c) for periodic boundaries
   uint8_t mask[kBlock];
+  uint8_t list[kHalfThreads / 32][kBlock];  // per warp: staged records that can reach its patch
 };
 
 // Which of the tile's four 8x8 warp patches can hold a pixel centre inside the
-// splat's support (same conservative box as patch_mask).
+// splat's support: the support's bounding box, widened by 5% and a quarter
+// pixel (which also covers the approximate square roots), against each patch.
+// Near-degenerate conics (condition number above about 4e4) reach every patch.
 __device__ __forceinline__ uint32_t patch_mask8(float cx, float cy, float ca, float cb, float cc, float thr,
                                                 float tile_x0, float tile_y0, uint32_t axis) {
   if (axis != 0u) return 0xfu;
   const float det = ca * cc - cb * cb;
   const float tr = ca + cc;
   if (!(det > 0.0f) || !(tr * tr <= 4e4f * det) || !(thr >= 0.0f)) return 0xfu;
-  const float q = 2.0f * thr;
-  const float hx = sqrtf(q * cc / det) * 1.05f + 0.25f;
-  const float hy = sqrtf(q * ca / det) * 1.05f + 0.25f;
+  const float q = __fdividef(2.0f * thr, det);
+  const float xx = q * cc, yy = q * ca;
+  const float hx = xx * rsqrtf(xx) * 1.05f + 0.25f;  // 0 gives NaN: every patch
+  const float hy = yy * rsqrtf(yy) * 1.05f + 0.25f;
   if (!(hx < 1e30f) || !(hy < 1e30f)) return 0xfu;
   uint32_t m = 0;
 #pragma unroll
@@ -79,7 +94,7 @@ __device__ __forceinline__ void blend_range_h2(uint32_t begin, uint32_t source_c
   const bool count0 = STATS && !done0, count1 = STATS && !done1;
   uint32_t stop0 = s1, stop1 = s1;
   const float pyc1 = pyc0 + 4.0f;
-  const __half2 cap = __float2half2_rn(0.99f);
+  const uint32_t lt = (1u << lane) - 1u;
   for (uint32_t b = s0; b < s1; b += kBlock) {
     if (!__syncthreads_or(!(done0 && done1))) break;
 #pragma unroll
@@ -92,24 +107,36 @@ __device__ __forceinline__ void blend_range_h2(uint32_t begin, uint32_t source_c
         const uint32_t g = __ldg(ids + begin + src);
         const float4 m = __ldg(mean + g);
         const float4 c = __ldg(conic + g);
-        const float thr = __logf(m.w * 255.0f);
-        sb.geo[slot] = make_float4(m.x, m.y, m.w, thr * kLog2e);
-        sb.con[slot] = make_float4(-0.5f * kLog2e * c.x, -kLog2e * c.y, -0.5f * kLog2e * c.z, m.z);
+        const float log2op = __log2f(m.w);
+        const float thr = (log2op + 7.99435329f) * 0.693147181f;  // ln(opacity * 255)
+        const __half2 lim = __float2half2_rn(fminf(log2op, kLog2MaxAlpha));
+        sb.geo[slot] = make_float4(m.x, m.y, -0.5f * kLog2e * c.x, -kLog2e * c.y);
+        sb.con[slot] = make_float4(-0.5f * kLog2e * c.z, log2op, __uint_as_float(*reinterpret_cast<const uint32_t*>(&lim)),
+                                   m.z);
         if (PERIODIC) sb.raw[slot] = c;
         sb.col[slot] = __ldg(color + g);
         sb.mask[slot] = (uint8_t)patch_mask8(m.x, m.y, c.x, c.y, c.z, thr, tile_x0, tile_y0, f.axis);
       }
     }
     __syncthreads();
+    // This warp's list of records that can reach its patch, in record order.
     const uint32_t n = min((uint32_t)kBlock, s1 - b);
-    for (uint32_t base = 0; base < n; base += 32) {
+    uint32_t cnt = 0;
+    for (uint32_t k0 = 0; k0 < n; k0 += 32) {
+      const uint32_t k = k0 + lane;
+      const bool reach = k < n && ((sb.mask[k] >> warp) & 1u);
+      const uint32_t bal = __ballot_sync(0xffffffffu, reach);
+      if (reach) sb.list[warp][cnt + __popc(bal & lt)] = (uint8_t)k;
+      cnt += __popc(bal);
+    }
+    __syncwarp();
+    for (uint32_t i0 = 0; i0 < cnt; i0 += 32) {
       if (__all_sync(0xffffffffu, done0 && done1)) break;
-      const uint32_t k = base + lane;
-      uint32_t bits = __ballot_sync(0xffffffffu, k < n && ((sb.mask[k] >> warp) & 1u));
-      while (bits) {
-        const uint32_t j = base + (uint32_t)(__ffs(bits) - 1);
-        bits &= bits - 1u;
-        if (done0 && done1) continue;
+      const float th0 = done0 ? __int_as_float(0x7f800000) : kLog2MinAlpha;
+      const float th1 = done1 ? __int_as_float(0x7f800000) : kLog2MinAlpha;
+      const uint32_t iend = min(i0 + 32u, cnt);
+      for (uint32_t i = i0; i < iend; ++i) {
+        const uint32_t j = sb.list[warp][i];
         const float4 g = sb.geo[j];
         const float4 c = sb.con[j];
         float p0, p1;
@@ -118,38 +145,39 @@ __device__ __forceinline__ void blend_range_h2(uint32_t begin, uint32_t source_c
           float dx0, dy0, dx1, dy1;
           boundary_delta<true>(pxc, pyc0, g.x, g.y, r.x, r.y, r.z, f, &dx0, &dy0);
           boundary_delta<true>(pxc, pyc1, g.x, g.y, r.x, r.y, r.z, f, &dx1, &dy1);
-          p0 = fmaf(c.x * dx0, dx0, fmaf(c.y * dx0, dy0, (c.z * dy0) * dy0));
-          p1 = fmaf(c.x * dx1, dx1, fmaf(c.y * dx1, dy1, (c.z * dy1) * dy1));
+          p0 = fmaf(g.z * dx0, dx0, fmaf(g.w * dx0, dy0, fmaf(c.x * dy0, dy0, c.y)));
+          p1 = fmaf(g.z * dx1, dx1, fmaf(g.w * dx1, dy1, fmaf(c.x * dy1, dy1, c.y)));
         } else {
           const float dx = pxc - g.x;
           const float dy0 = pyc0 - g.y, dy1 = pyc1 - g.y;
-          const float bdx = c.y * dx, xx = (c.x * dx) * dx;
-          p0 = fmaf(fmaf(c.z, dy0, bdx), dy0, xx);
-          p1 = fmaf(fmaf(c.z, dy1, bdx), dy1, xx);
+          const float bdx = g.w * dx, xx = fmaf(g.z * dx, dx, c.y);
+          p0 = fmaf(fmaf(c.x, dy0, bdx), dy0, xx);
+          p1 = fmaf(fmaf(c.x, dy1, bdx), dy1, xx);
         }
-        const bool use0 = !done0 && p0 >= -g.w;
-        const bool use1 = !done1 && p1 >= -g.w;
+        const bool use0 = p0 >= th0;
+        const bool use1 = p1 >= th1;
         if (!(use0 || use1)) continue;
-        const __half2 e = h2ex2_approx(__floats2half2_rn(fminf(p0, 0.0f), fminf(p1, 0.0f)));
-        const float2 al = __half22float2(__hmin2(__hmul2(__float2half2_rn(g.z), e), cap));
+        const uint32_t lim_bits = __float_as_uint(c.z);
+        const __half2 e = h2ex2_approx(__hmin2(__floats2half2_rn(p0, p1), *reinterpret_cast<const __half2*>(&lim_bits)));
+        const float2 al = __half22float2(e);
         const float4 col = sb.col[j];
         if (use0) {
           blend_pixel(al.x, col, c.w, a0);
-          if (STATS) ++c0n.blended;
-          if (a0.t < f.t_threshold) {
-            done0 = true;
-            if (STATS) stop0 = b + j + 1;
+          if (STATS) {
+            ++c0n.blended;
+            if (a0.t < f.t_threshold && stop0 == s1) stop0 = b + j + 1;
           }
         }
         if (use1) {
           blend_pixel(al.y, col, c.w, a1);
-          if (STATS) ++c1n.blended;
-          if (a1.t < f.t_threshold) {
-            done1 = true;
-            if (STATS) stop1 = b + j + 1;
+          if (STATS) {
+            ++c1n.blended;
+            if (a1.t < f.t_threshold && stop1 == s1) stop1 = b + j + 1;
           }
         }
       }
+      done0 = done0 || a0.t < f.t_threshold;
+      done1 = done1 || a1.t < f.t_threshold;
     }
   }
   __syncthreads();
@@ -180,7 +208,7 @@ __device__ __forceinline__ void store_pixel(const ViewDesc& v, const PassOptions
 }
 
 template <bool PERIODIC, bool STATS>
-__global__ void __launch_bounds__(kHalfThreads) k_raster_h2(const uint32_t* __restrict__ tile_offsets,
+__global__ void __launch_bounds__(kHalfThreads, 6) k_raster_h2(const uint32_t* __restrict__ tile_offsets,
                                                            const uint32_t* __restrict__ order,
                                                            const uint32_t* __restrict__ ids,
                                                            const float4* __restrict__ mean,
