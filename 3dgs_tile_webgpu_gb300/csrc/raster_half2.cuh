@@ -29,8 +29,6 @@
 namespace gs {
 
 constexpr int kHalfThreads = 128;
-constexpr float kLog2MinAlpha = -7.99435329f;  // log2(1/255)
-constexpr float kLog2MaxAlpha = -0.01449957f;  // log2(0.99)
 
 __device__ __forceinline__ __half2 h2ex2_approx(__half2 x) {
   uint32_t in = *reinterpret_cast<uint32_t*>(&x), out;

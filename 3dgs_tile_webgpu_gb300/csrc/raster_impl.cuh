@@ -27,10 +27,11 @@
 //  * ExactMath: the reference's expressions and tests in their order, with the
 //    deterministic exp/log; bit-identical to the CPU restatement when the
 //    translation unit is built with --fmad=false.
-//  * FastMath: staging folds -1/2 and log2(e) into the conic so one fused
-//    quadratic gives the exponent in base 2, one compare rejects splats below
-//    the 1/255 threshold before the exponential (ex2.approx), and
-//    transmittance is updated as T - T*alpha.
+//  * FastMath (blend_range_fast): staging folds -1/2, log2(e) and the opacity
+//    into the quadratic so it gives log2(alpha) directly, one compare rejects
+//    splats below the 1/255 threshold before the exponential (ex2.approx),
+//    each warp walks a compacted list of its records, transmittance is
+//    updated as T - T*alpha and tested once per 32 listed records.
 #pragma once
 
 #include <cuda_fp16.h>
@@ -108,16 +109,20 @@ struct PixelAcc {
 };
 
 // Shared batch. Exact form: geo = (cx, cy, opacity, threshold), con = (a, b, c,
-// depth). Fast form: geo = (cx, cy, opacity, threshold * log2 e),
-// con = (-a/2 log2 e, -b log2 e, -c/2 log2 e, depth), with the conic of the
-// periodic form kept as (a, b, c) in raw[].
+// depth). Fast form: geo = (cx, cy, -a/2 log2 e, -b log2 e), con = (-c/2 log2 e,
+// log2 opacity, min(log2 opacity, log2 0.99), depth), with the conic of the
+// periodic form kept as (a, b, c) in raw[] and per-warp record lists.
 struct Batch {
   float4 geo[kBlock];
   float4 con[kBlock];
   float4 col[kBlock];
   float4 raw[kBlock];
   uint8_t mask[kBlock];
+  uint8_t list[kBlock / 32][kBlock];
 };
+
+constexpr float kLog2MinAlpha = -7.99435329f;  // log2(1/255)
+constexpr float kLog2MaxAlpha = -0.01449957f;  // log2(0.99)
 
 // Which of the tile's eight 8x4 warp patches can hold a pixel centre inside
 // the splat's support {q(d) <= 2 threshold}. Conservative: the support's
@@ -153,37 +158,20 @@ __device__ __forceinline__ bool blend_one(const Batch& sb, uint32_t j, float pxc
                                           PixelAcc& a, uint32_t* blended) {
   const float4 g = sb.geo[j];
   const float4 c = sb.con[j];
-  float alpha;
-  if (M::kExact) {
-    float dx, dy;
-    boundary_delta<PERIODIC>(pxc, pyc, g.x, g.y, c.x, c.y, c.z, f, &dx, &dy);
-    const float power = ((c.x * (dx * dx) + ((c.y * 2.0f) * dx) * dy) + c.z * (dy * dy)) * -0.5f;
-    if (power > 0.0f || power < -g.w) return false;
-    alpha = rclamp(g.z * M::exp(power), 0.0f, 0.99f);
-    if (alpha < (float)(1.0 / 255.0)) return false;
-  } else {
-    float dx, dy;
-    if (PERIODIC) {
-      const float4 r = sb.raw[j];
-      boundary_delta<true>(pxc, pyc, g.x, g.y, r.x, r.y, r.z, f, &dx, &dy);
-    } else {
-      dx = pxc - g.x;
-      dy = pyc - g.y;
-    }
-    const float p2 = fmaf(c.x * dx, dx, fmaf(c.y * dx, dy, (c.z * dy) * dy));
-    if (!(p2 >= -g.w)) return false;  // below 1/255 (and the NaN-safe reject)
-    alpha = fminf(g.z * ex2_approx(fminf(p2, 0.0f)), 0.99f);
-  }
+  static_assert(M::kExact, "the fast form blends in blend_range_fast");
+  float dx, dy;
+  boundary_delta<PERIODIC>(pxc, pyc, g.x, g.y, c.x, c.y, c.z, f, &dx, &dy);
+  const float power = ((c.x * (dx * dx) + ((c.y * 2.0f) * dx) * dy) + c.z * (dy * dy)) * -0.5f;
+  if (power > 0.0f || power < -g.w) return false;
+  const float alpha = rclamp(g.z * M::exp(power), 0.0f, 0.99f);
+  if (alpha < (float)(1.0 / 255.0)) return false;
   const float4 col = sb.col[j];
   const float contrib = a.t * alpha;
   a.r = a.r + col.x * contrib;
   a.g = a.g + col.y * contrib;
   a.b = a.b + col.z * contrib;
   a.d = a.d + c.w * contrib;
-  if (M::kExact)
-    a.t = a.t * (1.0f - alpha);
-  else
-    a.t = a.t - contrib;
+  a.t = a.t * (1.0f - alpha);
   if (blended) ++*blended;
   return a.t < f.t_threshold;
 }
@@ -216,14 +204,8 @@ __device__ __forceinline__ void blend_range(uint32_t begin, uint32_t source_coun
       const float4 m = __ldg(mean + g);
       const float4 c = __ldg(conic + g);
       const float thr = M::log(m.w * 255.0f);
-      if (M::kExact) {
-        sb.geo[t] = make_float4(m.x, m.y, m.w, thr);
-        sb.con[t] = make_float4(c.x, c.y, c.z, m.z);
-      } else {
-        sb.geo[t] = make_float4(m.x, m.y, m.w, thr * kLog2e);
-        sb.con[t] = make_float4(-0.5f * kLog2e * c.x, -kLog2e * c.y, -0.5f * kLog2e * c.z, m.z);
-        if (PERIODIC) sb.raw[t] = c;
-      }
+      sb.geo[t] = make_float4(m.x, m.y, m.w, thr);
+      sb.con[t] = make_float4(c.x, c.y, c.z, m.z);
       sb.col[t] = __ldg(color + g);
       sb.mask[t] = (uint8_t)patch_mask(m.x, m.y, c.x, c.y, c.z, thr, tile_x0, tile_y0, f.axis);
     }
@@ -241,6 +223,93 @@ __device__ __forceinline__ void blend_range(uint32_t begin, uint32_t source_coun
           if (STATS && done) stop = b + j + 1;
         }
       }
+    }
+  }
+  __syncthreads();  // shared batch buffers are free again
+  if (counting) cnt.checked += stop - s0;
+}
+
+// Fast form of blend_range. The staging thread folds the opacity into the
+// exponent, p' = log2(opacity) - q(d)/2 log2(e), so that
+// alpha = min(opacity e^power, 0.99) = 2^min(p', L) with
+// L = min(log2 opacity, log2 0.99), and the reference's alpha >= 1/255 test is
+// p' >= log2(1/255). Each warp walks a compacted list of the records whose
+// support can reach its patch. Transmittance is tested against the threshold
+// once per 32 listed records: a pixel found done takes no more records (its
+// threshold becomes +inf), so it may blend up to 31 records past the
+// reference's stopping point, whose contributions sum to less than the
+// threshold.
+template <bool PERIODIC, bool STATS>
+__device__ __forceinline__ void blend_range_fast(uint32_t begin, uint32_t source_count, uint32_t raster_count,
+                                                 uint32_t s0, uint32_t s1, bool capped,
+                                                 const uint32_t* __restrict__ ids, const float4* __restrict__ mean,
+                                                 const float4* __restrict__ conic, const float4* __restrict__ color,
+                                                 const RasterFrame& f, float tile_x0, float tile_y0, float pxc,
+                                                 float pyc, bool done, PixelAcc& a, Batch& sb, RasterCounters& cnt) {
+  const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
+  const bool counting = STATS && !done;
+  uint32_t stop = s1;
+  const uint32_t lt = (1u << lane) - 1u;
+  for (uint32_t b = s0; b < s1; b += kBlock) {
+    if (!__syncthreads_or(!done)) break;
+    const uint32_t i = b + t;
+    if (i < s1) {
+      uint32_t src = i;
+      if (capped) src = (uint32_t)floorf((((float)i + 0.5f) * (float)source_count) / (float)raster_count);
+      const uint32_t g = __ldg(ids + begin + src);
+      const float4 m = __ldg(mean + g);
+      const float4 c = __ldg(conic + g);
+      const float log2op = __log2f(m.w);
+      const float thr = (log2op + 7.99435329f) * 0.693147181f;  // ln(opacity * 255)
+      sb.geo[t] = make_float4(m.x, m.y, -0.5f * kLog2e * c.x, -kLog2e * c.y);
+      sb.con[t] = make_float4(-0.5f * kLog2e * c.z, log2op, fminf(log2op, kLog2MaxAlpha), m.z);
+      if (PERIODIC) sb.raw[t] = c;
+      sb.col[t] = __ldg(color + g);
+      sb.mask[t] = (uint8_t)patch_mask(m.x, m.y, c.x, c.y, c.z, thr, tile_x0, tile_y0, f.axis);
+    }
+    __syncthreads();
+    const uint32_t n = min((uint32_t)kBlock, s1 - b);
+    uint32_t listed = 0;
+    for (uint32_t k0 = 0; k0 < n; k0 += 32) {
+      const uint32_t k = k0 + lane;
+      const bool reach = k < n && ((sb.mask[k] >> warp) & 1u);
+      const uint32_t bal = __ballot_sync(0xffffffffu, reach);
+      if (reach) sb.list[warp][listed + __popc(bal & lt)] = (uint8_t)k;
+      listed += __popc(bal);
+    }
+    __syncwarp();
+    for (uint32_t i0 = 0; i0 < listed; i0 += 32) {
+      if (__all_sync(0xffffffffu, done)) break;
+      const float th = done ? __int_as_float(0x7f800000) : kLog2MinAlpha;
+      const uint32_t iend = min(i0 + 32u, listed);
+      for (uint32_t q = i0; q < iend; ++q) {
+        const uint32_t j = sb.list[warp][q];
+        const float4 g = sb.geo[j];
+        const float4 c = sb.con[j];
+        float dx, dy;
+        if (PERIODIC) {
+          const float4 r = sb.raw[j];
+          boundary_delta<true>(pxc, pyc, g.x, g.y, r.x, r.y, r.z, f, &dx, &dy);
+        } else {
+          dx = pxc - g.x;
+          dy = pyc - g.y;
+        }
+        const float p = fmaf(g.z * dx, dx, fmaf(g.w * dx, dy, fmaf(c.x * dy, dy, c.y)));
+        if (!(p >= th)) continue;  // below 1/255, done, or NaN
+        const float alpha = ex2_approx(fminf(p, c.z));
+        const float4 col = sb.col[j];
+        const float contrib = a.t * alpha;
+        a.r = a.r + col.x * contrib;
+        a.g = a.g + col.y * contrib;
+        a.b = a.b + col.z * contrib;
+        a.d = a.d + c.w * contrib;
+        a.t = a.t - contrib;
+        if (STATS) {
+          ++cnt.blended;
+          if (a.t < f.t_threshold && stop == s1) stop = b + j + 1;
+        }
+      }
+      done = done || a.t < f.t_threshold;
     }
   }
   __syncthreads();  // shared batch buffers are free again
@@ -274,7 +343,7 @@ __device__ __forceinline__ float finalize_depth(float wd, float trans, const Pas
 // One block per tile of the batch (in work-list order); the tile's view
 // supplies its viewport and targets.
 template <class M, bool PERIODIC, bool STATS>
-__global__ void __launch_bounds__(kBlock) k_raster(const uint32_t* __restrict__ tile_offsets,
+__global__ void __launch_bounds__(kBlock, 3) k_raster(const uint32_t* __restrict__ tile_offsets,
                                                    const uint32_t* __restrict__ order,
                                                    const uint32_t* __restrict__ ids,
                                                    const float4* __restrict__ mean,
@@ -309,8 +378,12 @@ __global__ void __launch_bounds__(kBlock) k_raster(const uint32_t* __restrict__ 
   PixelAcc a = {0.0f, 0.0f, 0.0f, 1.0f, 0.0f};
   RasterCounters cnt = {0u, 0u};
   if (!chunked) {
-    blend_range<M, PERIODIC, STATS>(begin, source_count, raster_count, 0, raster_count, capped, ids, mean, conic,
-                                    color, f, tile_x0, tile_y0, pxc, pyc, !active, a, sb, cnt);
+    if constexpr (M::kExact)
+      blend_range<M, PERIODIC, STATS>(begin, source_count, raster_count, 0, raster_count, capped, ids, mean, conic,
+                                      color, f, tile_x0, tile_y0, pxc, pyc, !active, a, sb, cnt);
+    else
+      blend_range_fast<PERIODIC, STATS>(begin, source_count, raster_count, 0, raster_count, capped, ids, mean,
+                                        conic, color, f, tile_x0, tile_y0, pxc, pyc, !active, a, sb, cnt);
   } else {
     const uint32_t nchunk = (raster_count + chunk - 1) / chunk;
     bool finished = !active;
@@ -319,8 +392,12 @@ __global__ void __launch_bounds__(kBlock) k_raster(const uint32_t* __restrict__ 
       const uint32_t s0 = ch * chunk;
       const uint32_t s1 = min(s0 + chunk, raster_count);
       PixelAcc p = {0.0f, 0.0f, 0.0f, 1.0f, 0.0f};
-      blend_range<M, PERIODIC, STATS>(begin, source_count, raster_count, s0, s1, capped, ids, mean, conic, color, f,
-                                      tile_x0, tile_y0, pxc, pyc, finished, p, sb, cnt);
+      if constexpr (M::kExact)
+        blend_range<M, PERIODIC, STATS>(begin, source_count, raster_count, s0, s1, capped, ids, mean, conic, color,
+                                        f, tile_x0, tile_y0, pxc, pyc, finished, p, sb, cnt);
+      else
+        blend_range_fast<PERIODIC, STATS>(begin, source_count, raster_count, s0, s1, capped, ids, mean, conic,
+                                          color, f, tile_x0, tile_y0, pxc, pyc, finished, p, sb, cnt);
       if (!finished) {
         a.r = a.r + p.r * a.t;
         a.g = a.g + p.g * a.t;
