@@ -326,6 +326,26 @@ void launch_scan_counts(const uint32_t* ids, const uint32_t* tile_counts, uint32
 // ids are global over the batch (the view's tile_base + local id; the
 // sentinel is the batch's tile total). Also accumulates the tile sort's digit
 // histograms.
+//
+// Warp-cooperative: a warp owns 32 consecutive depth ranks and spreads the
+// union of their bounding-box tiles over its lanes, 32 box tiles per round,
+// so one wide splat no longer idles the other 31 lanes. Each lane finds the
+// rank owning its box tile by a binary search over the warp's inclusive box
+// counts, runs the reference's tile test, and places a hit after the owner's
+// earlier hits (owner's running count + hits of lower lanes with the same
+// owner this round). A splat's records thus fill its reserved range in
+// row-major box order, the order of the per-splat loop; the record set per
+// splat is what the stable tile sort sees, so the sorted result is the same.
+constexpr int kEmitWarps = kBlock / 32;
+
+struct EmitShared {
+  float f[10][kEmitWarps][32];     // cx, cy, conic a, b, c, threshold, rx, ry, view width, height
+  uint32_t u[8][kEmitWarps][32];   // tminx, tminy, box width, tiles_x, tile_base, base, reserved, item
+  uint32_t incl[kEmitWarps][32];   // inclusive box-tile counts
+  uint32_t filled[kEmitWarps][32]; // records placed so far per rank
+  uint32_t hist[4][256];
+};
+
 __global__ void __launch_bounds__(kBlock) k_emit(const uint32_t* __restrict__ ids, const float4* __restrict__ mean,
                                                  const float4* __restrict__ conic,
                                                  const uint32_t* __restrict__ ordered,
@@ -334,14 +354,18 @@ __global__ void __launch_bounds__(kBlock) k_emit(const uint32_t* __restrict__ id
                                                  uint32_t* __restrict__ tile_keys, uint32_t* __restrict__ tile_vals,
                                                  int passes, int digit_bits) {
   if (ctl->state[3] != 0u) return;  // overflow: emission dispatch is zero
-  __shared__ uint32_t s_hist[4][256];
-  const uint32_t tid = threadIdx.x;
-  for (uint32_t i = tid; i < 4 * 256; i += kBlock) (&s_hist[0][0])[i] = 0u;
-  __syncthreads();
+  __shared__ EmitShared sm;
+  const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
   const uint32_t n = ctl->visible_state[0];
+  if (blockIdx.x * kBlock >= n) return;  // whole block past the visible count
+  for (uint32_t i = tid; i < 4 * 256; i += kBlock) (&sm.hist[0][0])[i] = 0u;
   const uint32_t r = blockIdx.x * kBlock + tid;
   const uint32_t mask = (1u << digit_bits) - 1u;
   const uint32_t sentinel = bv.total_tiles;
+  const uint32_t lt = (1u << lane) - 1u;
+
+  // This lane's rank: its box and test inputs, staged for the whole warp.
+  uint32_t nbox = 0, reserved = 0;
   if (r < n) {
     const uint32_t g = ids[r];
     const ViewDesc& v = bv.views[find_view(bv.item_base, bv.nviews, g)];
@@ -351,8 +375,6 @@ __global__ void __launch_bounds__(kBlock) k_emit(const uint32_t* __restrict__ id
     const float rx = (float)(packed % 512u), ry = (float)(packed / 512u);
     const float thr = gsdm::logf_(m.w * 255.0f);
     const int tiles_x = (int)v.tiles_x, tiles_y = (int)v.tiles_y;
-    const uint32_t tile_base = v.tile_base;
-    const float vw = v.vw, vh = v.vh;
     const float mtx = (float)(tiles_x - 1), mty = (float)(tiles_y - 1);
     int tminx = (int)clampf(floorf((m.x - rx) / 16.0f), 0.0f, mtx);
     int tminy = (int)clampf(floorf((m.y - ry) / 16.0f), 0.0f, mty);
@@ -360,32 +382,83 @@ __global__ void __launch_bounds__(kBlock) k_emit(const uint32_t* __restrict__ id
     int tmaxy = (int)clampf(floorf((m.y + ry) / 16.0f), 0.0f, mty);
     if (o.axis == 1u) { tminx = 0; tmaxx = tiles_x - 1; }
     if (o.axis == 2u) { tminy = 0; tmaxy = tiles_y - 1; }
-    const uint32_t reserved = ordered[r];
-    const uint32_t base = offsets[r];
-    uint32_t local = 0;
-    for (int ty = tminy; ty <= tmaxy; ++ty)
-      for (int tx = tminx; tx <= tmaxx; ++tx)
-        if (boundary_tile_hit(m.x, m.y, c.x, c.y, c.z, thr, rx, ry, tx, ty, vw, vh, o.axis)) {
-          if (local < reserved && base + local < capacity) {
-            const uint32_t t = tile_base + (uint32_t)ty * (uint32_t)tiles_x + (uint32_t)tx;
-            tile_keys[base + local] = t;
-            tile_vals[base + local] = g;
-            for (int p = 0; p < passes; ++p) atomicAdd(&s_hist[p][(t >> (p * digit_bits)) & mask], 1u);
-          }
-          ++local;
-        }
-    for (uint32_t pad = local; pad < reserved; ++pad)
+    reserved = ordered[r];
+    const uint32_t bw = (uint32_t)(tmaxx - tminx + 1);
+    // A rank with nothing reserved emits nothing; its box takes no rounds.
+    nbox = reserved ? bw * (uint32_t)(tmaxy - tminy + 1) : 0u;
+    sm.f[0][warp][lane] = m.x; sm.f[1][warp][lane] = m.y;
+    sm.f[2][warp][lane] = c.x; sm.f[3][warp][lane] = c.y; sm.f[4][warp][lane] = c.z;
+    sm.f[5][warp][lane] = thr; sm.f[6][warp][lane] = rx; sm.f[7][warp][lane] = ry;
+    sm.f[8][warp][lane] = v.vw; sm.f[9][warp][lane] = v.vh;
+    sm.u[0][warp][lane] = (uint32_t)tminx; sm.u[1][warp][lane] = (uint32_t)tminy; sm.u[2][warp][lane] = bw;
+    sm.u[3][warp][lane] = (uint32_t)tiles_x; sm.u[4][warp][lane] = v.tile_base;
+    sm.u[5][warp][lane] = offsets[r]; sm.u[6][warp][lane] = reserved; sm.u[7][warp][lane] = g;
+  }
+  uint32_t incl = nbox;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= (uint32_t)d) incl += y;
+  }
+  sm.incl[warp][lane] = incl;
+  sm.filled[warp][lane] = 0u;
+  __syncthreads();  // histogram cleared; warp tables written
+  const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+
+  for (uint32_t j0 = 0; j0 < total; j0 += 32) {
+    const uint32_t j = j0 + lane;
+    const bool valid = j < total;
+    uint32_t owner = 0;
+#pragma unroll
+    for (uint32_t step = 16; step >= 1; step >>= 1)
+      if (sm.incl[warp][owner + step - 1] <= j) owner += step;
+    bool hit = false;
+    uint32_t t = 0;
+    if (valid) {
+      const uint32_t bw = sm.u[2][warp][owner];
+      const uint32_t first = owner ? sm.incl[warp][owner - 1] : 0u;
+      const uint32_t kk = j - first;
+      const uint32_t by = kk / bw, bx = kk - by * bw;
+      const int tx = (int)(sm.u[0][warp][owner] + bx), ty = (int)(sm.u[1][warp][owner] + by);
+      hit = boundary_tile_hit(sm.f[0][warp][owner], sm.f[1][warp][owner], sm.f[2][warp][owner],
+                              sm.f[3][warp][owner], sm.f[4][warp][owner], sm.f[5][warp][owner],
+                              sm.f[6][warp][owner], sm.f[7][warp][owner], tx, ty, sm.f[8][warp][owner],
+                              sm.f[9][warp][owner], o.axis);
+      t = sm.u[4][warp][owner] + (uint32_t)ty * sm.u[3][warp][owner] + (uint32_t)tx;
+    }
+    const uint32_t hits = __ballot_sync(0xffffffffu, hit);
+    const uint32_t same = __match_any_sync(0xffffffffu, valid ? owner : 32u + lane);
+    if (hit) {
+      const uint32_t local = sm.filled[warp][owner] + __popc(hits & same & lt);
+      const uint32_t base = sm.u[5][warp][owner];
+      if (local < sm.u[6][warp][owner] && base + local < capacity) {
+        tile_keys[base + local] = t;
+        tile_vals[base + local] = sm.u[7][warp][owner];
+        for (int p = 0; p < passes; ++p) atomicAdd(&sm.hist[p][(t >> (p * digit_bits)) & mask], 1u);
+      }
+    }
+    __syncwarp();
+    // The highest lane of each owner's group advances the owner's count.
+    if (valid && lane == 31u - (uint32_t)__clz(same)) sm.filled[warp][owner] += __popc(hits & same);
+    __syncwarp();
+  }
+
+  // Sentinel padding for reserved slots without a hit.
+  if (r < n) {
+    const uint32_t base = sm.u[5][warp][lane];
+    const uint32_t g = sm.u[7][warp][lane];
+    for (uint32_t pad = sm.filled[warp][lane]; pad < reserved; ++pad)
       if (base + pad < capacity) {
         tile_keys[base + pad] = sentinel;
         tile_vals[base + pad] = g;
-        for (int p = 0; p < passes; ++p) atomicAdd(&s_hist[p][(sentinel >> (p * digit_bits)) & mask], 1u);
+        for (int p = 0; p < passes; ++p) atomicAdd(&sm.hist[p][(sentinel >> (p * digit_bits)) & mask], 1u);
       }
   }
   __syncthreads();
   const uint32_t radix = 1u << digit_bits;
   for (uint32_t d = tid; d < radix; d += kBlock)
     for (int p = 0; p < passes; ++p)
-      if (s_hist[p][d]) atomicAdd(&ctl->tile_hist[p][d], s_hist[p][d]);
+      if (sm.hist[p][d]) atomicAdd(&ctl->tile_hist[p][d], sm.hist[p][d]);
 }
 
 void launch_emit(const uint32_t* ids, uint32_t n_max, const float4* mean, const float4* conic,
