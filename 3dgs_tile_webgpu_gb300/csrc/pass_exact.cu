@@ -28,8 +28,10 @@ __device__ __forceinline__ void load_sh(const uint32_t* __restrict__ p, uint32_t
       co[4 * i] = w.x; co[4 * i + 1] = w.y; co[4 * i + 2] = w.z; co[4 * i + 3] = w.w;
     }
   } else {
+    // Fully unrolled with constant indices so co[] stays in registers.
     const uint32_t C = (degree + 1) * (degree + 1);
-    for (uint32_t i = 0; i < C; ++i) co[i] = __ldg(p + i);
+#pragma unroll
+    for (uint32_t i = 0; i < 16; ++i) co[i] = i < C ? __ldg(p + i) : 0u;
   }
 }
 
@@ -42,23 +44,81 @@ __device__ __forceinline__ f3 eval_sh_any(uint32_t degree, const uint32_t* co, f
   }
 }
 
-__global__ void __launch_bounds__(kBlock) k_project(BatchView b, PassOptions o, float4* __restrict__ mean_out,
+// Per-warp tables of the projection's cooperative tile count: the splat
+// parameters of the tile test, the box, and the inclusive box-tile counts.
+struct CountShared {
+  float f[8][kBlock / 32][32];     // cx, cy, conic a, b, c, threshold, rx, ry
+  uint32_t u[3][kBlock / 32][32];  // tminx, tminy, box width
+  uint32_t incl[kBlock / 32][32];
+  uint32_t cnt[kBlock / 32][32];
+};
+
+// Counts the tiles of every lane's box that pass the reference's tile test,
+// with the warp's lanes spread over the union of the 32 boxes (32 box tiles
+// per round) instead of each lane walking its own box. Must be called by all
+// 32 lanes; a lane with nbox == 0 contributes nothing. Returns the lane's count.
+__device__ __forceinline__ uint32_t count_tiles_warp(CountShared& sm, uint32_t nbox, float vw, float vh,
+                                                     uint32_t axis) {
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  uint32_t incl = nbox;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= (uint32_t)d) incl += y;
+  }
+  sm.incl[warp][lane] = incl;
+  sm.cnt[warp][lane] = 0u;
+  __syncwarp();
+  const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+  for (uint32_t j0 = 0; j0 < total; j0 += 32) {
+    const uint32_t j = j0 + lane;
+    const bool valid = j < total;
+    uint32_t owner = 0;
+#pragma unroll
+    for (uint32_t step = 16; step >= 1; step >>= 1)
+      if (sm.incl[warp][owner + step - 1] <= j) owner += step;
+    bool hit = false;
+    if (valid) {
+      const uint32_t bw = sm.u[2][warp][owner];
+      const uint32_t k = j - (owner ? sm.incl[warp][owner - 1] : 0u);
+      const uint32_t by = k / bw, bx = k - by * bw;
+      hit = boundary_tile_hit(sm.f[0][warp][owner], sm.f[1][warp][owner], sm.f[2][warp][owner],
+                              sm.f[3][warp][owner], sm.f[4][warp][owner], sm.f[5][warp][owner],
+                              sm.f[6][warp][owner], sm.f[7][warp][owner], (int)(sm.u[0][warp][owner] + bx),
+                              (int)(sm.u[1][warp][owner] + by), vw, vh, axis);
+    }
+    const uint32_t hits = __ballot_sync(0xffffffffu, hit);
+    const uint32_t same = __match_any_sync(0xffffffffu, valid ? owner : 32u + lane);
+    if (valid && lane == 31u - (uint32_t)__clz(same)) sm.cnt[warp][owner] += __popc(hits & same);
+  }
+  __syncwarp();
+  return sm.cnt[warp][lane];
+}
+
+__global__ void __launch_bounds__(kBlock, 4) k_project(BatchView b, PassOptions o, float4* __restrict__ mean_out,
                                                     float4* __restrict__ conic_out, float4* __restrict__ color_out,
                                                     uint32_t* __restrict__ count_out, uint32_t* __restrict__ key_out) {
   __shared__ float s_snorm[256];
   __shared__ uint32_t s_view;
+  __shared__ CountShared s_count;
   s_snorm[threadIdx.x] = snorm8_value(threadIdx.x);
   if (threadIdx.x == 0) s_view = find_view(b.block_base, b.nviews, blockIdx.x);
   __syncthreads();
   const ViewDesc& v = b.views[s_view];
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   const uint32_t gid = (blockIdx.x - v.block_base) * kBlock + threadIdx.x;  // ordinal within the view
   const uint32_t item = v.item_base + gid;
+  const float vw = v.vw, vh = v.vh;
   float4 mo4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-  uint32_t cnt = 0, key = kInvisibleKey;
+  uint32_t cnt = 0, key = kInvisibleKey, nbox = 0, slot = 0;
+  Projected pr = {};
+  float op = 0.0f, rx = 0.0f, ry = 0.0f;
+  f3 vdir = {0.0f, 0.0f, 0.0f};
+  // Decode, project and cull; a splat that survives gets its tile box.
   do {
     if (gid >= v.active) break;  // padding up to the view's next block boundary
     const uint32_t C = v.C;
-    const uint32_t slot = __ldg(v.sh + (size_t)v.count * C + gid);
+    slot = __ldg(v.sh + (size_t)v.count * C + gid);
     if (slot >= v.count) break;  // out-of-range tail entries never draw
     const float4 mo = __ldg(v.means + slot);
     if (mo.w < 0.0f) break;  // empty slot (ProjectionStage.ts:408-410)
@@ -75,7 +135,7 @@ __global__ void __launch_bounds__(kBlock) k_project(BatchView b, PassOptions o, 
     // viewDirection = normalize(positionLocal - cameraLocal) (:469)
     const float ddx = mo.x - camx, ddy = mo.y - camy, ddz = mo.z - camz;
     const float dlen = sqrtf((ddx * ddx + ddy * ddy) + ddz * ddz);
-    const f3 vdir = {ddx / dlen, ddy / dlen, ddz / dlen};
+    vdir = {ddx / dlen, ddy / dlen, ddz / dlen};
     // view = modelView * (p, 1) (:479-482)
     const float vx = ((mv[0] * mo.x + mv[4] * mo.y) + mv[8] * mo.z) + mv[12] * 1.0f;
     const float vy = ((mv[1] * mo.x + mv[5] * mo.y) + mv[9] * mo.z) + mv[13] * 1.0f;
@@ -89,16 +149,16 @@ __global__ void __launch_bounds__(kBlock) k_project(BatchView b, PassOptions o, 
     float P[16];
 #pragma unroll
     for (int i = 0; i < 16; ++i) P[i] = v.P[i];
-    const float vw = v.vw, vh = v.vh;
-    const Projected pr = project({vx, vy, vz}, cv, P, vw, vh, v.vnear, v.vfar, o.filter);
+    pr = project({vx, vy, vz}, cv, P, vw, vh, v.vnear, v.vfar, o.filter);
     if (!pr.ok) break;
-    float op = clampf(so.w, 0.0f, 1.0f);
+    op = clampf(so.w, 0.0f, 1.0f);
     if (o.antialias == 0u) op = op * sqrtf(clampf(pr.orig_det / pr.det, 0.0f, 1.0f));
     if (op < (float)(1.0 / 255.0) || op != op) break;
     const float thr = gsdm::logf_(op * 255.0f);
     const float ex = sqrtf((thr * 2.0f) * clampf(pr.cov_x, 1e-12f, 1e4f));
     const float ey = sqrtf((thr * 2.0f) * clampf(pr.cov_z, 1e-12f, 1e4f));
-    const float rx = ceilf(ex), ry = ceilf(ey);
+    rx = ceilf(ex);
+    ry = ceilf(ey);
     if (rx <= 0.0f || ry <= 0.0f) break;
     const float bminx = pr.cx - rx, bminy = pr.cy - ry, bmaxx = pr.cx + rx, bmaxy = pr.cy + ry;
     if ((o.axis != 1u && (bmaxx < 0.0f || bminx >= vw)) || (o.axis != 2u && (bmaxy < 0.0f || bminy >= vh)))
@@ -117,14 +177,20 @@ __global__ void __launch_bounds__(kBlock) k_project(BatchView b, PassOptions o, 
     int tmaxy = (int)clampf(floorf(bmaxy / 16.0f), 0.0f, mty);
     if (o.axis == 1u) { tminx = 0; tmaxx = tiles_x - 1; }
     if (o.axis == 2u) { tminy = 0; tmaxy = tiles_y - 1; }
-    for (int ty = tminy; ty <= tmaxy; ++ty)
-      for (int tx = tminx; tx <= tmaxx; ++tx)
-        if (boundary_tile_hit(pr.cx, pr.cy, pr.conic_x, pr.conic_y, pr.conic_z, thr, rx, ry, tx, ty, vw, vh,
-                              o.axis))
-          ++cnt;
-    if (cnt == 0) break;
+    const uint32_t bw = (uint32_t)(tmaxx - tminx + 1);
+    nbox = bw * (uint32_t)(tmaxy - tminy + 1);
+    s_count.f[0][warp][lane] = pr.cx; s_count.f[1][warp][lane] = pr.cy;
+    s_count.f[2][warp][lane] = pr.conic_x; s_count.f[3][warp][lane] = pr.conic_y;
+    s_count.f[4][warp][lane] = pr.conic_z; s_count.f[5][warp][lane] = thr;
+    s_count.f[6][warp][lane] = rx; s_count.f[7][warp][lane] = ry;
+    s_count.u[0][warp][lane] = (uint32_t)tminx; s_count.u[1][warp][lane] = (uint32_t)tminy;
+    s_count.u[2][warp][lane] = bw;
+  } while (false);
+  // Tiles passing the tile test (projectionHelpers.ts:223-236), counted by the whole warp.
+  cnt = count_tiles_warp(s_count, nbox, vw, vh, o.axis);
+  if (cnt > 0) {
     uint32_t co[16];
-    load_sh(v.sh + (size_t)slot * C, v.degree, co);
+    load_sh(v.sh + (size_t)slot * v.C, v.degree, co);
     const f3 col = eval_sh_any(v.degree, co, vdir, s_snorm);
     mo4 = make_float4(pr.cx, pr.cy, pr.depth, op);
     conic_out[item] = make_float4(pr.conic_x, pr.conic_y, pr.conic_z, rx + ry * 512.0f);
@@ -135,7 +201,7 @@ __global__ void __launch_bounds__(kBlock) k_project(BatchView b, PassOptions o, 
       float t = clampf((pr.depth - v.vnear) / (v.vfar - v.vnear), 0.0f, 1.0f);
       key = (uint32_t)gsdm::round_even_small(t * 65535.0f);  // visibility.ts:140-144
     }
-  } while (false);
+  }
   mean_out[item] = mo4;
   count_out[item] = cnt;
   key_out[item] = key;
