@@ -206,7 +206,7 @@ __device__ __forceinline__ void store_pixel(const ViewDesc& v, const PassOptions
 }
 
 template <bool PERIODIC, bool STATS>
-__global__ void __launch_bounds__(kHalfThreads, 6) k_raster_h2(const uint32_t* __restrict__ tile_offsets,
+__global__ void __launch_bounds__(kHalfThreads, 7) k_raster_h2(const uint32_t* __restrict__ tile_offsets,
                                                            const uint32_t* __restrict__ order,
                                                            const uint32_t* __restrict__ ids,
                                                            const float4* __restrict__ mean,
