@@ -240,8 +240,13 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* s
 }
 
 // Launch wrappers implemented in the .cu files.
+// Packed raster record of a visible splat, read by the fast raster forms with
+// one 32-byte gather (two float4, 32-byte aligned):
+//   [0] cx, cy, -a/2 log2 e, -b log2 e
+//   [1] -c/2 log2 e, log2 opacity, half2(r, g) bits, half2(b, min(log2 opacity, log2 0.99)) bits
+// where (a, b, c) is the conic. Written by the projection when `rec` is not null.
 void launch_project(const BatchView& b, const PassOptions& o, float4* mean, float4* conic, float4* color,
-                    uint32_t* counts, uint32_t* keys, int max_degree, cudaStream_t st);
+                    uint32_t* counts, uint32_t* keys, float4* rec, cudaStream_t st);
 void launch_epoch_begin(uint32_t* epoch_base, cudaStream_t st);
 void launch_compact(const uint32_t* keys, uint32_t n, uint32_t* vis_off, uint32_t* keys_out, uint32_t* vals_out,
                     Control* ctl, unsigned long long* status, Epoch epoch, int depth_passes, cudaStream_t st);
@@ -268,8 +273,8 @@ void launch_tile_order(const uint32_t* tile_offsets, uint32_t ntile, Control* ct
                        cudaStream_t st);
 // Rasterizer over every tile of the batch (precision: 0 fp32, 1 exact, 2 half2).
 void launch_raster(int precision, const uint32_t* tile_offsets, const uint32_t* order, const uint32_t* sorted_ids,
-                   const float4* mean, const float4* conic, const float4* color, const BatchView& b,
-                   const PassOptions& o, Control* ctl, bool stats, cudaStream_t st);
+                   const float4* mean, const float4* conic, const float4* color, const float4* rec,
+                   const BatchView& b, const PassOptions& o, Control* ctl, bool stats, cudaStream_t st);
 void launch_raster_exact(const uint32_t* tile_offsets, const uint32_t* order, const uint32_t* sorted_ids,
                          const float4* mean, const float4* conic, const float4* color, const BatchView& b,
                          const PassOptions& o, Control* ctl, bool stats, cudaStream_t st);

@@ -97,7 +97,8 @@ __device__ __forceinline__ uint32_t count_tiles_warp(CountShared& sm, uint32_t n
 
 __global__ void __launch_bounds__(kBlock, 4) k_project(BatchView b, PassOptions o, float4* __restrict__ mean_out,
                                                     float4* __restrict__ conic_out, float4* __restrict__ color_out,
-                                                    uint32_t* __restrict__ count_out, uint32_t* __restrict__ key_out) {
+                                                    uint32_t* __restrict__ count_out, uint32_t* __restrict__ key_out,
+                                                    float4* __restrict__ rec_out) {
   __shared__ float s_snorm[256];
   __shared__ uint32_t s_view;
   __shared__ CountShared s_count;
@@ -195,6 +196,16 @@ __global__ void __launch_bounds__(kBlock, 4) k_project(BatchView b, PassOptions 
     mo4 = make_float4(pr.cx, pr.cy, pr.depth, op);
     conic_out[item] = make_float4(pr.conic_x, pr.conic_y, pr.conic_z, rx + ry * 512.0f);
     color_out[item] = make_float4(col.x, col.y, col.z, __uint_as_float(slot ^ kActiveTag));
+    if (rec_out) {
+      // Packed raster record of the fast forms (layout in pass_common.cuh).
+      const float log2op = __log2f(op);
+      const __half2 rg = __floats2half2_rn(col.x, col.y);
+      const __half2 bl = __floats2half2_rn(col.z, fminf(log2op, kLog2MaxAlpha));
+      rec_out[2 * (size_t)item] = make_float4(pr.cx, pr.cy, -0.5f * kLog2e * pr.conic_x, -kLog2e * pr.conic_y);
+      rec_out[2 * (size_t)item + 1] =
+          make_float4(-0.5f * kLog2e * pr.conic_z, log2op, __uint_as_float(*reinterpret_cast<const uint32_t*>(&rg)),
+                      __uint_as_float(*reinterpret_cast<const uint32_t*>(&bl)));
+    }
     if (o.depth_mode == 0u) {
       key = __float_as_uint(pr.depth);  // visibility.ts:139
     } else {
@@ -208,10 +219,9 @@ __global__ void __launch_bounds__(kBlock, 4) k_project(BatchView b, PassOptions 
 }
 
 void launch_project(const BatchView& b, const PassOptions& o, float4* mean, float4* conic, float4* color,
-                    uint32_t* counts, uint32_t* keys, int max_degree, cudaStream_t st) {
-  (void)max_degree;
+                    uint32_t* counts, uint32_t* keys, float4* rec, cudaStream_t st) {
   if (b.total_blocks == 0) return;
-  k_project<<<b.total_blocks, kBlock, 0, st>>>(b, o, mean, conic, color, counts, keys);
+  k_project<<<b.total_blocks, kBlock, 0, st>>>(b, o, mean, conic, color, counts, keys, rec);
 }
 
 // ---------------------------------------------------------------------------
@@ -562,7 +572,7 @@ void launch_tile_ranges(const uint32_t* keys, Control* ctl, uint32_t ntile, uint
 void launch_raster_exact(const uint32_t* tile_offsets, const uint32_t* order, const uint32_t* ids,
                          const float4* mean, const float4* conic, const float4* color, const BatchView& b,
                          const PassOptions& o, Control* ctl, bool stats, cudaStream_t st) {
-  launch_raster_policy<ExactMath>(tile_offsets, order, ids, mean, conic, color, b, o, ctl, stats, st);
+  launch_raster_policy<ExactMath>(tile_offsets, order, ids, mean, conic, color, nullptr, b, o, ctl, stats, st);
 }
 
 }  // namespace gs

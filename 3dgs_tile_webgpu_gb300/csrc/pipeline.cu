@@ -39,6 +39,7 @@ struct gs3d_pipeline {
   // Per-slot workspaces (sized by data.count).
   uint32_t slot_cap = 0;
   float4* mean = nullptr;
+  float4* rec = nullptr;  // packed raster records, two float4 per slot
   float4* conic = nullptr;
   float4* color = nullptr;
   uint32_t* counts = nullptr;
@@ -198,6 +199,7 @@ gs3d_status ensure_slots(gs3d_pipeline* p, uint32_t count) {
   const uint32_t cap = std::max(count, p->slot_cap * 2u);
   cudaError_t e = cudaSuccess;
   if ((e = dalloc(p->mean, cap)) || (e = dalloc(p->conic, cap)) || (e = dalloc(p->color, cap)) ||
+      (e = dalloc(p->rec, 2 * (size_t)cap)) ||
       (e = dalloc(p->counts, cap)) || (e = dalloc(p->keys, cap)) || (e = dalloc(p->vis_off, cap)) ||
       (e = dalloc(p->dk[0], cap)) || (e = dalloc(p->dk[1], cap)) || (e = dalloc(p->dv[0], cap)) ||
       (e = dalloc(p->dv[1], cap)) || (e = dalloc(p->ordered, cap)) || (e = dalloc(p->ioff, cap))) {
@@ -305,7 +307,7 @@ void release_all(gs3d_pipeline* p) {
     dfree(p->stage_dev[i]);
     if (p->stage_pinned[i]) cudaFreeHost(p->stage_pinned[i]);
   }
-  dfree(p->mean); dfree(p->conic); dfree(p->color); dfree(p->counts); dfree(p->keys); dfree(p->vis_off);
+  dfree(p->mean); dfree(p->rec); dfree(p->conic); dfree(p->color); dfree(p->counts); dfree(p->keys); dfree(p->vis_off);
   dfree(p->dk[0]); dfree(p->dk[1]); dfree(p->dv[0]); dfree(p->dv[1]); dfree(p->ordered); dfree(p->ioff);
   dfree(p->tk[0]); dfree(p->tk[1]); dfree(p->tv[0]); dfree(p->tv[1]);
   dfree(p->tile_offsets); dfree(p->tile_order); dfree(p->ctl); dfree(p->epoch_dev); dfree(p->output_state); dfree(p->status);
@@ -611,7 +613,8 @@ void record_batch(gs3d_pipeline* p, const Plan& pl, unsigned char* dev, cudaStre
 
   // K1: projection.
   mark(p, GS3D_STAGE_PROJECT, st);
-  launch_project(bv, o, p->mean, p->conic, p->color, p->counts, p->keys, 3, st);
+  const bool exact = p->desc.raster_precision == GS3D_RASTER_EXACT;
+  launch_project(bv, o, p->mean, p->conic, p->color, p->counts, p->keys, exact ? nullptr : p->rec, st);
   launches += pl.blocks ? 1 : 0;
   // Visibility compaction.
   mark(p, GS3D_STAGE_COMPACT, st);
@@ -663,7 +666,7 @@ void record_batch(gs3d_pipeline* p, const Plan& pl, unsigned char* dev, cudaStre
   // Raster.
   mark(p, GS3D_STAGE_RASTER, st);
   launch_raster((int)p->desc.raster_precision, p->tile_offsets, p->tile_order, p->tv[tcur], p->mean, p->conic,
-                p->color, bv, o, ctl, p->desc.raster_stats != 0, st);
+                p->color, p->rec, bv, o, ctl, p->desc.raster_stats != 0, st);
   ++launches;
   mark(p, GS3D_STAGE_COUNT, st);
   if (p->profiling) ++p->profiled;

@@ -58,17 +58,17 @@ void launch_tile_order(const uint32_t* tile_offsets, uint32_t ntile, Control* ct
 }
 
 void launch_raster(int precision, const uint32_t* tile_offsets, const uint32_t* order, const uint32_t* ids,
-                   const float4* mean, const float4* conic, const float4* color, const BatchView& b,
-                   const PassOptions& o, Control* ctl, bool stats, cudaStream_t st) {
+                   const float4* mean, const float4* conic, const float4* color, const float4* rec,
+                   const BatchView& b, const PassOptions& o, Control* ctl, bool stats, cudaStream_t st) {
   if (precision == 1) {
     launch_raster_exact(tile_offsets, order, ids, mean, conic, color, b, o, ctl, stats, st);
     return;
   }
   if (precision == 2) {
-    launch_raster_half2(tile_offsets, order, ids, mean, conic, color, b, o, ctl, stats, st);
+    launch_raster_half2(tile_offsets, order, ids, mean, color, rec, b, o, ctl, stats, st);
     return;
   }
-  launch_raster_policy<FastMath>(tile_offsets, order, ids, mean, conic, color, b, o, ctl, stats, st);
+  launch_raster_policy<FastMath>(tile_offsets, order, ids, mean, conic, color, rec, b, o, ctl, stats, st);
 }
 
 }  // namespace gs

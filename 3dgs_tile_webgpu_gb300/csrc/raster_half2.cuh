@@ -84,7 +84,7 @@ template <bool PERIODIC, bool STATS>
 __device__ __forceinline__ void blend_range_h2(uint32_t begin, uint32_t source_count, uint32_t raster_count,
                                                uint32_t s0, uint32_t s1, bool capped,
                                                const uint32_t* __restrict__ ids, const float4* __restrict__ mean,
-                                               const float4* __restrict__ conic, const float4* __restrict__ color,
+                                               const float4* __restrict__ rec, bool need_depth,
                                                const RasterFrame& f, float tile_x0, float tile_y0, float pxc,
                                                float pyc0, bool done0, bool done1, PixelAcc& a0, PixelAcc& a1,
                                                HalfBatch& sb, RasterCounters& c0n, RasterCounters& c1n) {
@@ -103,17 +103,20 @@ __device__ __forceinline__ void blend_range_h2(uint32_t begin, uint32_t source_c
         uint32_t src = i;
         if (capped) src = (uint32_t)floorf((((float)i + 0.5f) * (float)source_count) / (float)raster_count);
         const uint32_t g = __ldg(ids + begin + src);
-        const float4 m = __ldg(mean + g);
-        const float4 c = __ldg(conic + g);
-        const float log2op = __log2f(m.w);
-        const float thr = (log2op + 7.99435329f) * 0.693147181f;  // ln(opacity * 255)
-        const __half2 lim = __float2half2_rn(fminf(log2op, kLog2MaxAlpha));
-        sb.geo[slot] = make_float4(m.x, m.y, -0.5f * kLog2e * c.x, -kLog2e * c.y);
-        sb.con[slot] = make_float4(-0.5f * kLog2e * c.z, log2op, __uint_as_float(*reinterpret_cast<const uint32_t*>(&lim)),
-                                   m.z);
+        const float4 r0 = __ldg(rec + 2 * (size_t)g);  // one 32-byte record
+        const float4 r1 = __ldg(rec + 2 * (size_t)g + 1);
+        const float depth = need_depth ? __ldg(&mean[g].z) : 0.0f;
+        const float4 c = raw_conic(r0, r1);
+        const float thr = (r1.y + 7.99435329f) * 0.693147181f;  // ln(opacity * 255)
+        const uint32_t rg_bits = __float_as_uint(r1.z), bl_bits = __float_as_uint(r1.w);
+        const float2 rg = __half22float2(*reinterpret_cast<const __half2*>(&rg_bits));
+        const __half2 bl = *reinterpret_cast<const __half2*>(&bl_bits);
+        const __half2 lim = __half2half2(__high2half(bl));
+        sb.geo[slot] = r0;
+        sb.con[slot] = make_float4(r1.x, r1.y, __uint_as_float(*reinterpret_cast<const uint32_t*>(&lim)), depth);
         if (PERIODIC) sb.raw[slot] = c;
-        sb.col[slot] = __ldg(color + g);
-        sb.mask[slot] = (uint8_t)patch_mask8(m.x, m.y, c.x, c.y, c.z, thr, tile_x0, tile_y0, f.axis);
+        sb.col[slot] = make_float4(rg.x, rg.y, __low2float(bl), 0.0f);
+        sb.mask[slot] = (uint8_t)patch_mask8(r0.x, r0.y, c.x, c.y, c.z, thr, tile_x0, tile_y0, f.axis);
       }
     }
     __syncthreads();
@@ -210,8 +213,7 @@ __global__ void __launch_bounds__(kHalfThreads, 7) k_raster_h2(const uint32_t* _
                                                            const uint32_t* __restrict__ order,
                                                            const uint32_t* __restrict__ ids,
                                                            const float4* __restrict__ mean,
-                                                           const float4* __restrict__ conic,
-                                                           const float4* __restrict__ color, BatchView bv,
+                                                           const float4* __restrict__ rec, BatchView bv,
                                                            PassOptions o, Control* __restrict__ ctl) {
   if (ctl->state[3] != 0u) return;  // overflow: nothing is published
   __shared__ HalfBatch sb;
@@ -242,8 +244,9 @@ __global__ void __launch_bounds__(kHalfThreads, 7) k_raster_h2(const uint32_t* _
   PixelAcc a0 = {0.0f, 0.0f, 0.0f, 1.0f, 0.0f}, a1 = a0;
   RasterCounters n0 = {0u, 0u}, n1 = {0u, 0u};
   if (!chunked) {
-    blend_range_h2<PERIODIC, STATS>(begin, source_count, raster_count, 0, raster_count, capped, ids, mean, conic,
-                                    color, f, tile_x0, tile_y0, pxc, pyc0, !active0, !active1, a0, a1, sb, n0, n1);
+    blend_range_h2<PERIODIC, STATS>(begin, source_count, raster_count, 0, raster_count, capped, ids, mean, rec,
+                                    v.depth != nullptr, f, tile_x0, tile_y0, pxc, pyc0, !active0, !active1, a0, a1,
+                                    sb, n0, n1);
   } else {
     const uint32_t nchunk = (raster_count + chunk - 1) / chunk;
     bool fin0 = !active0, fin1 = !active1;
@@ -251,8 +254,9 @@ __global__ void __launch_bounds__(kHalfThreads, 7) k_raster_h2(const uint32_t* _
       if (!__syncthreads_or(!(fin0 && fin1))) break;
       const uint32_t s0 = ch * chunk, s1 = min(s0 + chunk, raster_count);
       PixelAcc p0 = {0.0f, 0.0f, 0.0f, 1.0f, 0.0f}, p1 = p0;
-      blend_range_h2<PERIODIC, STATS>(begin, source_count, raster_count, s0, s1, capped, ids, mean, conic, color,
-                                      f, tile_x0, tile_y0, pxc, pyc0, fin0, fin1, p0, p1, sb, n0, n1);
+      blend_range_h2<PERIODIC, STATS>(begin, source_count, raster_count, s0, s1, capped, ids, mean, rec,
+                                      v.depth != nullptr, f, tile_x0, tile_y0, pxc, pyc0, fin0, fin1, p0, p1, sb, n0,
+                                      n1);
       if (!fin0) {
         a0.r = a0.r + p0.r * a0.t; a0.g = a0.g + p0.g * a0.t; a0.b = a0.b + p0.b * a0.t;
         a0.d = a0.d + p0.d * a0.t; a0.t = a0.t * p0.t;
@@ -287,12 +291,12 @@ __global__ void __launch_bounds__(kHalfThreads, 7) k_raster_h2(const uint32_t* _
 }
 
 inline void launch_raster_half2(const uint32_t* tile_offsets, const uint32_t* order, const uint32_t* ids,
-                                const float4* mean, const float4* conic, const float4* color, const BatchView& b,
+                                const float4* mean, const float4* color, const float4* rec, const BatchView& b,
                                 const PassOptions& o, Control* ctl, bool stats, cudaStream_t st) {
+  (void)color;  // colours come from the packed records
   if (b.total_tiles == 0) return;
-#define GS_RASTER_H2(P, S)                                                                                     \
-  k_raster_h2<P, S><<<b.total_tiles, kHalfThreads, 0, st>>>(tile_offsets, order, ids, mean, conic, color, b, o, \
-                                                            ctl)
+#define GS_RASTER_H2(P, S) \
+  k_raster_h2<P, S><<<b.total_tiles, kHalfThreads, 0, st>>>(tile_offsets, order, ids, mean, rec, b, o, ctl)
   if (o.axis != 0u) {
     if (stats) GS_RASTER_H2(true, true); else GS_RASTER_H2(true, false);
   } else {

@@ -229,6 +229,13 @@ __device__ __forceinline__ void blend_range(uint32_t begin, uint32_t source_coun
   if (counting) cnt.checked += stop - s0;
 }
 
+// The conic (a, b, c) back from a packed raster record's scaled terms.
+__device__ __forceinline__ float4 raw_conic(const float4& r0, const float4& r1) {
+  constexpr float kNeg2Ln2 = -1.38629436f;  // 1 / (-1/2 log2 e)
+  constexpr float kNegLn2 = -0.693147181f;  // 1 / (-log2 e)
+  return make_float4(r0.z * kNeg2Ln2, r0.w * kNegLn2, r1.x * kNeg2Ln2, 0.0f);
+}
+
 // Fast form of blend_range. The staging thread folds the opacity into the
 // exponent, p' = log2(opacity) - q(d)/2 log2(e), so that
 // alpha = min(opacity e^power, 0.99) = 2^min(p', L) with
@@ -243,9 +250,10 @@ template <bool PERIODIC, bool STATS>
 __device__ __forceinline__ void blend_range_fast(uint32_t begin, uint32_t source_count, uint32_t raster_count,
                                                  uint32_t s0, uint32_t s1, bool capped,
                                                  const uint32_t* __restrict__ ids, const float4* __restrict__ mean,
-                                                 const float4* __restrict__ conic, const float4* __restrict__ color,
-                                                 const RasterFrame& f, float tile_x0, float tile_y0, float pxc,
-                                                 float pyc, bool done, PixelAcc& a, Batch& sb, RasterCounters& cnt) {
+                                                 const float4* __restrict__ color, const float4* __restrict__ rec,
+                                                 bool need_depth, const RasterFrame& f, float tile_x0, float tile_y0,
+                                                 float pxc, float pyc, bool done, PixelAcc& a, Batch& sb,
+                                                 RasterCounters& cnt) {
   const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
   const bool counting = STATS && !done;
   uint32_t stop = s1;
@@ -257,15 +265,16 @@ __device__ __forceinline__ void blend_range_fast(uint32_t begin, uint32_t source
       uint32_t src = i;
       if (capped) src = (uint32_t)floorf((((float)i + 0.5f) * (float)source_count) / (float)raster_count);
       const uint32_t g = __ldg(ids + begin + src);
-      const float4 m = __ldg(mean + g);
-      const float4 c = __ldg(conic + g);
-      const float log2op = __log2f(m.w);
-      const float thr = (log2op + 7.99435329f) * 0.693147181f;  // ln(opacity * 255)
-      sb.geo[t] = make_float4(m.x, m.y, -0.5f * kLog2e * c.x, -kLog2e * c.y);
-      sb.con[t] = make_float4(-0.5f * kLog2e * c.z, log2op, fminf(log2op, kLog2MaxAlpha), m.z);
+      const float4 r0 = __ldg(rec + 2 * (size_t)g);  // one 32-byte record
+      const float4 r1 = __ldg(rec + 2 * (size_t)g + 1);
+      const float depth = need_depth ? __ldg(&mean[g].z) : 0.0f;
+      const float4 c = raw_conic(r0, r1);
+      const float thr = (r1.y + 7.99435329f) * 0.693147181f;  // ln(opacity * 255)
+      sb.geo[t] = r0;
+      sb.con[t] = make_float4(r1.x, r1.y, fminf(r1.y, kLog2MaxAlpha), depth);
       if (PERIODIC) sb.raw[t] = c;
       sb.col[t] = __ldg(color + g);
-      sb.mask[t] = (uint8_t)patch_mask(m.x, m.y, c.x, c.y, c.z, thr, tile_x0, tile_y0, f.axis);
+      sb.mask[t] = (uint8_t)patch_mask(r0.x, r0.y, c.x, c.y, c.z, thr, tile_x0, tile_y0, f.axis);
     }
     __syncthreads();
     const uint32_t n = min((uint32_t)kBlock, s1 - b);
@@ -348,7 +357,8 @@ __global__ void __launch_bounds__(kBlock, 3) k_raster(const uint32_t* __restrict
                                                    const uint32_t* __restrict__ ids,
                                                    const float4* __restrict__ mean,
                                                    const float4* __restrict__ conic,
-                                                   const float4* __restrict__ color, BatchView bv, PassOptions o,
+                                                   const float4* __restrict__ color,
+                                                   const float4* __restrict__ rec, BatchView bv, PassOptions o,
                                                    Control* __restrict__ ctl) {
   // Overflow: the reference zeroes the raster dispatch, so nothing is written.
   if (ctl->state[3] != 0u) return;
@@ -383,7 +393,8 @@ __global__ void __launch_bounds__(kBlock, 3) k_raster(const uint32_t* __restrict
                                       color, f, tile_x0, tile_y0, pxc, pyc, !active, a, sb, cnt);
     else
       blend_range_fast<PERIODIC, STATS>(begin, source_count, raster_count, 0, raster_count, capped, ids, mean,
-                                        conic, color, f, tile_x0, tile_y0, pxc, pyc, !active, a, sb, cnt);
+                                        color, rec, v.depth != nullptr, f, tile_x0, tile_y0, pxc, pyc, !active, a,
+                                        sb, cnt);
   } else {
     const uint32_t nchunk = (raster_count + chunk - 1) / chunk;
     bool finished = !active;
@@ -396,8 +407,8 @@ __global__ void __launch_bounds__(kBlock, 3) k_raster(const uint32_t* __restrict
         blend_range<M, PERIODIC, STATS>(begin, source_count, raster_count, s0, s1, capped, ids, mean, conic, color,
                                         f, tile_x0, tile_y0, pxc, pyc, finished, p, sb, cnt);
       else
-        blend_range_fast<PERIODIC, STATS>(begin, source_count, raster_count, s0, s1, capped, ids, mean, conic,
-                                          color, f, tile_x0, tile_y0, pxc, pyc, finished, p, sb, cnt);
+        blend_range_fast<PERIODIC, STATS>(begin, source_count, raster_count, s0, s1, capped, ids, mean, color, rec,
+                                          v.depth != nullptr, f, tile_x0, tile_y0, pxc, pyc, finished, p, sb, cnt);
       if (!finished) {
         a.r = a.r + p.r * a.t;
         a.g = a.g + p.g * a.t;
@@ -443,12 +454,13 @@ __global__ void __launch_bounds__(kBlock, 3) k_raster(const uint32_t* __restrict
 
 template <class M>
 void launch_raster_policy(const uint32_t* tile_offsets, const uint32_t* order, const uint32_t* ids,
-                          const float4* mean, const float4* conic, const float4* color, const BatchView& b,
-                          const PassOptions& o, Control* ctl, bool stats, cudaStream_t st) {
+                          const float4* mean, const float4* conic, const float4* color, const float4* rec,
+                          const BatchView& b, const PassOptions& o, Control* ctl, bool stats, cudaStream_t st) {
   if (b.total_tiles == 0) return;
   const bool periodic = o.axis != 0u;
-#define GS_RASTER(P, S) \
-  k_raster<M, P, S><<<b.total_tiles, kBlock, 0, st>>>(tile_offsets, order, ids, mean, conic, color, b, o, ctl)
+#define GS_RASTER(P, S)                                                                                       \
+  k_raster<M, P, S><<<b.total_tiles, kBlock, 0, st>>>(tile_offsets, order, ids, mean, conic, color, rec, b, o, \
+                                                      ctl)
   if (periodic) {
     if (stats) GS_RASTER(true, true); else GS_RASTER(true, false);
   } else {

@@ -26,10 +26,10 @@ from dataclasses import dataclass, field
 
 from . import TiledGaussianPipeline, make_camera
 
-# Workspace bytes per padded ordinal (projected mean/conic/colour 48, counts,
-# keys, offsets 20, depth records x2 16) and per intersection record (tile ids
-# and ordinals, ping-pong: 16).
-BYTES_PER_ITEM = 84
+# Workspace bytes per padded ordinal (projected mean/conic/colour 48, packed
+# raster record 32, counts, keys, offsets 20, depth records x2 16) and per
+# intersection record (tile ids and ordinals, ping-pong: 16).
+BYTES_PER_ITEM = 116
 BYTES_PER_RECORD = 16
 
 

@@ -44,6 +44,8 @@ def parse():
     ap.add_argument("--plain-precision", default="fp32", choices=["fp32", "exact"])
     ap.add_argument("--latency-frames", type=int, default=240)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--forms", default="all", choices=["all", "batched"],
+                    help="'batched' skips the timed plain (one view per launch) form")
     ap.add_argument("--serve", action="store_true", help="serving-loop measurement (configuration 4)")
     ap.add_argument("--serve-rates", default="200,500,1000,2000")
     ap.add_argument("--serve-requests", type=int, default=300)
@@ -58,6 +60,25 @@ def peaks():
         return float(p["hbm_gbs"]), "measured"
     except Exception:
         return 6800.0, "fallback"
+
+
+TRAFFIC_FILE = os.path.join(ROOT, "profiles", "dram_traffic_config2_3M_1080p.md")
+
+
+def measured_traffic(stage: str, args) -> int | None:
+    """DRAM bytes (read + write) of one launch of `stage`'s kernel, from the
+    committed ncu summary, when that capture was taken on this workload."""
+    try:
+        with open(TRAFFIC_FILE) as f:
+            for line in f:
+                parts = line.split()
+                if len(parts) == 8 and parts[0] == "traffic" and parts[1] == stage:
+                    cfg = (int(parts[2]), int(parts[3]), int(parts[4]), int(parts[5]), parts[6])
+                    if cfg == (args.splats, args.width, args.height, args.cameras, args.precision):
+                        return int(parts[7])
+    except (OSError, ValueError):
+        pass
+    return None
 
 
 class Clocks:
@@ -305,8 +326,10 @@ def main() -> None:
             ms = float(t.item())
         return ms, sm, prof, nl, ck
 
-    ms_plain, stage_ms_plain, prof_plain, launches_plain, clocks_plain = timed(step_plain, plain)
-    fps_plain = args.steps * ncam * world / (ms_plain / 1000.0)
+    fps_plain = stage_ms_plain = launches_plain = clocks_plain = None
+    if args.forms == "all":
+        ms_plain, stage_ms_plain, prof_plain, launches_plain, clocks_plain = timed(step_plain, plain)
+        fps_plain = args.steps * ncam * world / (ms_plain / 1000.0)
 
     # Batched form: all cameras of a step in one launch sequence.
     batched = P.TiledGaussianPipeline(ds.data(), {"raster_precision": args.precision,
@@ -355,8 +378,10 @@ def main() -> None:
         out.sort()
         return out[len(out) // 2], out[min(len(out) - 1, int(0.99 * len(out)))]
 
-    p50_plain, p99_plain = latencies(lambda i: plain.render(cams[i % ncam], colors[0].data_ptr(), 0,
-                                                            color_format="rgba16f"), args.latency_frames)
+    p50_plain = p99_plain = None
+    if args.forms == "all":
+        p50_plain, p99_plain = latencies(lambda i: plain.render(cams[i % ncam], colors[0].data_ptr(), 0,
+                                                                color_format="rgba16f"), args.latency_frames)
     def batch_once(i):
         with torch.cuda.stream(gstream):
             batched.launch_graph(cams, stream=gstream.cuda_stream)
@@ -402,8 +427,9 @@ def main() -> None:
         gbs = b / (ms * 1e-3) / 1e9 if ms > 0 else 0.0
         stages[name] = {"ms": ms, "bytes": b, "GB/s": gbs, "frac": gbs / hbm}
     dom = max(stages, key=lambda k: stages[k]["ms"])
+    traffic = measured_traffic(dom, args)
     roofline = {"kernel": dom, "bound": "hbm", "achieved": stages[dom]["GB/s"], "peak": hbm, "unit": "GB/s",
-                "frac": stages[dom]["frac"], "traffic": None, "peak_source": peak_kind}
+                "frac": stages[dom]["frac"], "traffic": traffic, "peak_source": peak_kind}
 
     # Image quality of camera 0 against the FP64 oracle, and the CPU baseline.
     cpu = None
