@@ -7,7 +7,15 @@
 // The two pixels share dx and the x-only terms of the quadratic, the record
 // loads, the culling test and the loop.
 //
-// Per record the staging thread folds the opacity into the exponent:
+// The four warps of a tile work independently (no block barrier while
+// blending): each warp walks the tile's sorted records 32 at a time, every
+// lane gathers one packed 32-byte record (pass_common.cuh), tests whether the
+// splat's support can reach the warp's 8x8 patch (the exact minimum of the
+// quadratic over the patch's pixel-centre rectangle, with a margin), and the
+// records that can are compacted, in order, into the warp's shared staging
+// area. A warp leaves the tile as soon as its 64 pixels are done.
+//
+// Per record the projection folded the opacity into the exponent:
 //   p' = log2(opacity) - (a dx^2 + 2 b dx dy + c dy^2) / 2 * log2(e)
 // so alpha = min(opacity e^power, 0.99) = 2^min(p', L), L = min(log2 opacity,
 // log2 0.99), and the reference's alpha >= 1/255 test is p' >= log2(1/255).
@@ -15,11 +23,10 @@
 //   FP32   dx, dy0, dy1, p'0, p'1 and the two threshold compares
 //   half2  min(p', L) and its exp2 (ex2.approx.f16x2)
 //   FP32   transmittance and colour/depth accumulation
-// Each warp walks a compacted list of the records whose support can reach
-// its 8x8 patch. A pixel's transmittance is tested against the threshold once
-// per 32 listed records; a pixel found done stops blending from there on (its
-// threshold becomes +inf), so it may blend up to 31 records more than the
-// reference, whose contributions sum to less than the threshold.
+// A pixel's transmittance is tested against the threshold once per group of
+// 32 records; a pixel found done stops blending from there on (its threshold
+// becomes +inf), so it may blend up to 31 records more than the reference,
+// whose contributions sum to less than the threshold.
 #pragma once
 
 #include <cuda_fp16.h>
@@ -29,6 +36,7 @@
 namespace gs {
 
 constexpr int kHalfThreads = 128;
+constexpr int kHalfWarps = kHalfThreads / 32;
 
 __device__ __forceinline__ __half2 h2ex2_approx(__half2 x) {
   uint32_t in = *reinterpret_cast<uint32_t*>(&x), out;
@@ -36,39 +44,44 @@ __device__ __forceinline__ __half2 h2ex2_approx(__half2 x) {
   return *reinterpret_cast<__half2*>(&out);
 }
 
-struct HalfBatch {
-  float4 geo[kBlock];  // cx, cy, -a/2 log2 e, -b log2 e
-  float4 con[kBlock];  // -c/2 log2 e, log2 opacity, L as half2 bits, depth
-  float4 col[kBlock];
-  float4 raw[kBlock];  // conic (a, b, c) for periodic boundaries
-  uint8_t mask[kBlock];
-  uint8_t list[kHalfThreads / 32][kBlock];  // per warp: staged records that can reach its patch
+// One warp's staged records (up to 32, compacted in record order).
+struct WarpStage {
+  float4 geo[32];  // cx, cy, -a/2 log2 e, -b log2 e
+  float4 con[32];  // -c/2 log2 e, log2 opacity, L as half2 bits, depth
+  float4 col[32];
+  float4 raw[32];  // conic (a, b, c) for periodic boundaries
+  uint8_t idx[32]; // lane (record offset within the group) of each staged record
 };
 
-// Which of the tile's four 8x8 warp patches can hold a pixel centre inside the
-// splat's support: the support's bounding box, widened by 5% and a quarter
-// pixel (which also covers the approximate square roots), against each patch.
-// Near-degenerate conics (condition number above about 4e4) reach every patch.
-__device__ __forceinline__ uint32_t patch_mask8(float cx, float cy, float ca, float cb, float cc, float thr,
-                                                float tile_x0, float tile_y0, uint32_t axis) {
-  if (axis != 0u) return 0xfu;
-  const float det = ca * cc - cb * cb;
-  const float tr = ca + cc;
-  if (!(det > 0.0f) || !(tr * tr <= 4e4f * det) || !(thr >= 0.0f)) return 0xfu;
-  const float q = __fdividef(2.0f * thr, det);
-  const float xx = q * cc, yy = q * ca;
-  const float hx = xx * rsqrtf(xx) * 1.05f + 0.25f;  // 0 gives NaN: every patch
-  const float hy = yy * rsqrtf(yy) * 1.05f + 0.25f;
-  if (!(hx < 1e30f) || !(hy < 1e30f)) return 0xfu;
-  uint32_t m = 0;
+// Can a pixel centre of the rectangle [x0, x0 + 7] x [y0, y0 + 7] pass the
+// splat's alpha >= 1/255 test? With F = -(a' dx^2 + b' dx dy + c' dy^2) (the
+// packed record's scaled conic, F >= 0) and R = log2(255 opacity), a pixel
+// passes when F(d) <= R; the minimum of the convex F over the rectangle is 0
+// when the centre is inside, else it lies on an edge, where the one-variable
+// minimum is clamped to the edge. The margin (1% of R + 0.01) exceeds the
+// rounding of both evaluations for conics whose condition number is below
+// about 1e4; worse-conditioned splats always reach the patch.
+__device__ __forceinline__ bool patch_reach(float cx, float cy, float ap, float bp, float cp, float log2op,
+                                            float x0, float y0) {
+  const float A = -ap, B = -bp, C = -cp;
+  const float det4 = 4.0f * A * C - B * B;  // 4 det of [[A, B/2], [B/2, C]]
+  const float tr = A + C;
+  const float R = log2op + 7.99435329f;
+  if (!(A > 0.0f) || !(C > 0.0f) || !(det4 > 0.0f) || !(tr * tr <= 1e4f * det4)) return true;
+  const float dxl = x0 - cx, dxh = dxl + 7.0f, dyl = y0 - cy, dyh = dyl + 7.0f;
+  if (dxl <= 0.0f && dxh >= 0.0f && dyl <= 0.0f && dyh >= 0.0f) return true;
+  const float ic = __fdividef(-0.5f * B, C), ia = __fdividef(-0.5f * B, A);
+  float m = __int_as_float(0x7f800000);
 #pragma unroll
-  for (uint32_t w = 0; w < 4; ++w) {
-    const float x0 = tile_x0 + (float)(8u * (w & 1u)) + 0.5f;
-    const float y0 = tile_y0 + (float)(8u * (w >> 1)) + 0.5f;
-    const bool hit = cx + hx >= x0 && cx - hx <= x0 + 7.0f && cy + hy >= y0 && cy - hy <= y0 + 7.0f;
-    m |= hit ? (1u << w) : 0u;
+  for (int e = 0; e < 2; ++e) {
+    const float X = e ? dxh : dxl;
+    const float dy = fminf(fmaxf(ic * X, dyl), dyh);
+    m = fminf(m, fmaf(fmaf(C, dy, B * X), dy, A * X * X));
+    const float Y = e ? dyh : dyl;
+    const float dx = fminf(fmaxf(ia * Y, dxl), dxh);
+    m = fminf(m, fmaf(fmaf(A, dx, B * Y), dx, C * Y * Y));
   }
-  return m;
+  return !(m > fmaf(R, 1.01f, 0.01f));  // NaN: reach
 }
 
 __device__ __forceinline__ void blend_pixel(float alpha, const float4& col, float depth, PixelAcc& a) {
@@ -80,108 +93,98 @@ __device__ __forceinline__ void blend_pixel(float alpha, const float4& col, floa
   a.t = a.t - contrib;
 }
 
+// Blend records [s0, s1) of the tile into this warp's two pixels per lane.
+// Warp-level: needs no other warp of the block.
 template <bool PERIODIC, bool STATS>
 __device__ __forceinline__ void blend_range_h2(uint32_t begin, uint32_t source_count, uint32_t raster_count,
                                                uint32_t s0, uint32_t s1, bool capped,
                                                const uint32_t* __restrict__ ids, const float4* __restrict__ mean,
                                                const float4* __restrict__ rec, bool need_depth,
-                                               const RasterFrame& f, float tile_x0, float tile_y0, float pxc,
+                                               const RasterFrame& f, float patch_x0, float patch_y0, float pxc,
                                                float pyc0, bool done0, bool done1, PixelAcc& a0, PixelAcc& a1,
-                                               HalfBatch& sb, RasterCounters& c0n, RasterCounters& c1n) {
-  const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
+                                               WarpStage& ws, RasterCounters& c0n, RasterCounters& c1n) {
+  const uint32_t lane = threadIdx.x & 31u;
   const bool count0 = STATS && !done0, count1 = STATS && !done1;
   uint32_t stop0 = s1, stop1 = s1;
   const float pyc1 = pyc0 + 4.0f;
   const uint32_t lt = (1u << lane) - 1u;
-  for (uint32_t b = s0; b < s1; b += kBlock) {
-    if (!__syncthreads_or(!(done0 && done1))) break;
-#pragma unroll
-    for (uint32_t h = 0; h < 2; ++h) {
-      const uint32_t slot = t + h * kHalfThreads;
-      const uint32_t i = b + slot;
-      if (i < s1) {
-        uint32_t src = i;
-        if (capped) src = (uint32_t)floorf((((float)i + 0.5f) * (float)source_count) / (float)raster_count);
-        const uint32_t g = __ldg(ids + begin + src);
-        const float4 r0 = __ldg(rec + 2 * (size_t)g);  // one 32-byte record
-        const float4 r1 = __ldg(rec + 2 * (size_t)g + 1);
-        const float depth = need_depth ? __ldg(&mean[g].z) : 0.0f;
-        const float4 c = raw_conic(r0, r1);
-        const float thr = (r1.y + 7.99435329f) * 0.693147181f;  // ln(opacity * 255)
-        const uint32_t rg_bits = __float_as_uint(r1.z), bl_bits = __float_as_uint(r1.w);
-        const float2 rg = __half22float2(*reinterpret_cast<const __half2*>(&rg_bits));
-        const __half2 bl = *reinterpret_cast<const __half2*>(&bl_bits);
-        const __half2 lim = __half2half2(__high2half(bl));
-        sb.geo[slot] = r0;
-        sb.con[slot] = make_float4(r1.x, r1.y, __uint_as_float(*reinterpret_cast<const uint32_t*>(&lim)), depth);
-        if (PERIODIC) sb.raw[slot] = c;
-        sb.col[slot] = make_float4(rg.x, rg.y, __low2float(bl), 0.0f);
-        sb.mask[slot] = (uint8_t)patch_mask8(r0.x, r0.y, c.x, c.y, c.z, thr, tile_x0, tile_y0, f.axis);
-      }
+  for (uint32_t b = s0; b < s1; b += 32) {
+    if (__all_sync(0xffffffffu, done0 && done1)) break;
+    const uint32_t i = b + lane;
+    bool reach = false;
+    float4 r0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), r1 = r0;
+    float depth = 0.0f;
+    if (i < s1) {
+      uint32_t src = i;
+      if (capped) src = (uint32_t)floorf((((float)i + 0.5f) * (float)source_count) / (float)raster_count);
+      const uint32_t g = __ldg(ids + begin + src);
+      r0 = __ldg(rec + 2 * (size_t)g);  // one 32-byte record
+      r1 = __ldg(rec + 2 * (size_t)g + 1);
+      if (need_depth) depth = __ldg(&mean[g].z);
+      reach = PERIODIC || patch_reach(r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, patch_x0 + 0.5f, patch_y0 + 0.5f);
     }
-    __syncthreads();
-    // This warp's list of records that can reach its patch, in record order.
-    const uint32_t n = min((uint32_t)kBlock, s1 - b);
-    uint32_t cnt = 0;
-    for (uint32_t k0 = 0; k0 < n; k0 += 32) {
-      const uint32_t k = k0 + lane;
-      const bool reach = k < n && ((sb.mask[k] >> warp) & 1u);
-      const uint32_t bal = __ballot_sync(0xffffffffu, reach);
-      if (reach) sb.list[warp][cnt + __popc(bal & lt)] = (uint8_t)k;
-      cnt += __popc(bal);
+    const uint32_t bal = __ballot_sync(0xffffffffu, reach);
+    if (reach) {
+      const uint32_t q = __popc(bal & lt);
+      const uint32_t rg_bits = __float_as_uint(r1.z), bl_bits = __float_as_uint(r1.w);
+      const float2 rg = __half22float2(*reinterpret_cast<const __half2*>(&rg_bits));
+      const __half2 bl = *reinterpret_cast<const __half2*>(&bl_bits);
+      const __half2 lim = __half2half2(__high2half(bl));
+      ws.geo[q] = r0;
+      ws.con[q] = make_float4(r1.x, r1.y, __uint_as_float(*reinterpret_cast<const uint32_t*>(&lim)), depth);
+      ws.col[q] = make_float4(rg.x, rg.y, __low2float(bl), 0.0f);
+      if (PERIODIC) ws.raw[q] = raw_conic(r0, r1);
+      if (STATS) ws.idx[q] = (uint8_t)lane;
     }
     __syncwarp();
-    for (uint32_t i0 = 0; i0 < cnt; i0 += 32) {
-      if (__all_sync(0xffffffffu, done0 && done1)) break;
-      const float th0 = done0 ? __int_as_float(0x7f800000) : kLog2MinAlpha;
-      const float th1 = done1 ? __int_as_float(0x7f800000) : kLog2MinAlpha;
-      const uint32_t iend = min(i0 + 32u, cnt);
-      for (uint32_t i = i0; i < iend; ++i) {
-        const uint32_t j = sb.list[warp][i];
-        const float4 g = sb.geo[j];
-        const float4 c = sb.con[j];
-        float p0, p1;
-        if (PERIODIC) {
-          const float4 r = sb.raw[j];
-          float dx0, dy0, dx1, dy1;
-          boundary_delta<true>(pxc, pyc0, g.x, g.y, r.x, r.y, r.z, f, &dx0, &dy0);
-          boundary_delta<true>(pxc, pyc1, g.x, g.y, r.x, r.y, r.z, f, &dx1, &dy1);
-          p0 = fmaf(g.z * dx0, dx0, fmaf(g.w * dx0, dy0, fmaf(c.x * dy0, dy0, c.y)));
-          p1 = fmaf(g.z * dx1, dx1, fmaf(g.w * dx1, dy1, fmaf(c.x * dy1, dy1, c.y)));
-        } else {
-          const float dx = pxc - g.x;
-          const float dy0 = pyc0 - g.y, dy1 = pyc1 - g.y;
-          const float bdx = g.w * dx, xx = fmaf(g.z * dx, dx, c.y);
-          p0 = fmaf(fmaf(c.x, dy0, bdx), dy0, xx);
-          p1 = fmaf(fmaf(c.x, dy1, bdx), dy1, xx);
-        }
-        const bool use0 = p0 >= th0;
-        const bool use1 = p1 >= th1;
-        if (!(use0 || use1)) continue;
-        const uint32_t lim_bits = __float_as_uint(c.z);
-        const __half2 e = h2ex2_approx(__hmin2(__floats2half2_rn(p0, p1), *reinterpret_cast<const __half2*>(&lim_bits)));
-        const float2 al = __half22float2(e);
-        const float4 col = sb.col[j];
-        if (use0) {
-          blend_pixel(al.x, col, c.w, a0);
-          if (STATS) {
-            ++c0n.blended;
-            if (a0.t < f.t_threshold && stop0 == s1) stop0 = b + j + 1;
-          }
-        }
-        if (use1) {
-          blend_pixel(al.y, col, c.w, a1);
-          if (STATS) {
-            ++c1n.blended;
-            if (a1.t < f.t_threshold && stop1 == s1) stop1 = b + j + 1;
-          }
+    const uint32_t n = __popc(bal);
+    const float th0 = done0 ? __int_as_float(0x7f800000) : kLog2MinAlpha;
+    const float th1 = done1 ? __int_as_float(0x7f800000) : kLog2MinAlpha;
+    for (uint32_t j = 0; j < n; ++j) {
+      const float4 g = ws.geo[j];
+      const float4 c = ws.con[j];
+      float p0, p1;
+      if (PERIODIC) {
+        const float4 r = ws.raw[j];
+        float dx0, dy0, dx1, dy1;
+        boundary_delta<true>(pxc, pyc0, g.x, g.y, r.x, r.y, r.z, f, &dx0, &dy0);
+        boundary_delta<true>(pxc, pyc1, g.x, g.y, r.x, r.y, r.z, f, &dx1, &dy1);
+        p0 = fmaf(g.z * dx0, dx0, fmaf(g.w * dx0, dy0, fmaf(c.x * dy0, dy0, c.y)));
+        p1 = fmaf(g.z * dx1, dx1, fmaf(g.w * dx1, dy1, fmaf(c.x * dy1, dy1, c.y)));
+      } else {
+        const float dx = pxc - g.x;
+        const float dy0 = pyc0 - g.y, dy1 = pyc1 - g.y;
+        const float bdx = g.w * dx, xx = fmaf(g.z * dx, dx, c.y);
+        p0 = fmaf(fmaf(c.x, dy0, bdx), dy0, xx);
+        p1 = fmaf(fmaf(c.x, dy1, bdx), dy1, xx);
+      }
+      const bool use0 = p0 >= th0;
+      const bool use1 = p1 >= th1;
+      if (!(use0 || use1)) continue;
+      const uint32_t lim_bits = __float_as_uint(c.z);
+      const __half2 e =
+          h2ex2_approx(__hmin2(__floats2half2_rn(p0, p1), *reinterpret_cast<const __half2*>(&lim_bits)));
+      const float2 al = __half22float2(e);
+      const float4 col = ws.col[j];
+      if (use0) {
+        blend_pixel(al.x, col, c.w, a0);
+        if (STATS) {
+          ++c0n.blended;
+          if (a0.t < f.t_threshold && stop0 == s1) stop0 = b + ws.idx[j] + 1;
         }
       }
-      done0 = done0 || a0.t < f.t_threshold;
-      done1 = done1 || a1.t < f.t_threshold;
+      if (use1) {
+        blend_pixel(al.y, col, c.w, a1);
+        if (STATS) {
+          ++c1n.blended;
+          if (a1.t < f.t_threshold && stop1 == s1) stop1 = b + ws.idx[j] + 1;
+        }
+      }
     }
+    done0 = done0 || a0.t < f.t_threshold;
+    done1 = done1 || a1.t < f.t_threshold;
+    __syncwarp();  // the staging area is rewritten by the next group
   }
-  __syncthreads();
   if (count0) c0n.checked += stop0 - s0;
   if (count1) c1n.checked += stop1 - s0;
 }
@@ -209,14 +212,14 @@ __device__ __forceinline__ void store_pixel(const ViewDesc& v, const PassOptions
 }
 
 template <bool PERIODIC, bool STATS>
-__global__ void __launch_bounds__(kHalfThreads, 7) k_raster_h2(const uint32_t* __restrict__ tile_offsets,
+__global__ void __launch_bounds__(kHalfThreads, 8) k_raster_h2(const uint32_t* __restrict__ tile_offsets,
                                                            const uint32_t* __restrict__ order,
                                                            const uint32_t* __restrict__ ids,
                                                            const float4* __restrict__ mean,
                                                            const float4* __restrict__ rec, BatchView bv,
                                                            PassOptions o, Control* __restrict__ ctl) {
   if (ctl->state[3] != 0u) return;  // overflow: nothing is published
-  __shared__ HalfBatch sb;
+  __shared__ WarpStage s_stage[kHalfWarps];
   __shared__ uint32_t s_view;
   __shared__ unsigned long long s_stats[4];
   const uint32_t tile = order ? order[blockIdx.x] : blockIdx.x;
@@ -228,8 +231,10 @@ __global__ void __launch_bounds__(kHalfThreads, 7) k_raster_h2(const uint32_t* _
   const uint32_t local = tile - v.tile_base;
   const uint32_t tx = local % v.tiles_x, ty = local / v.tiles_x;
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-  const uint32_t px = tx * kTileSize + 8u * (warp & 1u) + morton_compact(lane);
-  const uint32_t py0 = ty * kTileSize + 8u * (warp >> 1) + morton_compact(lane >> 1);
+  WarpStage& ws = s_stage[warp];
+  const uint32_t patch_x = tx * kTileSize + 8u * (warp & 1u), patch_y = ty * kTileSize + 8u * (warp >> 1);
+  const uint32_t px = patch_x + morton_compact(lane);
+  const uint32_t py0 = patch_y + morton_compact(lane >> 1);
   const uint32_t py1 = py0 + 4u;
   const uint32_t W = (uint32_t)v.vw, H = (uint32_t)v.vh;
   const bool active0 = px < W && py0 < H, active1 = px < W && py1 < H;
@@ -239,24 +244,23 @@ __global__ void __launch_bounds__(kHalfThreads, 7) k_raster_h2(const uint32_t* _
   const uint32_t raster_count = capped ? min(source_count, o.max_per_tile) : source_count;
   const uint32_t chunk = o.chunk;
   const bool chunked = chunk != 0u && raster_count > chunk;
+  const bool need_depth = v.depth != nullptr;
   const float pxc = (float)px + 0.5f, pyc0 = (float)py0 + 0.5f;
-  const float tile_x0 = (float)(tx * kTileSize), tile_y0 = (float)(ty * kTileSize);
   PixelAcc a0 = {0.0f, 0.0f, 0.0f, 1.0f, 0.0f}, a1 = a0;
   RasterCounters n0 = {0u, 0u}, n1 = {0u, 0u};
   if (!chunked) {
     blend_range_h2<PERIODIC, STATS>(begin, source_count, raster_count, 0, raster_count, capped, ids, mean, rec,
-                                    v.depth != nullptr, f, tile_x0, tile_y0, pxc, pyc0, !active0, !active1, a0, a1,
-                                    sb, n0, n1);
+                                    need_depth, f, (float)patch_x, (float)patch_y, pxc, pyc0, !active0, !active1, a0,
+                                    a1, ws, n0, n1);
   } else {
     const uint32_t nchunk = (raster_count + chunk - 1) / chunk;
     bool fin0 = !active0, fin1 = !active1;
     for (uint32_t ch = 0; ch < nchunk; ++ch) {
-      if (!__syncthreads_or(!(fin0 && fin1))) break;
+      if (__all_sync(0xffffffffu, fin0 && fin1)) break;
       const uint32_t s0 = ch * chunk, s1 = min(s0 + chunk, raster_count);
       PixelAcc p0 = {0.0f, 0.0f, 0.0f, 1.0f, 0.0f}, p1 = p0;
-      blend_range_h2<PERIODIC, STATS>(begin, source_count, raster_count, s0, s1, capped, ids, mean, rec,
-                                      v.depth != nullptr, f, tile_x0, tile_y0, pxc, pyc0, fin0, fin1, p0, p1, sb, n0,
-                                      n1);
+      blend_range_h2<PERIODIC, STATS>(begin, source_count, raster_count, s0, s1, capped, ids, mean, rec, need_depth,
+                                      f, (float)patch_x, (float)patch_y, pxc, pyc0, fin0, fin1, p0, p1, ws, n0, n1);
       if (!fin0) {
         a0.r = a0.r + p0.r * a0.t; a0.g = a0.g + p0.g * a0.t; a0.b = a0.b + p0.b * a0.t;
         a0.d = a0.d + p0.d * a0.t; a0.t = a0.t * p0.t;
