@@ -572,7 +572,7 @@ void launch_tile_ranges(const uint32_t* keys, Control* ctl, uint32_t ntile, uint
 void launch_raster_exact(const uint32_t* tile_offsets, const uint32_t* order, const uint32_t* ids,
                          const float4* mean, const float4* conic, const float4* color, const BatchView& b,
                          const PassOptions& o, Control* ctl, bool stats, cudaStream_t st) {
-  launch_raster_policy<ExactMath>(tile_offsets, order, ids, mean, conic, color, nullptr, b, o, ctl, stats, st);
+  launch_raster_policy<ExactMath>(tile_offsets, order, ids, mean, conic, color, b, o, ctl, stats, st);
 }
 
 }  // namespace gs

@@ -1,6 +1,6 @@
-// FP32 rasterizer with hardware exp2 and multiply-add contraction: the
-// production form of the reference's direct tile rasterizer
-// (src/renderer/pipeline/TileRasterizer.ts:414-805); and the raster work list.
+// The fast raster forms (FP32 and packed half2) of the reference's direct tile
+// rasterizer (src/renderer/pipeline/TileRasterizer.ts:414-805), built with
+// multiply-add contraction, and the raster work list.
 #include "raster_half2.cuh"
 #include "raster_impl.cuh"
 
@@ -65,10 +65,10 @@ void launch_raster(int precision, const uint32_t* tile_offsets, const uint32_t* 
     return;
   }
   if (precision == 2) {
-    launch_raster_half2(tile_offsets, order, ids, mean, color, rec, b, o, ctl, stats, st);
+    launch_raster_pairs(true, tile_offsets, order, ids, mean, color, rec, b, o, ctl, stats, st);
     return;
   }
-  launch_raster_policy<FastMath>(tile_offsets, order, ids, mean, conic, color, rec, b, o, ctl, stats, st);
+  launch_raster_pairs(false, tile_offsets, order, ids, mean, color, rec, b, o, ctl, stats, st);
 }
 
 }  // namespace gs

@@ -1,6 +1,7 @@
-// Packed-half2 form of the tile rasterizer (the reference's direct rasterizer,
+// The fast forms of the tile rasterizer (the reference's direct rasterizer,
 // src/renderer/pipeline/TileRasterizer.ts:414-805, with the same chunk, cap,
-// boundary, background and depth semantics as raster_impl.cuh).
+// boundary, background and depth semantics as raster_impl.cuh): FP32 and
+// packed half2, one kernel template (HALF) over the same pixel-pair layout.
 //
 // 128 threads per 16x16 tile; each thread owns two pixels of one column,
 // (x, y) and (x, y + 4), so warp w owns the 8x8 patch at (8 (w & 1), 8 (w >> 1)).
@@ -21,7 +22,9 @@
 // log2 0.99), and the reference's alpha >= 1/255 test is p' >= log2(1/255).
 // Per record and pixel pair:
 //   FP32   dx, dy0, dy1, p'0, p'1 and the two threshold compares
-//   half2  min(p', L) and its exp2 (ex2.approx.f16x2)
+//   half2 form: min(p', L) and its exp2 in one ex2.approx.f16x2, colour from
+//               the record's f16 values
+//   FP32 form:  min(p', L) and exp2 per pixel (ex2.approx.f32), FP32 colour
 //   FP32   transmittance and colour/depth accumulation
 // A pixel's transmittance is tested against the threshold once per group of
 // 32 records; a pixel found done stops blending from there on (its threshold
@@ -53,37 +56,6 @@ struct WarpStage {
   uint8_t idx[32]; // lane (record offset within the group) of each staged record
 };
 
-// Can a pixel centre of the rectangle [x0, x0 + 7] x [y0, y0 + 7] pass the
-// splat's alpha >= 1/255 test? With F = -(a' dx^2 + b' dx dy + c' dy^2) (the
-// packed record's scaled conic, F >= 0) and R = log2(255 opacity), a pixel
-// passes when F(d) <= R; the minimum of the convex F over the rectangle is 0
-// when the centre is inside, else it lies on an edge, where the one-variable
-// minimum is clamped to the edge. The margin (1% of R + 0.01) exceeds the
-// rounding of both evaluations for conics whose condition number is below
-// about 1e4; worse-conditioned splats always reach the patch.
-__device__ __forceinline__ bool patch_reach(float cx, float cy, float ap, float bp, float cp, float log2op,
-                                            float x0, float y0) {
-  const float A = -ap, B = -bp, C = -cp;
-  const float det4 = 4.0f * A * C - B * B;  // 4 det of [[A, B/2], [B/2, C]]
-  const float tr = A + C;
-  const float R = log2op + 7.99435329f;
-  if (!(A > 0.0f) || !(C > 0.0f) || !(det4 > 0.0f) || !(tr * tr <= 1e4f * det4)) return true;
-  const float dxl = x0 - cx, dxh = dxl + 7.0f, dyl = y0 - cy, dyh = dyl + 7.0f;
-  if (dxl <= 0.0f && dxh >= 0.0f && dyl <= 0.0f && dyh >= 0.0f) return true;
-  const float ic = __fdividef(-0.5f * B, C), ia = __fdividef(-0.5f * B, A);
-  float m = __int_as_float(0x7f800000);
-#pragma unroll
-  for (int e = 0; e < 2; ++e) {
-    const float X = e ? dxh : dxl;
-    const float dy = fminf(fmaxf(ic * X, dyl), dyh);
-    m = fminf(m, fmaf(fmaf(C, dy, B * X), dy, A * X * X));
-    const float Y = e ? dyh : dyl;
-    const float dx = fminf(fmaxf(ia * Y, dxl), dxh);
-    m = fminf(m, fmaf(fmaf(A, dx, B * Y), dx, C * Y * Y));
-  }
-  return !(m > fmaf(R, 1.01f, 0.01f));  // NaN: reach
-}
-
 __device__ __forceinline__ void blend_pixel(float alpha, const float4& col, float depth, PixelAcc& a) {
   const float contrib = a.t * alpha;
   a.r = a.r + col.x * contrib;
@@ -95,10 +67,11 @@ __device__ __forceinline__ void blend_pixel(float alpha, const float4& col, floa
 
 // Blend records [s0, s1) of the tile into this warp's two pixels per lane.
 // Warp-level: needs no other warp of the block.
-template <bool PERIODIC, bool STATS>
+template <bool HALF, bool PERIODIC, bool STATS>
 __device__ __forceinline__ void blend_range_h2(uint32_t begin, uint32_t source_count, uint32_t raster_count,
                                                uint32_t s0, uint32_t s1, bool capped,
                                                const uint32_t* __restrict__ ids, const float4* __restrict__ mean,
+                                               const float4* __restrict__ color,
                                                const float4* __restrict__ rec, bool need_depth,
                                                const RasterFrame& f, float patch_x0, float patch_y0, float pxc,
                                                float pyc0, bool done0, bool done1, PixelAcc& a0, PixelAcc& a1,
@@ -112,7 +85,7 @@ __device__ __forceinline__ void blend_range_h2(uint32_t begin, uint32_t source_c
     if (__all_sync(0xffffffffu, done0 && done1)) break;
     const uint32_t i = b + lane;
     bool reach = false;
-    float4 r0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), r1 = r0;
+    float4 r0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), r1 = r0, col32 = r0;
     float depth = 0.0f;
     if (i < s1) {
       uint32_t src = i;
@@ -120,19 +93,26 @@ __device__ __forceinline__ void blend_range_h2(uint32_t begin, uint32_t source_c
       const uint32_t g = __ldg(ids + begin + src);
       r0 = __ldg(rec + 2 * (size_t)g);  // one 32-byte record
       r1 = __ldg(rec + 2 * (size_t)g + 1);
+      if (!HALF) col32 = __ldg(color + g);
       if (need_depth) depth = __ldg(&mean[g].z);
-      reach = PERIODIC || patch_reach(r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, patch_x0 + 0.5f, patch_y0 + 0.5f);
+      reach = PERIODIC || patch_reach(r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, patch_x0 + 0.5f, patch_y0 + 0.5f,
+                                          7.0f, 7.0f);
     }
     const uint32_t bal = __ballot_sync(0xffffffffu, reach);
     if (reach) {
       const uint32_t q = __popc(bal & lt);
-      const uint32_t rg_bits = __float_as_uint(r1.z), bl_bits = __float_as_uint(r1.w);
-      const float2 rg = __half22float2(*reinterpret_cast<const __half2*>(&rg_bits));
-      const __half2 bl = *reinterpret_cast<const __half2*>(&bl_bits);
-      const __half2 lim = __half2half2(__high2half(bl));
       ws.geo[q] = r0;
-      ws.con[q] = make_float4(r1.x, r1.y, __uint_as_float(*reinterpret_cast<const uint32_t*>(&lim)), depth);
-      ws.col[q] = make_float4(rg.x, rg.y, __low2float(bl), 0.0f);
+      if (HALF) {
+        const uint32_t rg_bits = __float_as_uint(r1.z), bl_bits = __float_as_uint(r1.w);
+        const float2 rg = __half22float2(*reinterpret_cast<const __half2*>(&rg_bits));
+        const __half2 bl = *reinterpret_cast<const __half2*>(&bl_bits);
+        const __half2 lim = __half2half2(__high2half(bl));
+        ws.con[q] = make_float4(r1.x, r1.y, __uint_as_float(*reinterpret_cast<const uint32_t*>(&lim)), depth);
+        ws.col[q] = make_float4(rg.x, rg.y, __low2float(bl), 0.0f);
+      } else {
+        ws.con[q] = make_float4(r1.x, r1.y, fminf(r1.y, kLog2MaxAlpha), depth);
+        ws.col[q] = col32;
+      }
       if (PERIODIC) ws.raw[q] = raw_conic(r0, r1);
       if (STATS) ws.idx[q] = (uint8_t)lane;
     }
@@ -161,10 +141,15 @@ __device__ __forceinline__ void blend_range_h2(uint32_t begin, uint32_t source_c
       const bool use0 = p0 >= th0;
       const bool use1 = p1 >= th1;
       if (!(use0 || use1)) continue;
-      const uint32_t lim_bits = __float_as_uint(c.z);
-      const __half2 e =
-          h2ex2_approx(__hmin2(__floats2half2_rn(p0, p1), *reinterpret_cast<const __half2*>(&lim_bits)));
-      const float2 al = __half22float2(e);
+      float2 al;
+      if (HALF) {
+        const uint32_t lim_bits = __float_as_uint(c.z);
+        al = __half22float2(
+            h2ex2_approx(__hmin2(__floats2half2_rn(p0, p1), *reinterpret_cast<const __half2*>(&lim_bits))));
+      } else {
+        al.x = ex2_approx(fminf(p0, c.z));
+        al.y = ex2_approx(fminf(p1, c.z));
+      }
       const float4 col = ws.col[j];
       if (use0) {
         blend_pixel(al.x, col, c.w, a0);
@@ -211,11 +196,12 @@ __device__ __forceinline__ void store_pixel(const ViewDesc& v, const PassOptions
   if (v.depth) v.depth[off] = finalize_depth(a.d, a.t, o, v.vnear, v.vfar);
 }
 
-template <bool PERIODIC, bool STATS>
-__global__ void __launch_bounds__(kHalfThreads, 8) k_raster_h2(const uint32_t* __restrict__ tile_offsets,
+template <bool HALF, bool PERIODIC, bool STATS>
+__global__ void __launch_bounds__(kHalfThreads, HALF ? 9 : 8) k_raster_h2(const uint32_t* __restrict__ tile_offsets,
                                                            const uint32_t* __restrict__ order,
                                                            const uint32_t* __restrict__ ids,
                                                            const float4* __restrict__ mean,
+                                                           const float4* __restrict__ color,
                                                            const float4* __restrict__ rec, BatchView bv,
                                                            PassOptions o, Control* __restrict__ ctl) {
   if (ctl->state[3] != 0u) return;  // overflow: nothing is published
@@ -249,8 +235,8 @@ __global__ void __launch_bounds__(kHalfThreads, 8) k_raster_h2(const uint32_t* _
   PixelAcc a0 = {0.0f, 0.0f, 0.0f, 1.0f, 0.0f}, a1 = a0;
   RasterCounters n0 = {0u, 0u}, n1 = {0u, 0u};
   if (!chunked) {
-    blend_range_h2<PERIODIC, STATS>(begin, source_count, raster_count, 0, raster_count, capped, ids, mean, rec,
-                                    need_depth, f, (float)patch_x, (float)patch_y, pxc, pyc0, !active0, !active1, a0,
+    blend_range_h2<HALF, PERIODIC, STATS>(begin, source_count, raster_count, 0, raster_count, capped, ids, mean,
+                                          color, rec, need_depth, f, (float)patch_x, (float)patch_y, pxc, pyc0, !active0, !active1, a0,
                                     a1, ws, n0, n1);
   } else {
     const uint32_t nchunk = (raster_count + chunk - 1) / chunk;
@@ -259,7 +245,8 @@ __global__ void __launch_bounds__(kHalfThreads, 8) k_raster_h2(const uint32_t* _
       if (__all_sync(0xffffffffu, fin0 && fin1)) break;
       const uint32_t s0 = ch * chunk, s1 = min(s0 + chunk, raster_count);
       PixelAcc p0 = {0.0f, 0.0f, 0.0f, 1.0f, 0.0f}, p1 = p0;
-      blend_range_h2<PERIODIC, STATS>(begin, source_count, raster_count, s0, s1, capped, ids, mean, rec, need_depth,
+      blend_range_h2<HALF, PERIODIC, STATS>(begin, source_count, raster_count, s0, s1, capped, ids, mean, color,
+                                            rec, need_depth,
                                       f, (float)patch_x, (float)patch_y, pxc, pyc0, fin0, fin1, p0, p1, ws, n0, n1);
       if (!fin0) {
         a0.r = a0.r + p0.r * a0.t; a0.g = a0.g + p0.g * a0.t; a0.b = a0.b + p0.b * a0.t;
@@ -294,17 +281,27 @@ __global__ void __launch_bounds__(kHalfThreads, 8) k_raster_h2(const uint32_t* _
   if (active1) store_pixel(v, o, px, py1, a1);
 }
 
-inline void launch_raster_half2(const uint32_t* tile_offsets, const uint32_t* order, const uint32_t* ids,
+// half = true: packed half2 form; false: FP32 form.
+inline void launch_raster_pairs(bool half, const uint32_t* tile_offsets, const uint32_t* order, const uint32_t* ids,
                                 const float4* mean, const float4* color, const float4* rec, const BatchView& b,
                                 const PassOptions& o, Control* ctl, bool stats, cudaStream_t st) {
-  (void)color;  // colours come from the packed records
   if (b.total_tiles == 0) return;
-#define GS_RASTER_H2(P, S) \
-  k_raster_h2<P, S><<<b.total_tiles, kHalfThreads, 0, st>>>(tile_offsets, order, ids, mean, rec, b, o, ctl)
-  if (o.axis != 0u) {
-    if (stats) GS_RASTER_H2(true, true); else GS_RASTER_H2(true, false);
+#define GS_RASTER_H2(H, P, S)                                                                                   \
+  k_raster_h2<H, P, S><<<b.total_tiles, kHalfThreads, 0, st>>>(tile_offsets, order, ids, mean, color, rec, b, o, \
+                                                               ctl)
+  const bool periodic = o.axis != 0u;
+  if (half) {
+    if (periodic) {
+      if (stats) GS_RASTER_H2(true, true, true); else GS_RASTER_H2(true, true, false);
+    } else {
+      if (stats) GS_RASTER_H2(true, false, true); else GS_RASTER_H2(true, false, false);
+    }
   } else {
-    if (stats) GS_RASTER_H2(false, true); else GS_RASTER_H2(false, false);
+    if (periodic) {
+      if (stats) GS_RASTER_H2(false, true, true); else GS_RASTER_H2(false, true, false);
+    } else {
+      if (stats) GS_RASTER_H2(false, false, true); else GS_RASTER_H2(false, false, false);
+    }
   }
 #undef GS_RASTER_H2
 }

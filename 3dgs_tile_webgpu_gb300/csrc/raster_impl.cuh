@@ -23,15 +23,11 @@
 // transmittance falls below the threshold, which yields exactly the composite
 // of the reference's parallel chunk tasks.
 //
-// Two arithmetic policies:
-//  * ExactMath: the reference's expressions and tests in their order, with the
-//    deterministic exp/log; bit-identical to the CPU restatement when the
-//    translation unit is built with --fmad=false.
-//  * FastMath (blend_range_fast): staging folds -1/2, log2(e) and the opacity
-//    into the quadratic so it gives log2(alpha) directly, one compare rejects
-//    splats below the 1/255 threshold before the exponential (ex2.approx),
-//    each warp walks a compacted list of its records, transmittance is
-//    updated as T - T*alpha and tested once per 32 listed records.
+// Arithmetic: the reference's expressions and tests in their order, with the
+// deterministic exp/log (ExactMath); bit-identical to the CPU restatement when
+// the translation unit is built with --fmad=false. The fast forms
+// (raster_half2.cuh: FP32 and packed half2) share the helpers at the end of this
+// file: the packed-record decoding and the exact ellipse-patch test.
 #pragma once
 
 #include <cuda_fp16.h>
@@ -47,11 +43,6 @@ struct ExactMath {
   static constexpr bool kExact = true;
   static __device__ __forceinline__ float exp(float x) { return gsdm::expf_(x); }
   static __device__ __forceinline__ float log(float x) { return gsdm::logf_(x); }
-};
-struct FastMath {
-  static constexpr bool kExact = false;
-  static __device__ __forceinline__ float exp(float x) { return __expf(x); }
-  static __device__ __forceinline__ float log(float x) { return __logf(x); }
 };
 
 __device__ __forceinline__ float ex2_approx(float x) {
@@ -108,17 +99,13 @@ struct PixelAcc {
   float r, g, b, t, d;
 };
 
-// Shared batch. Exact form: geo = (cx, cy, opacity, threshold), con = (a, b, c,
-// depth). Fast form: geo = (cx, cy, -a/2 log2 e, -b log2 e), con = (-c/2 log2 e,
-// log2 opacity, min(log2 opacity, log2 0.99), depth), with the conic of the
-// periodic form kept as (a, b, c) in raw[] and per-warp record lists.
+// Shared batch of the exact form: geo = (cx, cy, opacity, threshold),
+// con = (a, b, c, depth), colour, and the 8-bit warp-patch masks.
 struct Batch {
   float4 geo[kBlock];
   float4 con[kBlock];
   float4 col[kBlock];
-  float4 raw[kBlock];
   uint8_t mask[kBlock];
-  uint8_t list[kBlock / 32][kBlock];
 };
 
 constexpr float kLog2MinAlpha = -7.99435329f;  // log2(1/255)
@@ -236,93 +223,35 @@ __device__ __forceinline__ float4 raw_conic(const float4& r0, const float4& r1) 
   return make_float4(r0.z * kNeg2Ln2, r0.w * kNegLn2, r1.x * kNeg2Ln2, 0.0f);
 }
 
-// Fast form of blend_range. The staging thread folds the opacity into the
-// exponent, p' = log2(opacity) - q(d)/2 log2(e), so that
-// alpha = min(opacity e^power, 0.99) = 2^min(p', L) with
-// L = min(log2 opacity, log2 0.99), and the reference's alpha >= 1/255 test is
-// p' >= log2(1/255). Each warp walks a compacted list of the records whose
-// support can reach its patch. Transmittance is tested against the threshold
-// once per 32 listed records: a pixel found done takes no more records (its
-// threshold becomes +inf), so it may blend up to 31 records past the
-// reference's stopping point, whose contributions sum to less than the
-// threshold.
-template <bool PERIODIC, bool STATS>
-__device__ __forceinline__ void blend_range_fast(uint32_t begin, uint32_t source_count, uint32_t raster_count,
-                                                 uint32_t s0, uint32_t s1, bool capped,
-                                                 const uint32_t* __restrict__ ids, const float4* __restrict__ mean,
-                                                 const float4* __restrict__ color, const float4* __restrict__ rec,
-                                                 bool need_depth, const RasterFrame& f, float tile_x0, float tile_y0,
-                                                 float pxc, float pyc, bool done, PixelAcc& a, Batch& sb,
-                                                 RasterCounters& cnt) {
-  const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
-  const bool counting = STATS && !done;
-  uint32_t stop = s1;
-  const uint32_t lt = (1u << lane) - 1u;
-  for (uint32_t b = s0; b < s1; b += kBlock) {
-    if (!__syncthreads_or(!done)) break;
-    const uint32_t i = b + t;
-    if (i < s1) {
-      uint32_t src = i;
-      if (capped) src = (uint32_t)floorf((((float)i + 0.5f) * (float)source_count) / (float)raster_count);
-      const uint32_t g = __ldg(ids + begin + src);
-      const float4 r0 = __ldg(rec + 2 * (size_t)g);  // one 32-byte record
-      const float4 r1 = __ldg(rec + 2 * (size_t)g + 1);
-      const float depth = need_depth ? __ldg(&mean[g].z) : 0.0f;
-      const float4 c = raw_conic(r0, r1);
-      const float thr = (r1.y + 7.99435329f) * 0.693147181f;  // ln(opacity * 255)
-      sb.geo[t] = r0;
-      sb.con[t] = make_float4(r1.x, r1.y, fminf(r1.y, kLog2MaxAlpha), depth);
-      if (PERIODIC) sb.raw[t] = c;
-      sb.col[t] = __ldg(color + g);
-      sb.mask[t] = (uint8_t)patch_mask(r0.x, r0.y, c.x, c.y, c.z, thr, tile_x0, tile_y0, f.axis);
-    }
-    __syncthreads();
-    const uint32_t n = min((uint32_t)kBlock, s1 - b);
-    uint32_t listed = 0;
-    for (uint32_t k0 = 0; k0 < n; k0 += 32) {
-      const uint32_t k = k0 + lane;
-      const bool reach = k < n && ((sb.mask[k] >> warp) & 1u);
-      const uint32_t bal = __ballot_sync(0xffffffffu, reach);
-      if (reach) sb.list[warp][listed + __popc(bal & lt)] = (uint8_t)k;
-      listed += __popc(bal);
-    }
-    __syncwarp();
-    for (uint32_t i0 = 0; i0 < listed; i0 += 32) {
-      if (__all_sync(0xffffffffu, done)) break;
-      const float th = done ? __int_as_float(0x7f800000) : kLog2MinAlpha;
-      const uint32_t iend = min(i0 + 32u, listed);
-      for (uint32_t q = i0; q < iend; ++q) {
-        const uint32_t j = sb.list[warp][q];
-        const float4 g = sb.geo[j];
-        const float4 c = sb.con[j];
-        float dx, dy;
-        if (PERIODIC) {
-          const float4 r = sb.raw[j];
-          boundary_delta<true>(pxc, pyc, g.x, g.y, r.x, r.y, r.z, f, &dx, &dy);
-        } else {
-          dx = pxc - g.x;
-          dy = pyc - g.y;
-        }
-        const float p = fmaf(g.z * dx, dx, fmaf(g.w * dx, dy, fmaf(c.x * dy, dy, c.y)));
-        if (!(p >= th)) continue;  // below 1/255, done, or NaN
-        const float alpha = ex2_approx(fminf(p, c.z));
-        const float4 col = sb.col[j];
-        const float contrib = a.t * alpha;
-        a.r = a.r + col.x * contrib;
-        a.g = a.g + col.y * contrib;
-        a.b = a.b + col.z * contrib;
-        a.d = a.d + c.w * contrib;
-        a.t = a.t - contrib;
-        if (STATS) {
-          ++cnt.blended;
-          if (a.t < f.t_threshold && stop == s1) stop = b + j + 1;
-        }
-      }
-      done = done || a.t < f.t_threshold;
-    }
+// Can a pixel centre of the rectangle [x0, x0 + wx] x [y0, y0 + wy] pass the
+// splat's alpha >= 1/255 test? With F = -(a' dx^2 + b' dx dy + c' dy^2) (the
+// packed record's scaled conic, F >= 0) and R = log2(255 opacity), a pixel
+// passes when F(d) <= R; the minimum of the convex F over the rectangle is 0
+// when the centre is inside, else it lies on an edge, where the one-variable
+// minimum is clamped to the edge. The margin (1% of R + 0.01) exceeds the
+// rounding of both evaluations for conics whose condition number is below
+// about 1e4; worse-conditioned splats always reach the rectangle.
+__device__ __forceinline__ bool patch_reach(float cx, float cy, float ap, float bp, float cp, float log2op,
+                                            float x0, float y0, float wx, float wy) {
+  const float A = -ap, B = -bp, C = -cp;
+  const float det4 = 4.0f * A * C - B * B;  // 4 det of [[A, B/2], [B/2, C]]
+  const float tr = A + C;
+  const float R = log2op + 7.99435329f;
+  if (!(A > 0.0f) || !(C > 0.0f) || !(det4 > 0.0f) || !(tr * tr <= 1e4f * det4)) return true;
+  const float dxl = x0 - cx, dxh = dxl + wx, dyl = y0 - cy, dyh = dyl + wy;
+  if (dxl <= 0.0f && dxh >= 0.0f && dyl <= 0.0f && dyh >= 0.0f) return true;
+  const float ic = __fdividef(-0.5f * B, C), ia = __fdividef(-0.5f * B, A);
+  float m = __int_as_float(0x7f800000);
+#pragma unroll
+  for (int e = 0; e < 2; ++e) {
+    const float X = e ? dxh : dxl;
+    const float dy = fminf(fmaxf(ic * X, dyl), dyh);
+    m = fminf(m, fmaf(fmaf(C, dy, B * X), dy, A * X * X));
+    const float Y = e ? dyh : dyl;
+    const float dx = fminf(fmaxf(ia * Y, dxl), dxh);
+    m = fminf(m, fmaf(fmaf(A, dx, B * Y), dx, C * Y * Y));
   }
-  __syncthreads();  // shared batch buffers are free again
-  if (counting) cnt.checked += stop - s0;
+  return !(m > fmaf(R, 1.01f, 0.01f));  // NaN: reach
 }
 
 __device__ __forceinline__ bool finite_r(float v) { return v == v && fabsf(v) <= 3.402823e+38f; }
@@ -357,8 +286,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_raster(const uint32_t* __restrict
                                                    const uint32_t* __restrict__ ids,
                                                    const float4* __restrict__ mean,
                                                    const float4* __restrict__ conic,
-                                                   const float4* __restrict__ color,
-                                                   const float4* __restrict__ rec, BatchView bv, PassOptions o,
+                                                   const float4* __restrict__ color, BatchView bv, PassOptions o,
                                                    Control* __restrict__ ctl) {
   // Overflow: the reference zeroes the raster dispatch, so nothing is written.
   if (ctl->state[3] != 0u) return;
@@ -388,13 +316,8 @@ __global__ void __launch_bounds__(kBlock, 3) k_raster(const uint32_t* __restrict
   PixelAcc a = {0.0f, 0.0f, 0.0f, 1.0f, 0.0f};
   RasterCounters cnt = {0u, 0u};
   if (!chunked) {
-    if constexpr (M::kExact)
-      blend_range<M, PERIODIC, STATS>(begin, source_count, raster_count, 0, raster_count, capped, ids, mean, conic,
-                                      color, f, tile_x0, tile_y0, pxc, pyc, !active, a, sb, cnt);
-    else
-      blend_range_fast<PERIODIC, STATS>(begin, source_count, raster_count, 0, raster_count, capped, ids, mean,
-                                        color, rec, v.depth != nullptr, f, tile_x0, tile_y0, pxc, pyc, !active, a,
-                                        sb, cnt);
+    blend_range<M, PERIODIC, STATS>(begin, source_count, raster_count, 0, raster_count, capped, ids, mean, conic,
+                                    color, f, tile_x0, tile_y0, pxc, pyc, !active, a, sb, cnt);
   } else {
     const uint32_t nchunk = (raster_count + chunk - 1) / chunk;
     bool finished = !active;
@@ -403,12 +326,8 @@ __global__ void __launch_bounds__(kBlock, 3) k_raster(const uint32_t* __restrict
       const uint32_t s0 = ch * chunk;
       const uint32_t s1 = min(s0 + chunk, raster_count);
       PixelAcc p = {0.0f, 0.0f, 0.0f, 1.0f, 0.0f};
-      if constexpr (M::kExact)
-        blend_range<M, PERIODIC, STATS>(begin, source_count, raster_count, s0, s1, capped, ids, mean, conic, color,
-                                        f, tile_x0, tile_y0, pxc, pyc, finished, p, sb, cnt);
-      else
-        blend_range_fast<PERIODIC, STATS>(begin, source_count, raster_count, s0, s1, capped, ids, mean, color, rec,
-                                          v.depth != nullptr, f, tile_x0, tile_y0, pxc, pyc, finished, p, sb, cnt);
+      blend_range<M, PERIODIC, STATS>(begin, source_count, raster_count, s0, s1, capped, ids, mean, conic, color, f,
+                                      tile_x0, tile_y0, pxc, pyc, finished, p, sb, cnt);
       if (!finished) {
         a.r = a.r + p.r * a.t;
         a.g = a.g + p.g * a.t;
@@ -454,13 +373,12 @@ __global__ void __launch_bounds__(kBlock, 3) k_raster(const uint32_t* __restrict
 
 template <class M>
 void launch_raster_policy(const uint32_t* tile_offsets, const uint32_t* order, const uint32_t* ids,
-                          const float4* mean, const float4* conic, const float4* color, const float4* rec,
-                          const BatchView& b, const PassOptions& o, Control* ctl, bool stats, cudaStream_t st) {
+                          const float4* mean, const float4* conic, const float4* color, const BatchView& b,
+                          const PassOptions& o, Control* ctl, bool stats, cudaStream_t st) {
   if (b.total_tiles == 0) return;
   const bool periodic = o.axis != 0u;
-#define GS_RASTER(P, S)                                                                                       \
-  k_raster<M, P, S><<<b.total_tiles, kBlock, 0, st>>>(tile_offsets, order, ids, mean, conic, color, rec, b, o, \
-                                                      ctl)
+#define GS_RASTER(P, S) \
+  k_raster<M, P, S><<<b.total_tiles, kBlock, 0, st>>>(tile_offsets, order, ids, mean, conic, color, b, o, ctl)
   if (periodic) {
     if (stats) GS_RASTER(true, true); else GS_RASTER(true, false);
   } else {
