@@ -85,7 +85,7 @@ def default_options() -> dict:
         "subpixel_sample_culling": True, "raster_transmittance_threshold": 1e-4,
         "depth_alpha_threshold": 0.95, "filter_variance": 0.3, "invalid_depth_value": 1.0,
         "boundary_policy": "clip", "raster_precision": "fp32", "depth_encoding": "device",
-        "raster_stats": False, "device": 0,
+        "raster_stats": False, "projection_precision": "fp32", "device": 0,
     }
 
 
@@ -111,6 +111,7 @@ def make_desc(options: dict | None = None) -> PipelineDesc:
     d.raster_precision = {"fp32": 0, "exact": 1, "half2": 2}[o["raster_precision"]]
     d.depth_encoding = {"device": 0, "raw": 1}[o["depth_encoding"]]
     d.raster_stats = 1 if o["raster_stats"] else 0
+    d.projection_precision = {"fp32": 0, "fp64": 1}[o["projection_precision"]]
     return d
 
 

@@ -3,7 +3,7 @@ from __future__ import annotations
 
 import ctypes as C
 
-GS3D_ABI_VERSION = 1
+GS3D_ABI_VERSION = 2
 GS3D_OK = 0
 GS3D_ERROR_INVALID_ARGUMENT = 1
 GS3D_ERROR_RANGE = 2
@@ -32,7 +32,8 @@ class PipelineDesc(C.Structure):
                 ("raster_transmittance_threshold", C.c_float), ("depth_alpha_threshold", C.c_float),
                 ("filter_variance", C.c_float), ("invalid_depth_value", C.c_float),
                 ("boundary_policy", C.c_uint32), ("raster_precision", C.c_uint32),
-                ("depth_encoding", C.c_uint32), ("raster_stats", C.c_uint32)]
+                ("depth_encoding", C.c_uint32), ("raster_stats", C.c_uint32),
+                ("projection_precision", C.c_uint32)]
 
 
 class Camera(C.Structure):

@@ -46,7 +46,7 @@ struct PassOptions {
   float t_threshold;
   float depth_alpha_threshold;
   float invalid_depth;
-  uint32_t pad0;
+  uint32_t proj_fp64;      // 1: FP64 far-origin mean transform and near-singular conic
 };
 
 // The batch table in device memory: three ascending base arrays (nviews + 1

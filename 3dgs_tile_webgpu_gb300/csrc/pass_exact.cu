@@ -95,6 +95,7 @@ __device__ __forceinline__ uint32_t count_tiles_warp(CountShared& sm, uint32_t n
   return sm.cnt[warp][lane];
 }
 
+template <bool FP64>
 __global__ void __launch_bounds__(kBlock, 4) k_project(BatchView b, PassOptions o, float4* __restrict__ mean_out,
                                                     float4* __restrict__ conic_out, float4* __restrict__ color_out,
                                                     uint32_t* __restrict__ count_out, uint32_t* __restrict__ key_out,
@@ -137,10 +138,20 @@ __global__ void __launch_bounds__(kBlock, 4) k_project(BatchView b, PassOptions 
     const float ddx = mo.x - camx, ddy = mo.y - camy, ddz = mo.z - camz;
     const float dlen = sqrtf((ddx * ddx + ddy * ddy) + ddz * ddz);
     vdir = {ddx / dlen, ddy / dlen, ddz / dlen};
-    // view = modelView * (p, 1) (:479-482)
-    const float vx = ((mv[0] * mo.x + mv[4] * mo.y) + mv[8] * mo.z) + mv[12] * 1.0f;
-    const float vy = ((mv[1] * mo.x + mv[5] * mo.y) + mv[9] * mo.z) + mv[13] * 1.0f;
-    const float vz = ((mv[2] * mo.x + mv[6] * mo.y) + mv[10] * mo.z) + mv[14] * 1.0f;
+    // view = modelView * (p, 1) (:479-482); the FP64 form evaluates it in
+    // double so far-origin coordinates do not cancel against the translation.
+    double vxd = 0.0, vyd = 0.0, vzd = 0.0;
+    float vx, vy, vz;
+    if (FP64) {
+      vxd = (((double)mv[0] * mo.x + (double)mv[4] * mo.y) + (double)mv[8] * mo.z) + (double)mv[12];
+      vyd = (((double)mv[1] * mo.x + (double)mv[5] * mo.y) + (double)mv[9] * mo.z) + (double)mv[13];
+      vzd = (((double)mv[2] * mo.x + (double)mv[6] * mo.y) + (double)mv[10] * mo.z) + (double)mv[14];
+      vx = (float)vxd; vy = (float)vyd; vz = (float)vzd;
+    } else {
+      vx = ((mv[0] * mo.x + mv[4] * mo.y) + mv[8] * mo.z) + mv[12] * 1.0f;
+      vy = ((mv[1] * mo.x + mv[5] * mo.y) + mv[9] * mo.z) + mv[13] * 1.0f;
+      vz = ((mv[2] * mo.x + mv[6] * mo.y) + mv[10] * mo.z) + mv[14] * 1.0f;
+    }
     m3 l2v;
 #pragma unroll
     for (int c = 0; c < 3; ++c)
@@ -151,6 +162,14 @@ __global__ void __launch_bounds__(kBlock, 4) k_project(BatchView b, PassOptions 
 #pragma unroll
     for (int i = 0; i < 16; ++i) P[i] = v.P[i];
     pr = project({vx, vy, vz}, cv, P, vw, vh, v.vnear, v.vfar, o.filter);
+    if (FP64) {
+      // Near-singular in FP32 (tiny anti-aliasing factor, high condition
+      // number, or rejected past the depth test): redo the chain in double.
+      const float cond_num = (pr.cov_x + pr.cov_z) * (pr.cov_x + pr.cov_z);
+      const bool redo = !pr.ok ? (-vz > v.vnear && -vz < v.vfar)
+                               : (pr.orig_det < 1e-2f * pr.det || !(cond_num <= 4e3f * pr.det));
+      if (redo) pr = project_fp64(vxd, vyd, vzd, so, q, mv, P, vw, vh, v.vnear, v.vfar, o.filter);
+    }
     if (!pr.ok) break;
     op = clampf(so.w, 0.0f, 1.0f);
     if (o.antialias == 0u) op = op * sqrtf(clampf(pr.orig_det / pr.det, 0.0f, 1.0f));
@@ -221,7 +240,10 @@ __global__ void __launch_bounds__(kBlock, 4) k_project(BatchView b, PassOptions 
 void launch_project(const BatchView& b, const PassOptions& o, float4* mean, float4* conic, float4* color,
                     uint32_t* counts, uint32_t* keys, float4* rec, cudaStream_t st) {
   if (b.total_blocks == 0) return;
-  k_project<<<b.total_blocks, kBlock, 0, st>>>(b, o, mean, conic, color, counts, keys, rec);
+  if (o.proj_fp64)
+    k_project<true><<<b.total_blocks, kBlock, 0, st>>>(b, o, mean, conic, color, counts, keys, rec);
+  else
+    k_project<false><<<b.total_blocks, kBlock, 0, st>>>(b, o, mean, conic, color, counts, keys, rec);
 }
 
 // ---------------------------------------------------------------------------

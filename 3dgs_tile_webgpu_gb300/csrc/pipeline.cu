@@ -144,6 +144,7 @@ gs3d_status validate_desc(gs3d_pipeline* p, const gs3d_pipeline_desc& d) {
   if (d.boundary_policy > 2) return fail(p, GS3D_ERROR_INVALID_ARGUMENT, "boundaryPolicy must be clip, repeat-x or repeat-y");
   if (d.raster_precision > 2) return fail(p, GS3D_ERROR_INVALID_ARGUMENT, "unknown raster precision");
   if (d.depth_encoding > 1) return fail(p, GS3D_ERROR_INVALID_ARGUMENT, "unknown depth encoding");
+  if (d.projection_precision > 1) return fail(p, GS3D_ERROR_INVALID_ARGUMENT, "unknown projection precision");
   // GaussianPass.ts:178-192,231-255
   if (d.intersection_capacity == 0 || d.intersection_capacity > 0x7fffffffull)
     return fail(p, GS3D_ERROR_RANGE, "intersectionCapacity must be a positive integer below 2^31");
@@ -351,6 +352,7 @@ void gs3d_pipeline_desc_defaults(gs3d_pipeline_desc* d) {
   d->boundary_policy = GS3D_BOUNDARY_CLIP;
   d->raster_precision = GS3D_RASTER_FP32;
   d->depth_encoding = 0;
+  d->projection_precision = GS3D_PROJECTION_FP32;
 }
 
 gs3d_status gs3d_pipeline_create(const gs3d_pipeline_desc* desc, const gs3d_gaussian_data* data,
@@ -596,6 +598,7 @@ void record_batch(gs3d_pipeline* p, const Plan& pl, unsigned char* dev, cudaStre
   o.chunk = p->desc.raster_chunk_size;
   o.max_per_tile = p->desc.max_rasterized_splats_per_tile;
   o.depth_encoding = p->desc.depth_encoding;
+  o.proj_fp64 = p->desc.projection_precision == GS3D_PROJECTION_FP64 ? 1u : 0u;
   memcpy(o.background, p->desc.background, sizeof(o.background));
   o.t_threshold = p->desc.raster_transmittance_threshold;
   o.depth_alpha_threshold = p->desc.depth_alpha_threshold;

@@ -193,6 +193,91 @@ __device__ __forceinline__ Projected project(f3 view, const m3& cv, const float*
   return o;
 }
 
+// FP64 form of view_covariance + project (projectionHelpers.ts:4-116), for the
+// FP64 projection form: the same steps, constants and tests in double
+// precision, from the view-space centre the caller computed in double. Used
+// for far-origin scenes (the caller's double mean transform avoids the
+// cancellation between large world coordinates and the model-view
+// translation) and for near-singular splats (the 2D covariance, its
+// determinant and the conic lose most of their bits in FP32 when the
+// projected covariance is nearly rank one).
+__device__ __noinline__ Projected project_fp64(double vx, double vy, double vz, float4 so, float4 q_in,
+                                               const float* mv, const float* P, float vw, float vh, float vnear,
+                                               float vfar, float filter) {
+  Projected o;
+  o.ok = false;
+  const double depth = -vz;
+  if (!(depth > (double)vnear && depth < (double)vfar)) return o;
+  const double clip_x = (P[0] * vx + P[4] * vy) + P[8] * vz + P[12];
+  const double clip_y = (P[1] * vx + P[5] * vy) + P[9] * vz + P[13];
+  const double clip_w = (P[3] * vx + P[7] * vy) + P[11] * vz + P[15];
+  if (clip_w <= 0.0) return o;
+  // 3D covariance R S^2 R^T in view space (L R S^2 R^T L^T, L = model-view 3x3).
+  const double sx = fmax((double)so.x, 1e-7), sy = fmax((double)so.y, 1e-7), sz = fmax((double)so.z, 1e-7);
+  const double qn = sqrt(((double)q_in.x * q_in.x + (double)q_in.y * q_in.y) + (double)q_in.z * q_in.z +
+                         (double)q_in.w * q_in.w);
+  const double qx = q_in.x / qn, qy = q_in.y / qn, qz = q_in.z / qn, qw = q_in.w / qn;
+  double R[3][3];  // R[c][r], column-major like m3
+  R[0][0] = 1.0 - 2.0 * (qy * qy + qz * qz); R[0][1] = 2.0 * (qx * qy + qz * qw); R[0][2] = 2.0 * (qx * qz - qy * qw);
+  R[1][0] = 2.0 * (qx * qy - qz * qw); R[1][1] = 1.0 - 2.0 * (qx * qx + qz * qz); R[1][2] = 2.0 * (qy * qz + qx * qw);
+  R[2][0] = 2.0 * (qx * qz + qy * qw); R[2][1] = 2.0 * (qy * qz - qx * qw); R[2][2] = 1.0 - 2.0 * (qx * qx + qy * qy);
+  const double s2[3] = {sx * sx, sy * sy, sz * sz};
+  double M[3][3];  // M = L R (columns), so the covariance is M diag(s2) M^T
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+      M[c][r] = ((double)mv[r] * R[c][0] + (double)mv[4 + r] * R[c][1]) + (double)mv[8 + r] * R[c][2];
+  double cv[3][3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int r = 0; r < 3; ++r) cv[c][r] = (M[0][r] * s2[0] * M[0][c] + M[1][r] * s2[1] * M[1][c]) + M[2][r] * s2[2] * M[2][c];
+  const double cx = ((clip_x / clip_w) * 0.5 + 0.5) * vw;
+  const double cy = (0.5 - (clip_y / clip_w) * 0.5) * vh;
+  const double fx = (0.5 * vw) * P[0], fy = (0.5 * vh) * P[5];
+  const double inv = 1.0 / depth;
+  const double j0[3] = {fx * inv, 0.0, fx * vx * inv * inv};
+  const double j1[3] = {0.0, -fy * inv, -fy * vy * inv * inv};
+  double t0[3], t1[3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    t0[r] = (cv[0][r] * j0[0] + cv[1][r] * j0[1]) + cv[2][r] * j0[2];
+    t1[r] = (cv[0][r] * j1[0] + cv[1][r] * j1[1]) + cv[2][r] * j1[2];
+  }
+  const double c_x = (j0[0] * t0[0] + j0[1] * t0[1]) + j0[2] * t0[2];
+  const double c_y = (j0[0] * t1[0] + j0[1] * t1[1]) + j0[2] * t1[2];
+  const double c_z = (j1[0] * t1[0] + j1[1] * t1[1]) + j1[2] * t1[2];
+  const double orig_det = fmax(c_x * c_z - c_y * c_y, 0.0);
+  double s00 = c_x + filter, s01 = c_y, s11 = c_z + filter;
+  if (!(isfinite(s00) && isfinite(s01) && isfinite(s11))) return o;
+  const double mid = 0.5 * (s00 + s11);
+  const double rad = sqrt((0.25 * (s00 - s11)) * (s00 - s11) + s01 * s01);
+  const double lmin = fmin(fmax(mid - rad, 1e-6), 1e4), lmax = fmin(fmax(mid + rad, 1e-6), 1e4);
+  const double theta = 0.5 * atan2(2.0 * s01, s00 - s11);
+  const double cs = cos(theta), sn = sin(theta);
+  s00 = (lmin * sn) * sn + (lmax * cs) * cs;
+  s01 = ((lmax - lmin) * cs) * sn;
+  s11 = (lmin * cs) * cs + (lmax * sn) * sn;
+  // Exact arithmetic keeps both diagonal terms in [lmin, lmax]; hold that so
+  // the 1e4 bound below does not flip on rounding for splats whose
+  // eigenvalues are both clamped (the FP32 form drops some of those).
+  s00 = fmin(fmax(s00, lmin), lmax);
+  s11 = fmin(fmax(s11, lmin), lmax);
+  const double det = s00 * s11 - s01 * s01;
+  if (det <= 1e-8) return o;
+  const double k0 = s11 / det, k1 = -s01 / det, k2 = s00 / det;
+  if (!(isfinite(cx) && isfinite(cy) && isfinite(depth) && isfinite(k0) && isfinite(k1) && isfinite(k2)))
+    return o;
+  if (!(depth > 0.0 && s00 > 0.0 && s11 > 0.0 && s00 <= 1e4 && s11 <= 1e4 && k0 > 0.0 && k2 > 0.0)) return o;
+  o.ok = true;
+  o.cx = (float)cx; o.cy = (float)cy; o.depth = (float)depth;
+  o.conic_x = (float)k0; o.conic_y = (float)k1; o.conic_z = (float)k2;
+  o.cov_x = (float)s00; o.cov_z = (float)s11;
+  o.det = (float)det; o.orig_det = (float)orig_det;
+  return o;
+}
+
 // projectionHelpers.ts:150-155: unpack4x8snorm(.xyz) * exp2(e). `snorm`
 // holds max(b / 127, -1) for every signed byte b (index b & 255), the exact
 // quotients, so the lookup is bit-identical to dividing.

@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define GS3D_ABI_VERSION 1u
+#define GS3D_ABI_VERSION 2u
 
 typedef enum gs3d_status {
   GS3D_OK = 0,
@@ -63,6 +63,17 @@ typedef enum gs3d_boundary_policy {
  * deterministic math library and no FMA contraction (bit-identical to the CPU
  * restatement). HALF2 evaluates Gaussian weights two pixels per lane in packed
  * half precision with FP32 transmittance and colour accumulation. */
+/* Projection arithmetic. FP32 is the reference's (ProjectionStage.ts, bit-exact
+ * with the CPU restatement). FP64 has no counterpart in the reference: it
+ * evaluates the model-view mean transform in double (far-origin scenes) and
+ * redoes the covariance -> determinant -> conic chain in double for splats
+ * that are near-singular in FP32; results then follow the FP64 oracle, not the
+ * FP32 restatement. */
+typedef enum gs3d_projection_precision {
+  GS3D_PROJECTION_FP32 = 0,
+  GS3D_PROJECTION_FP64 = 1
+} gs3d_projection_precision;
+
 typedef enum gs3d_raster_precision {
   GS3D_RASTER_FP32 = 0,
   GS3D_RASTER_EXACT = 1,
@@ -109,6 +120,7 @@ typedef struct gs3d_pipeline_desc {
   uint32_t raster_precision;      /* gs3d_raster_precision, default FP32 */
   uint32_t depth_encoding;        /* 0: default device depth node; 1: raw alpha-weighted depth */
   uint32_t raster_stats;          /* rasterStats (types.ts:283): per-pixel work counters, default 0 */
+  uint32_t projection_precision;  /* gs3d_projection_precision, default FP32 */
 } gs3d_pipeline_desc;
 
 /* Per-frame camera state: what FrameUniforms.update and ObjectFrameState.update

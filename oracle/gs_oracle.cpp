@@ -248,6 +248,14 @@ template <typename T> static M4<T> projection_result(V2<T> center, T depth, V3<T
   s00 = (lmin * sn) * sn + (lmax * cs) * cs;
   s01 = ((lmax - lmin) * cs) * sn;
   s11 = (lmin * cs) * cs + (lmax * sn) * sn;
+  if (sizeof(T) == sizeof(double)) {
+    // FP64 twin: in exact arithmetic both diagonal terms lie in [lmin, lmax]
+    // (cos^2 + sin^2 = 1); keep that so the validity test's 1e4 bound does not
+    // flip on the last bit for splats whose eigenvalues are both clamped. The
+    // FP32 restatement keeps the reference's rounding, cliff included.
+    s00 = clampT(s00, lmin, lmax);
+    s11 = clampT(s11, lmin, lmax);
+  }
   T det = s00 * s11 - s01 * s01;
   if (det <= K<T>(1e-8f)) return zero_m4<T>();
   T inv = K<T>(1.0f) / det;

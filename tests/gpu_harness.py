@@ -26,6 +26,7 @@ def pipeline_options(frame: dict, precision: str = "exact", capacity: int | None
         "invalid_depth_value": float(frame.get("invalid_depth_value", 1.0)),
         "depth_encoding": "raw" if frame.get("depth_encoding", 0) == 1 else "device",
         "raster_precision": precision,
+        "projection_precision": frame.get("projection_precision", "fp32"),
     }
 
 

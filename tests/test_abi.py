@@ -40,6 +40,7 @@ def test_abi_version_and_defaults(lib):
     assert abs(d.depth_alpha_threshold - 0.95) < 1e-7
     assert abs(d.filter_variance - 0.3) < 1e-7
     assert d.subpixel_sample_culling == 1
+    assert d.projection_precision == 0  # FP32: the reference's arithmetic
 
 
 @pytest.mark.parametrize("field,value,status", [
@@ -50,6 +51,7 @@ def test_abi_version_and_defaults(lib):
     ("depth_alpha_threshold", 1.5, 2),           # GaussianPass.ts:231-238
     ("intersection_capacity", 0, 2),
     ("depth_sort_mode", 5, 1),
+    ("projection_precision", 2, 1),
     ("abi_version", 99, 1),
 ])
 def test_invalid_options_are_rejected_before_any_device_work(lib, field, value, status):
