@@ -141,36 +141,48 @@ __device__ __forceinline__ unsigned long long wait_status(const unsigned long lo
   return v;
 }
 
-// Warp-wide decoupled look-back for a single value per tile: every lane reads
-// one predecessor, so one round trip covers 32 tiles. Returns the exclusive
-// prefix of `tile` in every lane. All 32 lanes of the warp must call it.
-template <bool SATURATE>
+// Warp-wide decoupled look-back for a single value per tile: every lane
+// requests K predecessors at once (lane l reads tile end - 32 k - l), so one
+// round trip covers 32 K tiles; the sub-windows are then resolved nearest
+// first, waiting only on the ones needed before an inclusive prefix turns up.
+// Returns the exclusive prefix of `tile` in every lane. All 32 lanes of the
+// warp must call it.
+template <bool SATURATE, int K = 4>
 __device__ __forceinline__ uint32_t warp_lookback(const unsigned long long* status, uint32_t tile, uint32_t epoch,
                                                   uint32_t* err) {
   const uint32_t lane = threadIdx.x & 31u;
   uint32_t excl = 0;
   int64_t end = (int64_t)tile - 1;
   while (end >= 0) {
-    const int64_t idx = end - (int64_t)lane;
-    bool incl = true, expired = false;
-    uint32_t val = 0;
-    if (idx >= 0) {
-      const unsigned long long* p = status + idx;
-      const unsigned long long v = wait_status(p, ld_acquire(p), epoch, err, &expired);
-      incl = expired || ((v >> 32) & 3ull) == kFlagInclusive;
-      val = expired ? 0u : (uint32_t)v;
-    }
-    const uint32_t inc_mask = __ballot_sync(0xffffffffu, incl);
-    const uint32_t stop = inc_mask ? (uint32_t)(__ffs(inc_mask) - 1) : 31u;  // nearest inclusive lane
-    uint32_t x = lane <= stop ? val : 0u;
+    unsigned long long v[K];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const uint32_t y = __shfl_xor_sync(0xffffffffu, x, o);
-      x = SATURATE ? sat_add(x, y) : x + y;
+    for (int k = 0; k < K; ++k) {
+      const int64_t idx = end - 32 * k - (int64_t)lane;
+      v[k] = idx >= 0 ? ld_acquire(status + idx) : 0ull;
     }
-    excl = SATURATE ? sat_add(excl, x) : excl + x;
-    if (inc_mask) break;
-    end -= 32;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      if (end - 32 * k < 0) return excl;  // no predecessors left
+      const int64_t idx = end - 32 * k - (int64_t)lane;
+      bool incl = true, expired = false;
+      uint32_t val = 0;
+      if (idx >= 0) {
+        const unsigned long long w = wait_status(status + idx, v[k], epoch, err, &expired);
+        incl = expired || ((w >> 32) & 3ull) == kFlagInclusive;
+        val = expired ? 0u : (uint32_t)w;
+      }
+      const uint32_t inc_mask = __ballot_sync(0xffffffffu, incl);
+      const uint32_t stop = inc_mask ? (uint32_t)(__ffs(inc_mask) - 1) : 31u;  // nearest inclusive lane
+      uint32_t x = lane <= stop ? val : 0u;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const uint32_t y = __shfl_xor_sync(0xffffffffu, x, o);
+        x = SATURATE ? sat_add(x, y) : x + y;
+      }
+      excl = SATURATE ? sat_add(excl, x) : excl + x;
+      if (inc_mask) return excl;
+    }
+    end -= 32 * K;
   }
   return excl;
 }

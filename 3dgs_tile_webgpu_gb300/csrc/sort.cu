@@ -26,6 +26,7 @@
 namespace gs {
 
 constexpr int kSortWarps = 8;
+constexpr int kSortWindow = 8;  // predecessor tiles requested per look-back round trip, per digit
 constexpr int kSortItems = 16;  // kSortTile = 8 warps * 32 lanes * 16 items
 
 // Lanes of the warp holding the same BITS-bit digit, by ballot bit-splitting.
@@ -147,7 +148,7 @@ __global__ void __launch_bounds__(kBlock, 3)
   if (tid < RADIX) {
     uint32_t prefix = 0;
     if (tile > 0) {
-      prefix = window_lookback<8>(status + tid, RADIX, tile, epoch, err);
+      prefix = window_lookback<kSortWindow>(status + tid, RADIX, tile, epoch, err);
       st_release(status + (size_t)tile * RADIX + tid, pack_status(epoch, kFlagInclusive, prefix + block_count));
     }
     s_global_base[tid] = s_hist_excl[tid] + prefix;
