@@ -18,7 +18,7 @@ import os
 import threading
 
 from . import abi
-from .abi import (GS3D_OK, Camera, GaussianData, PipelineDesc, Resources, Stats, Targets, View)
+from .abi import (GS3D_OK, Camera, GaussianData, PipelineDesc, Resources, Stats, Targets, Tuning, View)
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "_build", "libgs3d.so")
@@ -206,6 +206,32 @@ class TiledGaussianPipeline:
                                     if depth_ptr else None)
             keep.append((data, cam))
         return arr, keep
+
+    def set_tuning(self, tuning: dict) -> None:
+        """Launch shape (outputs do not depend on it): ``views_per_launch``
+        (0 = a whole batch at once), ``tile_digit_bits`` (4..8),
+        ``work_order`` (1 = heaviest tiles first)."""
+        t = Tuning()
+        self._lib.gs3d_pipeline_get_tuning(self._p, C.byref(t))
+        for k, v in tuning.items():
+            setattr(t, k, int(v))
+        _raise(self._lib, self._lib.gs3d_pipeline_set_tuning(self._p, C.byref(t)), self._p)
+
+    def get_tuning(self) -> dict:
+        t = Tuning()
+        _raise(self._lib, self._lib.gs3d_pipeline_get_tuning(self._p, C.byref(t)), self._p)
+        return {"views_per_launch": t.views_per_launch, "tile_digit_bits": t.tile_digit_bits,
+                "work_order": t.work_order}
+
+    def autotune(self, views: list, trials: int = 3, stream: int = 0) -> tuple[dict, float]:
+        """Time candidate tunings on this batch (same tuple layout as
+        render_batch), keep the fastest; returns (tuning, ms per batch)."""
+        arr, keep = self._views_array(views)
+        t, ms = Tuning(), C.c_double()
+        _raise(self._lib, self._lib.gs3d_pipeline_autotune(self._p, arr, len(views), int(trials), C.byref(t),
+                                                           C.byref(ms), C.c_void_p(int(stream))), self._p)
+        del keep
+        return self.get_tuning(), float(ms.value)
 
     def capture_graph(self, views: list, stream: int) -> None:
         """Capture the batched pass for these views into CUDA graphs (same

@@ -52,6 +52,11 @@ class View(C.Structure):
                 ("height", C.c_uint32), ("targets", Targets)]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("views_per_launch", C.c_uint32), ("tile_digit_bits", C.c_uint32), ("work_order", C.c_uint32),
+                ("reserved", C.c_uint32)]
+
+
 class Stats(C.Structure):
     _fields_ = [("visible_gaussian_count", C.c_uint32), ("intersection_count", C.c_uint32),
                 ("requested_intersections", C.c_uint32), ("overflow", C.c_uint32),
@@ -82,6 +87,10 @@ SIGNATURES = {
     "gs3d_pipeline_prepare_frame": (C.c_int, [_P, C.c_uint32, C.c_uint32]),
     "gs3d_pipeline_render": (C.c_int, [_P, C.POINTER(Camera), C.c_uint32, C.c_int, C.POINTER(Targets), _P]),
     "gs3d_pipeline_render_batch": (C.c_int, [_P, C.POINTER(View), C.c_uint32, C.c_uint32, C.c_int, _P]),
+    "gs3d_pipeline_set_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
+    "gs3d_pipeline_get_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
+    "gs3d_pipeline_autotune": (C.c_int, [_P, C.POINTER(View), C.c_uint32, C.c_uint32, C.POINTER(Tuning),
+                                         C.POINTER(C.c_double), _P]),
     "gs3d_pipeline_capture_graph": (C.c_int, [_P, C.POINTER(View), C.c_uint32, _P]),
     "gs3d_pipeline_launch_graph": (C.c_int, [_P, C.POINTER(Camera), C.c_uint32, C.c_uint32, C.c_int, _P]),
     "gs3d_pipeline_batch_layout": (C.c_int, [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.c_uint32,

@@ -20,13 +20,55 @@ namespace {
 
 constexpr uint32_t kObjectRing = 4;  // pinned batch-table staging slots
 constexpr uint32_t kMaxViews = 4096;
-constexpr uint32_t kEpochMask = (1u << 30) - 1u;
 constexpr uint32_t kStageEvents = GS3D_STAGE_COUNT + 1;
 
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
 };
+
+}  // namespace
+
+// Totals of a batch rendered as several launch sequences (views per launch
+// below the batch size): every launch sequence zeroes and refills the control
+// block, so its counts are added here before the next one starts.
+struct BatchSummary {
+  uint32_t visible, intersections, requested, overflow;
+  uint32_t error, prev_version, chunks, pad;
+  unsigned long long raster[4];
+};
+
+namespace {
+
+__global__ void k_summary_begin(BatchSummary* s, const uint32_t* output_state) {
+  s->visible = s->intersections = s->requested = s->overflow = 0u;
+  s->error = s->chunks = s->pad = 0u;
+  s->prev_version = output_state[1];
+  for (int i = 0; i < 4; ++i) s->raster[i] = 0ull;
+}
+
+// Adds one launch sequence's counts; after the last one, writes the batch's
+// output state (attempt, version, demand, overflow): the version advances
+// only if no launch sequence overflowed, and the demand is the largest of the
+// sequences (they share one intersection buffer).
+__global__ void k_summary_add(BatchSummary* s, const Control* c, const uint32_t* frame_params,
+                              uint32_t* output_state, int last) {
+  s->visible += c->visible_state[0];
+  s->intersections += c->state[0];
+  s->requested = max(s->requested, c->state[1]);
+  s->overflow |= c->state[3];
+  s->error |= c->error;
+  for (int i = 0; i < 4; ++i) s->raster[i] += c->raster_stats[i];
+  s->chunks += 1u;
+  if (last) {
+    const uint32_t attempt = frame_params[0];
+    const uint32_t last_version = frame_params[1] ? 0u : s->prev_version;
+    output_state[0] = attempt;
+    output_state[1] = s->overflow ? last_version : attempt;
+    output_state[2] = s->requested;
+    output_state[3] = s->overflow ? 1u : 0u;
+  }
+}
 
 }  // namespace
 
@@ -89,6 +131,16 @@ struct gs3d_pipeline {
   std::vector<gs3d_camera> graph_cameras;
   uint32_t graph_launches = 0;
   uint32_t graph_next = 0;
+  // Tuning (gs3d_pipeline_set_tuning / autotune) and the device summary of a
+  // batch rendered as several launch sequences.
+  gs3d_tuning tuning{0u, 8u, 1u, 0u};
+  BatchSummary* summary = nullptr;
+  uint32_t last_chunks = 1;
+  struct GraphChunk {
+    uint32_t first, count;
+    size_t offset;
+  };
+  std::vector<GraphChunk> graph_chunks;
   // Frame.
   bool prepared = false;
   uint32_t width = 0, height = 0, tiles_x = 0, tiles_y = 0;
@@ -312,6 +364,7 @@ void release_all(gs3d_pipeline* p) {
   dfree(p->dk[0]); dfree(p->dk[1]); dfree(p->dv[0]); dfree(p->dv[1]); dfree(p->ordered); dfree(p->ioff);
   dfree(p->tk[0]); dfree(p->tk[1]); dfree(p->tv[0]); dfree(p->tv[1]);
   dfree(p->tile_offsets); dfree(p->tile_order); dfree(p->ctl); dfree(p->epoch_dev); dfree(p->output_state); dfree(p->status);
+  dfree(p->summary);
 }
 
 }  // namespace
@@ -376,7 +429,8 @@ gs3d_status gs3d_pipeline_create(const gs3d_pipeline_desc* desc, const gs3d_gaus
   }
   cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, p->device);
   for (uint32_t i = 0; i < kObjectRing; ++i) cudaEventCreateWithFlags(&p->stage_ev[i], cudaEventDisableTiming);
-  if ((e = dalloc(p->ctl, 1)) || (e = dalloc(p->output_state, 4)) || (e = dalloc(p->epoch_dev, 1))) {
+  if ((e = dalloc(p->ctl, 1)) || (e = dalloc(p->output_state, 4)) || (e = dalloc(p->epoch_dev, 1)) ||
+      (e = dalloc(p->summary, 1))) {
     s = cuda_fail(p, e, "allocating control block");
     release_all(p);
     delete p;
@@ -385,6 +439,7 @@ gs3d_status gs3d_pipeline_create(const gs3d_pipeline_desc* desc, const gs3d_gaus
   cudaMemset(p->output_state, 0, 4 * sizeof(uint32_t));
   cudaMemset(p->ctl, 0, sizeof(Control));
   cudaMemset(p->epoch_dev, 0, sizeof(uint32_t));
+  cudaMemset(p->summary, 0, sizeof(BatchSummary));
   prepare_sort_kernels();
   if ((s = ensure_slots(p, data->count)) != GS3D_OK || (s = ensure_capacity(p, desc->intersection_capacity)) != GS3D_OK ||
       (s = ensure_stage(p, 16384)) != GS3D_OK) {
@@ -643,8 +698,10 @@ void record_batch(gs3d_pipeline* p, const Plan& pl, unsigned char* dev, cudaStre
   ++launches;
   // Emission + tile-sort histograms.
   mark(p, GS3D_STAGE_EMIT, st);
+  // Fewest passes with digits of at most tuning.tile_digit_bits, then the narrowest digit.
   const uint32_t tile_bits = std::max(1u, ceil_log2((uint64_t)tile + 1));
-  const int tile_passes = (int)((tile_bits + 7) / 8);
+  const uint32_t max_digit = p->tuning.tile_digit_bits;
+  const int tile_passes = (int)((tile_bits + max_digit - 1) / max_digit);
   const int digit_bits = (int)((tile_bits + tile_passes - 1) / tile_passes);
   launch_emit(p->dv[cur], N, p->mean, p->conic, p->ordered, p->ioff, bv, o, ctl, cap32, p->tk[0], p->tv[0],
               tile_passes, digit_bits, st);
@@ -664,11 +721,15 @@ void record_batch(gs3d_pipeline* p, const Plan& pl, unsigned char* dev, cudaStre
   mark(p, GS3D_STAGE_RANGES, st);
   launch_tile_ranges(p->tk[tcur], ctl, tile, p->tile_offsets, p->sms, st);
   ++launches;
-  launch_tile_order(p->tile_offsets, tile, ctl, p->tile_order, p->sms, st);
-  launches += 2;
+  const bool ordered_tiles = p->tuning.work_order != 0u;
+  if (ordered_tiles) {
+    launch_tile_order(p->tile_offsets, tile, ctl, p->tile_order, p->sms, st);
+    launches += 2;
+  }
   // Raster.
   mark(p, GS3D_STAGE_RASTER, st);
-  launch_raster((int)p->desc.raster_precision, p->tile_offsets, p->tile_order, p->tv[tcur], p->mean, p->conic,
+  launch_raster((int)p->desc.raster_precision, p->tile_offsets, ordered_tiles ? p->tile_order : nullptr, p->tv[tcur],
+                p->mean, p->conic,
                 p->color, p->rec, bv, o, ctl, p->desc.raster_stats != 0, st);
   ++launches;
   mark(p, GS3D_STAGE_COUNT, st);
@@ -679,7 +740,7 @@ void record_batch(gs3d_pipeline* p, const Plan& pl, unsigned char* dev, cudaStre
 // The whole pass of TiledGaussianPipeline.render (TiledGaussianPipeline.ts:324-341)
 // for every view of a batch in one launch sequence.
 gs3d_status enqueue(gs3d_pipeline* p, const gs3d_view* views, uint32_t n, uint32_t attempt, int reset_valid,
-                    cudaStream_t st) {
+                    cudaStream_t st, const uint32_t** frame_params = nullptr) {
   Plan pl;
   gs3d_status s = plan_batch(p, views, n, &pl);
   if (s != GS3D_OK) return s;
@@ -693,8 +754,49 @@ gs3d_status enqueue(gs3d_pipeline* p, const gs3d_view* views, uint32_t n, uint32
   cudaEventRecord(p->stage_ev[slot], st);
   p->stage_ev_used[slot] = true;
   p->last_stream = st;
+  if (frame_params) *frame_params = (const uint32_t*)p->stage_dev[slot];
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(p, e, "launching the pass");
+  return GS3D_OK;
+}
+
+uint32_t views_per_launch(const gs3d_pipeline* p, uint32_t n) {
+  const uint32_t v = p->tuning.views_per_launch;
+  return v == 0u || v >= n ? n : v;
+}
+
+// A batch as launch sequences of at most tuning.views_per_launch views, one
+// after another on the stream (they share the workspaces), with the batch's
+// counts and output state summed up on the device.
+gs3d_status enqueue_batch(gs3d_pipeline* p, const gs3d_view* views, uint32_t n, uint32_t attempt, int reset_valid,
+                          cudaStream_t st) {
+  const uint32_t per = views_per_launch(p, n);
+  if (per >= n) {
+    p->last_chunks = 1;
+    return enqueue(p, views, n, attempt, reset_valid, st);
+  }
+  // Grow every workspace for the largest launch first, so no launch
+  // sequence is queued on buffers that a later one reallocates.
+  for (uint32_t k = 0; k < n; k += per) {
+    Plan pl;
+    gs3d_status s = plan_batch(p, views + k, std::min(per, n - k), &pl);
+    if (s != GS3D_OK) return s;
+    if ((s = ensure_stage(p, pl.stage_bytes)) != GS3D_OK) return s;
+  }
+  k_summary_begin<<<1, 1, 0, st>>>(p->summary, p->output_state);
+  uint32_t launches = 1;
+  for (uint32_t k = 0; k < n; k += per) {
+    const uint32_t m = std::min(per, n - k);
+    const uint32_t* params = nullptr;
+    gs3d_status s = enqueue(p, views + k, m, attempt, reset_valid, st, &params);
+    if (s != GS3D_OK) return s;
+    launches += p->last_launches + 1;
+    k_summary_add<<<1, 1, 0, st>>>(p->summary, p->ctl, params, p->output_state, k + m >= n ? 1 : 0);
+  }
+  p->last_chunks = (n + per - 1) / per;
+  p->last_launches = launches;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(p, e, "launching the batch");
   return GS3D_OK;
 }
 
@@ -715,6 +817,7 @@ gs3d_status gs3d_pipeline_render(gs3d_pipeline* p, const gs3d_camera* cam, uint3
   v.width = p->width;
   v.height = p->height;
   v.targets = *targets;
+  p->last_chunks = 1;
   return enqueue(p, &v, 1, attempt, reset_valid, (cudaStream_t)stream);
 }
 
@@ -723,7 +826,7 @@ gs3d_status gs3d_pipeline_render_batch(gs3d_pipeline* p, const gs3d_view* views,
   if (!p || !views) return GS3D_ERROR_INVALID_ARGUMENT;
   cudaSetDevice(p->device);
   p->prepared = true;
-  return enqueue(p, views, count, attempt, reset_valid, (cudaStream_t)stream);
+  return enqueue_batch(p, views, count, attempt, reset_valid, (cudaStream_t)stream);
 }
 
 gs3d_status gs3d_pipeline_capture_graph(gs3d_pipeline* p, const gs3d_view* views, uint32_t count, void* stream) {
@@ -734,12 +837,25 @@ gs3d_status gs3d_pipeline_capture_graph(gs3d_pipeline* p, const gs3d_view* views
   if (!st) return fail(p, GS3D_ERROR_INVALID_ARGUMENT, "graph capture needs a non-default stream");
   if (p->last_stream) cudaStreamSynchronize(p->last_stream);
   release_graphs(p);
-  Plan pl;
-  gs3d_status s = plan_batch(p, views, count, &pl);
-  if (s != GS3D_OK) return s;
+  // One staged batch table per launch sequence, back to back in one buffer;
+  // every workspace is grown for the largest sequence before capturing.
+  const uint32_t per = views_per_launch(p, count);
+  std::vector<Plan> plans;
+  p->graph_chunks.clear();
+  size_t total = 0;
+  for (uint32_t k = 0; k < count; k += per) {
+    Plan pl;
+    gs3d_status s = plan_batch(p, views + k, std::min(per, count - k), &pl);
+    if (s != GS3D_OK) return s;
+    plans.push_back(pl);
+    p->graph_chunks.push_back({k, pl.n, total});
+    total = align16(total + pl.stage_bytes);
+  }
+  const bool chunked = plans.size() > 1;
+  uint32_t launches = chunked ? 1u : 0u;
   for (int g = 0; g < 2; ++g) {
-    cudaError_t e = cudaMallocHost((void**)&p->graph_pinned[g], pl.stage_bytes);
-    if (e == cudaSuccess) e = dalloc(p->graph_dev[g], pl.stage_bytes);
+    cudaError_t e = cudaMallocHost((void**)&p->graph_pinned[g], total);
+    if (e == cudaSuccess) e = dalloc(p->graph_dev[g], total);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->graph_ev[g], cudaEventDisableTiming);
     if (e != cudaSuccess) {
       release_graphs(p);
@@ -751,7 +867,15 @@ gs3d_status gs3d_pipeline_capture_graph(gs3d_pipeline* p, const gs3d_view* views
       release_graphs(p);
       return cuda_fail(p, e, "beginning stream capture");
     }
-    record_batch(p, pl, p->graph_dev[g], st);
+    if (chunked) k_summary_begin<<<1, 1, 0, st>>>(p->summary, p->output_state);
+    for (size_t c = 0; c < plans.size(); ++c) {
+      unsigned char* dev = p->graph_dev[g] + p->graph_chunks[c].offset;
+      record_batch(p, plans[c], dev, st);
+      if (g == 0) launches += p->last_launches + (chunked ? 1u : 0u);
+      if (chunked)
+        k_summary_add<<<1, 1, 0, st>>>(p->summary, p->ctl, (const uint32_t*)dev, p->output_state,
+                                       c + 1 == plans.size() ? 1 : 0);
+    }
     e = cudaStreamEndCapture(st, &graph);
     if (e == cudaSuccess) e = cudaGraphInstantiate(&p->graph_exec[g], graph, 0);
     if (graph) cudaGraphDestroy(graph);
@@ -760,11 +884,11 @@ gs3d_status gs3d_pipeline_capture_graph(gs3d_pipeline* p, const gs3d_view* views
       return cuda_fail(p, e, "capturing the pass");
     }
   }
-  p->graph_stage_bytes = pl.stage_bytes;
+  p->graph_stage_bytes = total;
   p->prepared = true;
   p->graph_views.assign(views, views + count);
   p->graph_cameras.resize(count);
-  p->graph_launches = p->last_launches;
+  p->graph_launches = launches;
   p->graph_next = 0;
   return GS3D_OK;
 }
@@ -784,24 +908,109 @@ gs3d_status gs3d_pipeline_launch_graph(gs3d_pipeline* p, const gs3d_camera* came
   }
   const int g = (int)(p->graph_next++ & 1u);
   if (p->graph_ev_used[g]) cudaEventSynchronize(p->graph_ev[g]);
-  Plan pl;
-  pl.n = count;
-  pl.items = 0;
-  size_t objects = 0;
-  for (uint32_t i = 0; i < count; ++i) objects += cameras[i].object_count;
-  const size_t header = 16 + align16(3 * (size_t)(count + 1) * sizeof(uint32_t));
-  pl.views_off = header;
-  pl.objects_off = align16(header + (size_t)count * sizeof(ViewDesc));
-  pl.stage_bytes = pl.objects_off + objects * 40 * sizeof(float);
-  stage_batch(p, p->graph_views.data(), pl, attempt, reset_valid, p->graph_pinned[g], p->graph_dev[g]);
+  for (const auto& ch : p->graph_chunks) {
+    Plan pl;
+    pl.n = ch.count;
+    size_t objects = 0;
+    for (uint32_t i = 0; i < ch.count; ++i) objects += cameras[ch.first + i].object_count;
+    const size_t header = 16 + align16(3 * (size_t)(ch.count + 1) * sizeof(uint32_t));
+    pl.views_off = header;
+    pl.objects_off = align16(header + (size_t)ch.count * sizeof(ViewDesc));
+    pl.stage_bytes = pl.objects_off + objects * 40 * sizeof(float);
+    stage_batch(p, p->graph_views.data() + ch.first, pl, attempt, reset_valid, p->graph_pinned[g] + ch.offset,
+                p->graph_dev[g] + ch.offset);
+  }
   maybe_reset_epochs(p, st);
-  cudaMemcpyAsync(p->graph_dev[g], p->graph_pinned[g], pl.stage_bytes, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(p->graph_dev[g], p->graph_pinned[g], p->graph_stage_bytes, cudaMemcpyHostToDevice, st);
   cudaError_t e = cudaGraphLaunch(p->graph_exec[g], st);
   cudaEventRecord(p->graph_ev[g], st);
   p->graph_ev_used[g] = true;
   p->last_stream = st;
   p->last_launches = p->graph_launches;
+  p->last_chunks = (uint32_t)p->graph_chunks.size();
   if (e != cudaSuccess) return cuda_fail(p, e, "launching the graph");
+  return GS3D_OK;
+}
+
+gs3d_status gs3d_pipeline_set_tuning(gs3d_pipeline* p, const gs3d_tuning* t) {
+  if (!p || !t) return GS3D_ERROR_INVALID_ARGUMENT;
+  if (t->tile_digit_bits < 4 || t->tile_digit_bits > 8)
+    return fail(p, GS3D_ERROR_RANGE, "tile_digit_bits must be in [4, 8]");
+  if (t->work_order > 1) return fail(p, GS3D_ERROR_INVALID_ARGUMENT, "work_order must be 0 or 1");
+  if (p->last_stream) cudaStreamSynchronize(p->last_stream);
+  release_graphs(p);  // captured graphs follow the tuning they were captured with
+  p->tuning = *t;
+  p->tuning.reserved = 0;
+  return GS3D_OK;
+}
+
+gs3d_status gs3d_pipeline_get_tuning(gs3d_pipeline* p, gs3d_tuning* t) {
+  if (!p || !t) return GS3D_ERROR_INVALID_ARGUMENT;
+  *t = p->tuning;
+  return GS3D_OK;
+}
+
+gs3d_status gs3d_pipeline_autotune(gs3d_pipeline* p, const gs3d_view* views, uint32_t count, uint32_t trials,
+                                   gs3d_tuning* best, double* best_ms, void* stream) {
+  if (!p || !views || count == 0) return GS3D_ERROR_INVALID_ARGUMENT;
+  if (trials == 0) trials = 3;
+  cudaSetDevice(p->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (p->last_stream) cudaStreamSynchronize(p->last_stream);
+  release_graphs(p);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  // Milliseconds per batch with tuning t (one untimed render first, which
+  // also grows the workspaces); an overflowing batch is an error.
+  auto measure = [&](const gs3d_tuning& t, double* ms) -> gs3d_status {
+    p->tuning = t;
+    gs3d_status s = enqueue_batch(p, views, count, 1, 0, st);
+    if (s != GS3D_OK) return s;
+    gs3d_stats stats;
+    if ((s = gs3d_pipeline_read_stats(p, &stats)) != GS3D_OK) return s;
+    if (stats.overflow) return fail(p, GS3D_ERROR_RANGE, "intersection capacity too small for the batch");
+    cudaEventRecord(e0, st);
+    for (uint32_t i = 0; i < trials; ++i)
+      if ((s = enqueue_batch(p, views, count, 1, 0, st)) != GS3D_OK) return s;
+    cudaEventRecord(e1, st);
+    cudaEventSynchronize(e1);
+    float f = 0.0f;
+    cudaEventElapsedTime(&f, e0, e1);
+    *ms = (double)f / trials;
+    return GS3D_OK;
+  };
+  gs3d_tuning cur{0u, 8u, 1u, 0u};
+  double cur_ms = 0.0;
+  gs3d_status s = measure(cur, &cur_ms);
+  // Coordinate descent: views per launch (halving), widest tile-sort digit,
+  // then the raster work order.
+  for (uint32_t v = count / 2; s == GS3D_OK && v >= 1; v /= 2) {
+    gs3d_tuning t = cur;
+    t.views_per_launch = v;
+    double ms = 0.0;
+    if ((s = measure(t, &ms)) == GS3D_OK && ms < cur_ms) { cur = t; cur_ms = ms; }
+    if (v == 1) break;
+  }
+  const gs3d_tuning by_views = cur;
+  for (uint32_t d = 7; s == GS3D_OK && d >= 4; --d) {
+    gs3d_tuning t = by_views;
+    t.tile_digit_bits = d;
+    double ms = 0.0;
+    if ((s = measure(t, &ms)) == GS3D_OK && ms < cur_ms) { cur = t; cur_ms = ms; }
+  }
+  if (s == GS3D_OK) {
+    gs3d_tuning t = cur;
+    t.work_order = 0u;
+    double ms = 0.0;
+    if ((s = measure(t, &ms)) == GS3D_OK && ms < cur_ms) { cur = t; cur_ms = ms; }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  p->tuning = cur;
+  if (s != GS3D_OK) return s;
+  if (best) *best = cur;
+  if (best_ms) *best_ms = cur_ms;
   return GS3D_OK;
 }
 
@@ -825,6 +1034,18 @@ gs3d_status gs3d_pipeline_read_stats(gs3d_pipeline* p, gs3d_stats* out) {
   Control c;
   e = cudaMemcpy(&c, p->ctl, sizeof(Control), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return cuda_fail(p, e, "reading the pass state");
+  if (p->last_chunks > 1) {
+    // A batch of several launch sequences: the totals of all of them.
+    BatchSummary b;
+    e = cudaMemcpy(&b, p->summary, sizeof(b), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(p, e, "reading the batch summary");
+    c.visible_state[0] = b.visible;
+    c.state[0] = b.intersections;
+    c.state[1] = b.requested;
+    c.state[3] = b.overflow;
+    c.error = b.error;
+    for (int i = 0; i < 4; ++i) c.raster_stats[i] = b.raster[i];
+  }
   memset(out, 0, sizeof(*out));
   out->visible_gaussian_count = c.visible_state[0];
   out->intersection_count = c.state[0];

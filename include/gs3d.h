@@ -223,8 +223,38 @@ typedef struct gs3d_view {
   gs3d_targets targets;
 } gs3d_view;
 
+/* Launch-shape tuning (no counterpart in the reference, whose dispatch shape
+ * is fixed; outputs do not depend on it). views_per_launch: a batch of more
+ * views runs as consecutive launch sequences of at most that many views on the
+ * same stream (0 = the whole batch at once); read_stats then reports their
+ * totals (visible and intersection counts summed, requested = the largest
+ * sequence's demand, overflow if any sequence overflowed), the output state
+ * covers the whole batch, and get_resources and batch_layout describe the
+ * last sequence. tile_digit_bits: the widest digit of the tile sort, 4..8.
+ * work_order: 1 = rasterize tiles heaviest first, 0 = in tile order.
+ * Setting a tuning releases captured graphs. */
+typedef struct gs3d_tuning {
+  uint32_t views_per_launch; /* default 0 */
+  uint32_t tile_digit_bits;  /* default 8 */
+  uint32_t work_order;       /* default 1 */
+  uint32_t reserved;
+} gs3d_tuning;
+
+gs3d_status gs3d_pipeline_set_tuning(gs3d_pipeline* pipeline, const gs3d_tuning* tuning);
+gs3d_status gs3d_pipeline_get_tuning(gs3d_pipeline* pipeline, gs3d_tuning* tuning);
+
+/* Times the batch under candidate tunings (coordinate descent: views per
+ * launch halving from the batch size, tile digit width 7..4, then the work
+ * order; `trials` timed batches each after one untimed one), keeps the
+ * fastest and returns it with its milliseconds per batch. The views' targets
+ * receive the renders. GS3D_ERROR_RANGE if the intersection capacity cannot
+ * hold the batch. */
+gs3d_status gs3d_pipeline_autotune(gs3d_pipeline* pipeline, const gs3d_view* views, uint32_t count, uint32_t trials,
+                                   gs3d_tuning* best, double* best_ms, void* stream);
+
 /* Batched rendering (an extension; the reference renders one camera per
- * pass): every view runs through one launch sequence. Views are
+ * pass): the views run through one launch sequence (or several, see
+ * gs3d_tuning.views_per_launch). Views are
  * concatenated: view v owns items [item_base[v], item_base[v] + active) and
  * global tile ids [tile_base[v], tile_base[v+1]); each view's tiles hold
  * exactly the records, order and image a single-view render of that view
