@@ -44,6 +44,7 @@ def parse():
     ap.add_argument("--plain-precision", default="fp32", choices=["fp32", "exact"])
     ap.add_argument("--latency-frames", type=int, default=240)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shape for the batched form")
     ap.add_argument("--forms", default="all", choices=["all", "batched"],
                     help="'batched' skips the timed plain (one view per launch) form")
     ap.add_argument("--serve", action="store_true", help="serving-loop measurement (configuration 4)")
@@ -65,17 +66,18 @@ def peaks():
 TRAFFIC_FILE = os.path.join(ROOT, "profiles", "dram_traffic_config2_3M_1080p.md")
 
 
-def measured_traffic(stage: str, args) -> int | None:
-    """DRAM bytes (read + write) of one launch of `stage`'s kernel, from the
-    committed ncu summary, when that capture was taken on this workload."""
+def measured_traffic(stage: str, args, views_per_launch: int) -> int | None:
+    """DRAM bytes (read + write) of `stage`'s kernel per batch of the step,
+    from the committed ncu summary, when that capture was taken on this
+    workload and launch shape."""
     try:
         with open(TRAFFIC_FILE) as f:
             for line in f:
                 parts = line.split()
-                if len(parts) == 8 and parts[0] == "traffic" and parts[1] == stage:
-                    cfg = (int(parts[2]), int(parts[3]), int(parts[4]), int(parts[5]), parts[6])
-                    if cfg == (args.splats, args.width, args.height, args.cameras, args.precision):
-                        return int(parts[7])
+                if len(parts) == 9 and parts[0] == "traffic" and parts[1] == stage:
+                    cfg = (int(parts[2]), int(parts[3]), int(parts[4]), int(parts[5]), parts[6], int(parts[7]))
+                    if cfg == (args.splats, args.width, args.height, args.cameras, args.precision, views_per_launch):
+                        return int(parts[8])
     except (OSError, ValueError):
         pass
     return None
@@ -336,6 +338,12 @@ def main() -> None:
                                                   "intersection_capacity": int(demand * 1.25 * ncam) + 256})
     views = [(data, cam, W, H, colors[i].data_ptr(), 0, "rgba16f") for i, cam in enumerate(cams)]
     gstream = torch.cuda.Stream()
+    # Launch shape from the autotuner (outputs do not depend on it), before
+    # the untimed sizing render and the graph capture.
+    tune_ms = None
+    if not args.no_autotune:
+        _, tune_ms = batched.autotune(views, trials=3)
+    tuning = batched.get_tuning()
     batched.render_batch(views)  # size the workspaces, then capture the pass as a graph
     torch.cuda.synchronize()
     batched.capture_graph(views, gstream.cuda_stream)
@@ -350,6 +358,9 @@ def main() -> None:
         return batched.last_launch_count()
 
     ms_total, stage_ms, profiled, launches, clock_info = timed(step_batched, batched)
+    # Stage times are means per launch sequence; a batch may run as several.
+    seq_per_batch = profiled / args.steps if profiled else 1.0
+    stage_ms = {k: v * seq_per_batch for k, v in stage_ms.items()}
     # Same batches replayed from the captured graph (no per-stage events).
     for _ in range(3):
         step_graph()
@@ -427,7 +438,7 @@ def main() -> None:
         gbs = b / (ms * 1e-3) / 1e9 if ms > 0 else 0.0
         stages[name] = {"ms": ms, "bytes": b, "GB/s": gbs, "frac": gbs / hbm}
     dom = max(stages, key=lambda k: stages[k]["ms"])
-    traffic = measured_traffic(dom, args)
+    traffic = measured_traffic(dom, args, int(tuning["views_per_launch"]))
     roofline = {"kernel": dom, "bound": "hbm", "achieved": stages[dom]["GB/s"], "peak": hbm, "unit": "GB/s",
                 "frac": stages[dom]["frac"], "traffic": traffic, "peak_source": peak_kind}
 
@@ -461,10 +472,12 @@ def main() -> None:
                                f"{args.precision} raster",
                    "splats": args.splats, "width": W, "height": H, "cameras": len(cams),
                    "frames_per_step": len(cams), "parallelism": f"replicas x{world}",
+                   "launch_shape": tuning,
                    "l2": "inputs larger than L2 (288 MB packed scene read every frame)",
                    "visible_mean": v, "intersections_mean": inter},
         "p50_ms": p50, "p99_ms": p99, "psnr_db_vs_fp64": psnr_db,
         "forms": {"batched": {"precision": args.precision, "frames_per_s": fps, "views_per_batch": ncam,
+                              "tuning": tuning, "autotune_ms_per_batch": tune_ms,
                               "graph_replay_frames_per_s": fps_graph,
                               "p50_batch_ms": p50, "p99_batch_ms": p99, "psnr_db": psnr_db,
                               "stats": bstats},
