@@ -18,7 +18,8 @@ import os
 import threading
 
 from . import abi
-from .abi import (GS3D_OK, Camera, GaussianData, PipelineDesc, Resources, Stats, Targets, Tuning, View)
+from .abi import (GS3D_OK, Camera, GaussianData, PipelineDesc, Resources, SplatSource, Stats, Targets, Tuning,
+                  View)
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "_build", "libgs3d.so")
@@ -299,3 +300,23 @@ class TiledGaussianPipeline:
             self.dispose()
         except Exception:
             pass
+
+
+def pack_splats(centers, scales, opacity, quaternions, rgb, sh_rest, first_slot: int, means, scales_opacity,
+                rotations, sh_coefficients, capacity: int, object_id: int = 0, stream: int = 0) -> None:
+    """Encode linear splat attributes into slots [first_slot, first_slot + n)
+    of a store's packed device buffers on the GPU (the compact layout of the
+    reference's Rust packer, engine.rs:1801-1891). Arguments are CUDA tensors:
+    centers/scales (n, 3), opacity (n,), quaternions (n, 4) xyzw, rgb (n, 3),
+    sh_rest (n, C-1, 3) or None; outputs as in ``scenes.pack_scene``."""
+    lib = load()
+    n = int(centers.shape[0])
+    degree = 0 if sh_rest is None else int(round((int(sh_rest.shape[1]) + 1) ** 0.5)) - 1
+    src = SplatSource()
+    src.centers, src.scales, src.opacity = centers.data_ptr(), scales.data_ptr(), opacity.data_ptr()
+    src.quaternions, src.rgb = quaternions.data_ptr(), rgb.data_ptr()
+    src.sh_rest = sh_rest.data_ptr() if sh_rest is not None else None
+    src.count, src.sh_degree, src.object_id = n, degree, int(object_id)
+    _raise(lib, lib.gs3d_pack_splats(C.byref(src), int(first_slot), means.data_ptr(), scales_opacity.data_ptr(),
+                                     rotations.data_ptr(), sh_coefficients.data_ptr(), int(capacity),
+                                     C.c_void_p(int(stream))))

@@ -57,6 +57,11 @@ class Tuning(C.Structure):
                 ("reserved", C.c_uint32)]
 
 
+class SplatSource(C.Structure):
+    _fields_ = [(name, C.c_void_p) for name in ("centers", "scales", "opacity", "quaternions", "rgb", "sh_rest")] + \
+               [("count", C.c_uint32), ("sh_degree", C.c_uint32), ("object_id", C.c_uint32), ("reserved", C.c_uint32)]
+
+
 class Stats(C.Structure):
     _fields_ = [("visible_gaussian_count", C.c_uint32), ("intersection_count", C.c_uint32),
                 ("requested_intersections", C.c_uint32), ("overflow", C.c_uint32),
@@ -103,6 +108,7 @@ SIGNATURES = {
     "gs3d_pipeline_stage_times": (C.c_int, [_P, C.POINTER(C.c_float), C.POINTER(C.c_uint32)]),
     "gs3d_stage_name": (C.c_char_p, [C.c_uint32]),
     "gs3d_compact_visible_static": (C.c_int, [_P, C.c_uint32, _P, _P, _P, _P, _P]),
+    "gs3d_pack_splats": (C.c_int, [C.POINTER(SplatSource), C.c_uint32, _P, _P, _P, _P, C.c_uint32, _P]),
     "gs3d_capacity_next": (C.c_uint64, [C.c_uint64, C.c_double, C.c_double, C.c_uint64, C.c_uint64]),
 }
 

@@ -1,8 +1,9 @@
 """Builds libgs3d.so (the C-ABI CUDA library) in-tree with nvcc for sm_103a.
 
 Translation units compile in parallel. ``pass_exact.cu`` holds every stage
-whose integer results must be bit-identical to the CPU restatement and is
-compiled with ``--fmad=false``; the other units use the default contraction.
+whose integer results must be bit-identical to the CPU restatement and
+``packer.cu`` restates the Rust packer's arithmetic; both are compiled with
+``--fmad=false``; the other units use the default contraction.
 """
 from __future__ import annotations
 
@@ -26,6 +27,7 @@ UNITS = {
     "raster.cu": [],
     "pipeline.cu": [],
     "static_scratch.cu": [],
+    "packer.cu": ["--fmad=false"],
 }
 
 

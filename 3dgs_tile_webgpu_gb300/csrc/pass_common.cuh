@@ -74,11 +74,13 @@ __device__ __forceinline__ uint32_t find_view(const uint32_t* base, uint32_t nvi
   return lo;
 }
 
+constexpr uint32_t kMaxSortPasses = 4;  // digit histograms held per sort
+
 // Per-frame control block, zeroed before each render.
 struct Control {
   uint32_t tickets[16];          // dynamic tile ids of the look-back kernels
-  uint32_t depth_hist[4][256];   // digit histograms of the depth sort
-  uint32_t tile_hist[4][256];    // digit histograms of the tile sort
+  uint32_t depth_hist[kMaxSortPasses][256];  // digit histograms of the depth sort
+  uint32_t tile_hist[kMaxSortPasses][256];   // digit histograms of the tile sort
   uint32_t visible_state[4];     // visible, visible, radix blocks, 0
   uint32_t state[4];             // count, total, radix blocks, overflow
   uint32_t error;                // bit 0: look-back wait expired

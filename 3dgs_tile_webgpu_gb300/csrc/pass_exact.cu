@@ -261,10 +261,10 @@ __global__ void __launch_bounds__(kBlock) k_compact(const uint32_t* __restrict__
   const uint32_t epoch = ep.get();
   __shared__ uint32_t s_tile, s_prefix;
   __shared__ uint32_t s_warp[kBlock / 32];
-  __shared__ uint32_t s_hist[4][256];
+  __shared__ uint32_t s_hist[kMaxSortPasses][256];
   const uint32_t tid = threadIdx.x;
   if (tid == 0) s_tile = atomicAdd(&ctl->tickets[kTicketCompact], 1u);
-  for (uint32_t i = tid; i < 4 * 256; i += kBlock) (&s_hist[0][0])[i] = 0u;
+  for (uint32_t i = tid; i < kMaxSortPasses * 256; i += kBlock) (&s_hist[0][0])[i] = 0u;
   __syncthreads();
   const uint32_t tile = s_tile;
   const uint32_t ntiles = n == 0 ? 1u : (n + kScanTile - 1) / kScanTile;
@@ -441,7 +441,7 @@ struct EmitShared {
   uint32_t u[8][kEmitWarps][32];   // tminx, tminy, box width, tiles_x, tile_base, base, reserved, item
   uint32_t incl[kEmitWarps][32];   // inclusive box-tile counts
   uint32_t filled[kEmitWarps][32]; // records placed so far per rank
-  uint32_t hist[4][256];
+  uint32_t hist[kMaxSortPasses][256];
 };
 
 __global__ void __launch_bounds__(kBlock) k_emit(const uint32_t* __restrict__ ids, const float4* __restrict__ mean,
@@ -456,7 +456,7 @@ __global__ void __launch_bounds__(kBlock) k_emit(const uint32_t* __restrict__ id
   const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
   const uint32_t n = ctl->visible_state[0];
   if (blockIdx.x * kBlock >= n) return;  // whole block past the visible count
-  for (uint32_t i = tid; i < 4 * 256; i += kBlock) (&sm.hist[0][0])[i] = 0u;
+  for (uint32_t i = tid; i < kMaxSortPasses * 256; i += kBlock) (&sm.hist[0][0])[i] = 0u;
   const uint32_t r = blockIdx.x * kBlock + tid;
   const uint32_t mask = (1u << digit_bits) - 1u;
   const uint32_t sentinel = bv.total_tiles;

@@ -698,10 +698,12 @@ void record_batch(gs3d_pipeline* p, const Plan& pl, unsigned char* dev, cudaStre
   ++launches;
   // Emission + tile-sort histograms.
   mark(p, GS3D_STAGE_EMIT, st);
-  // Fewest passes with digits of at most tuning.tile_digit_bits, then the narrowest digit.
+  // Fewest passes with digits of at most tuning.tile_digit_bits, then the
+  // narrowest digit; never more than the 4 passes the digit histograms hold
+  // (the digit then widens past the tuning, up to 8 bits for 32-bit ids).
   const uint32_t tile_bits = std::max(1u, ceil_log2((uint64_t)tile + 1));
   const uint32_t max_digit = p->tuning.tile_digit_bits;
-  const int tile_passes = (int)((tile_bits + max_digit - 1) / max_digit);
+  const int tile_passes = (int)std::min<uint32_t>(kMaxSortPasses, (tile_bits + max_digit - 1) / max_digit);
   const int digit_bits = (int)((tile_bits + tile_passes - 1) / tile_passes);
   launch_emit(p->dv[cur], N, p->mean, p->conic, p->ordered, p->ioff, bv, o, ctl, cap32, p->tk[0], p->tv[0],
               tile_passes, digit_bits, st);

@@ -280,3 +280,53 @@ def config2_scene(n: int = 3_000_000) -> dict:
 def config2_frames(count: int = 16, width: int = 1920, height: int = 1080, **options) -> list:
     return [make_frame(c, width, height, 60.0, 0.1, 1000.0, **options)
             for c in orbit_cameras(count, 30.0, seed=1002)]
+
+
+CONFIG3_SIZES = (50_000, 100_000, 250_000, 500_000, 750_000, 1_000_000, 1_500_000, 2_000_000)
+CONFIG3_RESOLUTIONS = ((640, 480), (1280, 720), (1920, 1080), (3840, 2160))
+
+
+def _rotation(rng) -> np.ndarray:
+    q = rng.standard_normal(4)
+    q /= np.linalg.norm(q)
+    x, y, z, w = q
+    return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                     [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                     [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
+
+
+def config3_scene(sizes=CONFIG3_SIZES, seed: int = 1003) -> tuple[dict, list]:
+    """Benchmark configuration 3: one store holding the clouds as objects
+    0..k-1 (configuration 1 distributions), and each object's world matrix: a
+    seeded rigid transform with uniform scale U(0.5, 2), the clouds spread on
+    a ring of radius 20."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    parts = [uniform_cloud(n, seed=seed * 10 + i, object_id=i) for i, n in enumerate(sizes)]
+    worlds = []
+    for i in range(len(sizes)):
+        m = np.eye(4)
+        m[:3, :3] = _rotation(rng) * rng.uniform(0.5, 2.0)
+        ang = 2 * math.pi * i / len(sizes)
+        m[:3, 3] = (20.0 * math.cos(ang), rng.uniform(-3.0, 3.0), 20.0 * math.sin(ang))
+        worlds.append(m)
+    count = sum(p["count"] for p in parts)
+    C = sh_coefficient_count(parts[0]["sh_degree"])
+    sh = np.zeros(count * C + count, np.uint32)
+    sh[: count * C] = np.concatenate([p["sh"][: p["count"] * C] for p in parts])
+    sh[count * C:] = np.arange(count, dtype=np.uint32)
+    scene = {"count": count, "active_count": count, "sh_degree": parts[0]["sh_degree"],
+             "means": np.concatenate([p["means"] for p in parts]),
+             "shape": np.concatenate([p["shape"] for p in parts]),
+             "rotations": np.concatenate([p["rotations"] for p in parts]), "sh": sh}
+    return scene, worlds
+
+
+def config3_frames(worlds, count: int = 32, seed: int = 1003) -> list:
+    """32 orbit cameras (radius 45 around the ring) with resolutions drawn
+    from 640x480, 1280x720, 1920x1080 and 3840x2160."""
+    rng = np.random.Generator(np.random.PCG64(seed + 1))
+    frames = []
+    for cam_world in orbit_cameras(count, 45.0, seed=seed):
+        w, h = CONFIG3_RESOLUTIONS[int(rng.integers(0, len(CONFIG3_RESOLUTIONS)))]
+        frames.append(make_frame(cam_world, w, h, 60.0, 0.1, 1000.0, object_worlds=worlds))
+    return frames

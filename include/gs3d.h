@@ -308,6 +308,34 @@ gs3d_status gs3d_pipeline_set_profiling(gs3d_pipeline* pipeline, int enabled);
 gs3d_status gs3d_pipeline_stage_times(gs3d_pipeline* pipeline, float* ms, uint32_t* renders);
 const char* gs3d_stage_name(uint32_t stage);
 
+/* On-device compact packer (the reference packs on the CPU:
+ * rust/gaussian-backend/src/engine.rs:1801-1891 encode_attributes with the
+ * compact layout, spark-lib splat_encode.rs:127-136,234-252, pack_sh
+ * engine.rs:1940-1949). Writes slots [first_slot, first_slot + count) of a
+ * store's packed buffers (device pointers; `capacity` = the store's slot
+ * count): means (x, y, z, object_id), compact scalesOpacity (f16 ln-scales,
+ * f16 opacity), oct101012 rotations, rgb8e8 SH (slot * C words; the DC word
+ * from (rgb - 0.5) / SH_C0). The active-slot tail is left to the caller.
+ * Inputs are device arrays: centers and scales (linear) count x 3, opacity
+ * count, quaternions count x 4 (xyzw, normalised here), rgb count x 3,
+ * sh_rest count x (C - 1) x 3 (null at degree 0). Asynchronous on `stream`. */
+typedef struct gs3d_splat_source {
+  const float* centers;
+  const float* scales;
+  const float* opacity;
+  const float* quaternions;
+  const float* rgb;
+  const float* sh_rest;
+  uint32_t count;
+  uint32_t sh_degree;
+  uint32_t object_id;
+  uint32_t reserved;
+} gs3d_splat_source;
+
+gs3d_status gs3d_pack_splats(const gs3d_splat_source* source, uint32_t first_slot, float* means,
+                             uint32_t* scales_opacity, uint32_t* rotations, uint32_t* sh_coefficients,
+                             uint32_t capacity, void* stream);
+
 /* Visibility compaction with no device allocation. This entry point has no
  * counterpart in the reference. It serves callers that cannot call cudaMalloc
  * where they enqueue work: code running during CUDA graph capture, hosts that

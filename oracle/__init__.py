@@ -102,6 +102,11 @@ def lib():
             L.gso_pack_sh.argtypes = [_FP]
             L.gso_encode_oct101012.restype = _U
             L.gso_encode_oct101012.argtypes = [_FP]
+            L.gso_f16_bits.restype = _U
+            L.gso_f16_bits.argtypes = [_F]
+            L.gso_pack_splat.restype = None
+            L.gso_pack_splat.argtypes = [_FP, _FP, _F, _FP, _FP, _FP, _U, _U, _FP, C.POINTER(C.c_uint32),
+                                         C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
             L.gso_view_covariance.argtypes = [_FP, _FP, _FP, _FP]
             L.gso_projection_result.argtypes = [_FP, _F, _FP, _F, _FP]
             L.gso_perspective_projection.argtypes = [_FP, _FP, _FP, _FP, _F, _FP]
@@ -262,3 +267,30 @@ def _estimate_records(L, sc, fr, n) -> int:
     out.sorted_records = _ptr(keep["sr"])
     L.gso_render(C.byref(sc), C.byref(probe), C.byref(out), 0)
     return int(out.state[1])
+
+
+def pack_splats(centers, scales, opacity, quats, rgb, sh_rest, object_id: int = 0) -> dict:
+    """The compact packed buffers of linear splat attributes, one splat at a
+    time through the C restatement of the reference's CPU packer (libm, like
+    the Rust backend): checks the on-device packer."""
+    L = lib()
+    n = int(np.asarray(centers).shape[0])
+    C_ = 1 + (0 if sh_rest is None else int(np.asarray(sh_rest).shape[1]))
+    centers = np.ascontiguousarray(centers, np.float32)
+    scales = np.ascontiguousarray(scales, np.float32)
+    opacity = np.ascontiguousarray(opacity, np.float32)
+    quats = np.ascontiguousarray(quats, np.float32)
+    rgb = np.ascontiguousarray(rgb, np.float32)
+    rest = np.ascontiguousarray(sh_rest if sh_rest is not None else np.zeros((n, 0, 3)), np.float32)
+    means = np.zeros((n, 4), np.float32)
+    shape = np.zeros((n, 2), np.uint32)
+    rot = np.zeros(n, np.uint32)
+    sh = np.zeros((n, C_), np.uint32)
+    fp = C.POINTER(C.c_float)
+    up = C.POINTER(C.c_uint32)
+    for i in range(n):
+        L.gso_pack_splat(centers[i].ctypes.data_as(fp), scales[i].ctypes.data_as(fp), float(opacity[i]),
+                         quats[i].ctypes.data_as(fp), rgb[i].ctypes.data_as(fp), rest[i].ctypes.data_as(fp), C_,
+                         int(object_id), means[i].ctypes.data_as(fp), shape[i].ctypes.data_as(up),
+                         rot[i:i + 1].ctypes.data_as(up), sh[i].ctypes.data_as(up))
+    return {"means": means, "shape": shape, "rotations": rot, "sh": sh}

@@ -560,6 +560,15 @@ void gso_decode_sh(uint32_t packed, float* out3) {
   out3[0] = v.x; out3[1] = v.y; out3[2] = v.z;
 }
 
+uint32_t gso_f16_bits(float x);
+
+// engine.rs:1801-1891 encode_attributes (compact layout) for one splat: the
+// packed means, scalesOpacity, rotation and C rgb8e8 SH words, on the CPU with
+// libm like the Rust backend (checks the on-device packer).
+void gso_pack_splat(const float* center, const float* scale, float opacity, const float* quat, const float* rgb,
+                    const float* sh_rest, uint32_t C, uint32_t object_id, float* means4, uint32_t* shape2,
+                    uint32_t* rot, uint32_t* sh);
+
 // rust/gaussian-backend/src/engine.rs:1940-1949 pack_sh.
 uint32_t gso_pack_sh(const float* rgb) {
   float mx = 0.0f;
@@ -576,6 +585,28 @@ uint32_t gso_pack_sh(const float* rgb) {
     b[i] = (uint32_t)(int32_t)q & 255u;
   }
   return b[0] | (b[1] << 8) | (b[2] << 16) | ((uint32_t)(exponent + 127) << 24);
+}
+
+// IEEE binary16 bits of a float, round to nearest even (half::f16::from_f32).
+static uint32_t f16_bits_rne(float x) {
+  uint32_t b;
+  memcpy(&b, &x, 4);
+  const uint32_t sign = (b >> 16) & 0x8000u;
+  const uint32_t ab = b & 0x7fffffffu;
+  if (ab >= 0x7f800000u) return sign | (ab > 0x7f800000u ? 0x7e00u : 0x7c00u);  // NaN / inf
+  if (ab >= 0x477ff000u) return sign | 0x7c00u;                                   // rounds past 65504
+  if (ab < 0x33000001u) return sign;                                              // below half the smallest subnormal
+  const int e = (int)(ab >> 23) - 127;
+  uint32_t mant = (ab & 0x7fffffu) | 0x800000u;
+  if (e < -14) {  // subnormal half
+    const int shift = -e - 14 + 13;
+    const uint32_t q = mant >> shift, rem = mant & ((1u << shift) - 1u), halfway = 1u << (shift - 1);
+    return sign | (q + (rem > halfway || (rem == halfway && (q & 1u))));
+  }
+  const uint32_t q = mant >> 13, rem = mant & 0x1fffu;
+  uint32_t h = ((uint32_t)(e + 15) << 10) | (q & 0x3ffu);
+  if (rem > 0x1000u || (rem == 0x1000u && (q & 1u))) ++h;  // carries into the exponent correctly
+  return sign | h;
 }
 
 // rust/vendor/spark-lib/src/splat_encode.rs:234-252 encode_quat_oct101012.
@@ -607,6 +638,23 @@ uint32_t gso_encode_oct101012(const float* q_in) {
   float r = theta / 3.14159265358979323846f * 4095.0f;
   r = r < 0.0f ? 0.0f : (r > 4095.0f ? 4095.0f : r);
   return ((uint32_t)roundf(r) << 20) | (uv[1] << 10) | uv[0];
+}
+
+uint32_t gso_f16_bits(float x) { return f16_bits_rne(x); }
+
+void gso_pack_splat(const float* center, const float* scale, float opacity, const float* quat, const float* rgb,
+                    const float* sh_rest, uint32_t C, uint32_t object_id, float* means4, uint32_t* shape2,
+                    uint32_t* rot, uint32_t* sh) {
+  means4[0] = center[0]; means4[1] = center[1]; means4[2] = center[2]; means4[3] = (float)object_id;
+  shape2[0] = f16_bits_rne(logf(scale[0])) | (f16_bits_rne(logf(scale[1])) << 16);
+  shape2[1] = f16_bits_rne(logf(scale[2])) | (f16_bits_rne(opacity) << 16);
+  const float inv = 1.0f / sqrtf(((quat[0] * quat[0] + quat[1] * quat[1]) + quat[2] * quat[2]) + quat[3] * quat[3]);
+  const float q[4] = {quat[0] * inv, quat[1] * inv, quat[2] * inv, quat[3] * inv};
+  *rot = gso_encode_oct101012(q);
+  const float k = 0.28209479177387814f;
+  const float dc[3] = {(rgb[0] - 0.5f) / k, (rgb[1] - 0.5f) / k, (rgb[2] - 0.5f) / k};
+  sh[0] = gso_pack_sh(dc);
+  for (uint32_t c = 1; c < C; ++c) sh[c] = gso_pack_sh(sh_rest + 3 * (size_t)(c - 1));
 }
 
 void gso_view_covariance(const float* scale, const float* rot, const float* mv16, float* out9) {

@@ -84,6 +84,20 @@ def test_tile_digit_width_and_work_order_change_nothing(digits, order):
     b.close()
 
 
+def test_narrow_tile_digits_on_many_tiles_stay_within_four_passes():
+    # Over 2^16 tiles (19-bit tile ids): 4-bit digits would need 5 passes; the
+    # sort caps the passes at the 4 its histograms hold and widens the digit.
+    clouds = [sc.uniform_cloud(3000, seed=74, log_scale=(-2.0, 0.5))]
+    frames = [cam(w=4096, h=4096), cam(eye=(2, 1, 10), w=4096, h=4096), cam(eye=(-2, 1, 9), w=4096, h=2048)]
+    pairs = [(clouds[0], f) for f in frames]
+    b = Batch(pairs)
+    ref, st = b.render({"tile_digit_bits": 8})
+    imgs, s = b.render({"tile_digit_bits": 4})
+    assert same_images(imgs, ref)
+    assert s["intersectionCount"] == st["intersectionCount"] and s["deviceError"] == 0
+    b.close()
+
+
 def test_chunked_batch_overflow_is_reported_for_the_batch():
     pairs = batch()
     b = Batch(pairs, capacity=1 << 22)
