@@ -18,8 +18,8 @@ import os
 import threading
 
 from . import abi
-from .abi import (GS3D_OK, Camera, GaussianData, PipelineDesc, Resources, SplatSource, Stats, Targets, Tuning,
-                  View)
+from .abi import (GS3D_OK, Camera, GaussianData, PipelineDesc, ProfileStats, Resources, SplatSource, Stats,
+                  Targets, Tuning, View)
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "_build", "libgs3d.so")
@@ -271,6 +271,29 @@ class TiledGaussianPipeline:
                               "pixels": int(s.raster_pixels), "alphaStopped": int(s.raster_alpha_stopped)}}
         _raise(self._lib, st, self._p)
         return out
+
+    def read_profile(self) -> dict:
+        """GaussianPassProfileStats of the last render (types.ts:105-148):
+        tileLoads, appliedTileCap (None without maxRasterizedSplatsPerTile),
+        tileCapEstimates at 2048/4096/8192, zeroPixelSubpixelSplats."""
+        s = ProfileStats()
+        _raise(self._lib, self._lib.gs3d_pipeline_read_profile(self._p, C.byref(s)), self._p)
+        L = s.tile_loads
+
+        def cap(c):
+            return {"cap": c.cap, "rasterizedIntersections": c.rasterized_intersections,
+                    "droppedIntersections": c.dropped_intersections, "droppedFraction": c.dropped_fraction,
+                    "affectedTiles": c.affected_tiles, "totalBatches": c.total_batches, "maxBatches": c.max_batches}
+
+        return {
+            "tileLoads": {"max": L.max, "mean": L.mean, "median": L.median, "p95": L.p95, "p99": L.p99,
+                          "tilesOver256": L.tiles_over_256, "tilesOver512": L.tiles_over_512,
+                          "tilesOver1024": L.tiles_over_1024, "tilesOver2048": L.tiles_over_2048,
+                          "totalBatches": L.total_batches, "maxBatches": L.max_batches},
+            "appliedTileCap": cap(s.applied_cap) if s.has_applied_cap else None,
+            "tileCapEstimates": [cap(c) for c in s.cap_estimates],
+            "zeroPixelSubpixelSplats": s.zero_pixel_subpixel_splats,
+        }
 
     def get_resources(self) -> Resources:
         r = Resources()

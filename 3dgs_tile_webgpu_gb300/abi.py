@@ -62,6 +62,23 @@ class SplatSource(C.Structure):
                [("count", C.c_uint32), ("sh_degree", C.c_uint32), ("object_id", C.c_uint32), ("reserved", C.c_uint32)]
 
 
+class TileLoadStats(C.Structure):
+    _fields_ = [(name, C.c_uint32) for name in ("max", "p95", "p99", "tiles_over_256", "tiles_over_512",
+                                                 "tiles_over_1024", "tiles_over_2048", "max_batches")] + \
+               [("mean", C.c_double), ("median", C.c_double), ("total_batches", C.c_uint64)]
+
+
+class TileCapStats(C.Structure):
+    _fields_ = [("cap", C.c_uint32), ("affected_tiles", C.c_uint32), ("rasterized_intersections", C.c_uint64),
+                ("dropped_intersections", C.c_uint64), ("dropped_fraction", C.c_double),
+                ("total_batches", C.c_uint64), ("max_batches", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+class ProfileStats(C.Structure):
+    _fields_ = [("tile_loads", TileLoadStats), ("cap_estimates", TileCapStats * 3), ("applied_cap", TileCapStats),
+                ("has_applied_cap", C.c_uint32), ("zero_pixel_subpixel_splats", C.c_uint32)]
+
+
 class Stats(C.Structure):
     _fields_ = [("visible_gaussian_count", C.c_uint32), ("intersection_count", C.c_uint32),
                 ("requested_intersections", C.c_uint32), ("overflow", C.c_uint32),
@@ -102,6 +119,7 @@ SIGNATURES = {
                                              C.POINTER(C.c_uint32)]),
     "gs3d_pipeline_read_stats": (C.c_int, [_P, C.POINTER(Stats)]),
     "gs3d_pipeline_get_resources": (C.c_int, [_P, C.POINTER(Resources)]),
+    "gs3d_pipeline_read_profile": (C.c_int, [_P, C.POINTER(ProfileStats)]),
     "gs3d_pipeline_last_error": (C.c_char_p, [_P]),
     "gs3d_pipeline_last_launch_count": (C.c_uint32, [_P]),
     "gs3d_pipeline_set_profiling": (C.c_int, [_P, C.c_int]),

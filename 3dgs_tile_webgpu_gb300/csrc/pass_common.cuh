@@ -289,6 +289,17 @@ void launch_tile_order(const uint32_t* tile_offsets, uint32_t ntile, Control* ct
 void launch_raster(int precision, const uint32_t* tile_offsets, const uint32_t* order, const uint32_t* sorted_ids,
                    const float4* mean, const float4* conic, const float4* color, const float4* rec,
                    const BatchView& b, const PassOptions& o, Control* ctl, bool stats, cudaStream_t st);
+// Profiling diagnostics: tile-load sums (caps: up to four, 0 = unused) and
+// the zero-pixel subpixel splat count (ProfileDiagnosticsStage.ts:22-116).
+struct TileLoadSums {
+  unsigned long long total, batches;
+  uint32_t max, max_batches, over[4];
+  unsigned long long cap_rasterized[4], cap_dropped[4], cap_batches[4];
+  uint32_t cap_affected[4], cap_max_batches[4];
+};
+void launch_profile(const float4* mean, const float4* conic, const BatchView& b, uint32_t n,
+                    const uint32_t* tile_offsets, uint32_t ntile, const uint32_t caps[4], TileLoadSums* sums,
+                    uint32_t* hist, uint32_t* zero_count, cudaStream_t st);
 void launch_raster_exact(const uint32_t* tile_offsets, const uint32_t* order, const uint32_t* sorted_ids,
                          const float4* mean, const float4* conic, const float4* color, const BatchView& b,
                          const PassOptions& o, Control* ctl, bool stats, cudaStream_t st);

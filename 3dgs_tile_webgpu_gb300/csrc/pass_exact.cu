@@ -591,6 +591,97 @@ void launch_tile_ranges(const uint32_t* keys, Control* ctl, uint32_t ntile, uint
 }
 
 // ---------------------------------------------------------------------------
+// Profiling diagnostics (ProfileDiagnosticsStage.ts:22-116).
+//
+// profileSubpixelCoverageWGSL (kernels/profileDiagnostics.ts:8-64): a
+// projected splat counts when the projection marked it subpixel (mean.w < 0),
+// or when its alpha-support box is at most one pixel in both dimensions and
+// holds no pixel centre inside the support. Counted on the device instead of
+// a per-splat flag buffer read back.
+__global__ void __launch_bounds__(kBlock) k_zero_pixel(const float4* __restrict__ mean,
+                                                       const float4* __restrict__ conic, BatchView bv,
+                                                       uint32_t n, uint32_t* __restrict__ count) {
+  const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+  uint32_t flag = 0;
+  if (i < n) {
+    const float4 m = mean[i];
+    if (m.w < 0.0f) {
+      flag = 1u;
+    } else if (m.w > 0.0f) {
+      const float4 c = conic[i];
+      const float det = c.x * c.z - c.y * c.y;
+      const float thr = gsdm::logf_(m.w * 255.0f);
+      if (det > 1e-12f && thr > 0.0f) {
+        const float s00 = c.z / det, s11 = c.x / det;
+        const float ex = sqrtf(maxf((2.0f * thr) * s00, 0.0f)), ey = sqrtf(maxf((2.0f * thr) * s11, 0.0f));
+        if (!(ex * 2.0f > 1.0f || ey * 2.0f > 1.0f)) {
+          const ViewDesc& v = bv.views[find_view(bv.item_base, bv.nviews, i)];
+          const int W = (int)v.vw, H = (int)v.vh;
+          const int x0 = max((int)ceilf((m.x - ex) - 0.5f), 0), y0 = max((int)ceilf((m.y - ey) - 0.5f), 0);
+          const int x1 = min((int)floorf((m.x + ex) - 0.5f), W - 1), y1 = min((int)floorf((m.y + ey) - 0.5f), H - 1);
+          bool has = false;
+          for (int py = y0; py <= y1; ++py)
+            for (int px = x0; px <= x1; ++px) {
+              const float dx = ((float)px + 0.5f) - m.x, dy = ((float)py + 0.5f) - m.y;
+              const float sigma = 0.5f * ((c.x * dx * dx + 2.0f * c.y * dx * dy) + c.z * dy * dy);
+              if (sigma <= thr) has = true;
+            }
+          flag = has ? 0u : 1u;
+        }
+      }
+    }
+  }
+  const uint32_t warp_sum = __popc(__ballot_sync(0xffffffffu, flag != 0u));
+  if ((threadIdx.x & 31u) == 0u && warp_sum) atomicAdd(count, warp_sum);
+}
+
+// Tile loads (utils/profileStats.ts:9-114): sums, maxima and threshold counts
+// over offsets[t + 1] - offsets[t], the same for the loads capped at each of
+// up to four caps, and a histogram of the loads (bin 65535 collects larger
+// ones) from which the host reads the median and percentiles.
+__global__ void __launch_bounds__(kBlock) k_tile_loads(const uint32_t* __restrict__ off, uint32_t ntile,
+                                                       uint4 caps, TileLoadSums* __restrict__ out,
+                                                       uint32_t* __restrict__ hist) {
+  const uint32_t t = blockIdx.x * kBlock + threadIdx.x;
+  if (t >= ntile) return;
+  const uint32_t load = off[t + 1] > off[t] ? off[t + 1] - off[t] : 0u;
+  atomicAdd(&out->total, (unsigned long long)load);
+  atomicMax(&out->max, load);
+  if (load > 256u) atomicAdd(&out->over[0], 1u);
+  if (load > 512u) atomicAdd(&out->over[1], 1u);
+  if (load > 1024u) atomicAdd(&out->over[2], 1u);
+  if (load > 2048u) atomicAdd(&out->over[3], 1u);
+  const uint32_t batches = (load + 255u) / 256u;
+  atomicAdd(&out->batches, (unsigned long long)batches);
+  atomicMax(&out->max_batches, batches);
+  atomicAdd(&hist[min(load, 65535u)], 1u);
+  const uint32_t cap[4] = {caps.x, caps.y, caps.z, caps.w};
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    if (cap[k] == 0u) continue;
+    const uint32_t r = min(load, cap[k]), d = load - r;
+    atomicAdd(&out->cap_rasterized[k], (unsigned long long)r);
+    if (d) {
+      atomicAdd(&out->cap_dropped[k], (unsigned long long)d);
+      atomicAdd(&out->cap_affected[k], 1u);
+    }
+    const uint32_t b = (r + 255u) / 256u;
+    atomicAdd(&out->cap_batches[k], (unsigned long long)b);
+    atomicMax(&out->cap_max_batches[k], b);
+  }
+}
+
+void launch_profile(const float4* mean, const float4* conic, const BatchView& b, uint32_t n,
+                    const uint32_t* tile_offsets, uint32_t ntile, const uint32_t caps[4], TileLoadSums* sums,
+                    uint32_t* hist, uint32_t* zero_count, cudaStream_t st) {
+  if (n) k_zero_pixel<<<(n + kBlock - 1) / kBlock, kBlock, 0, st>>>(mean, conic, b, n, zero_count);
+  if (ntile)
+    k_tile_loads<<<(ntile + kBlock - 1) / kBlock, kBlock, 0, st>>>(tile_offsets, ntile,
+                                                                  make_uint4(caps[0], caps[1], caps[2], caps[3]),
+                                                                  sums, hist);
+}
+
+// ---------------------------------------------------------------------------
 void launch_raster_exact(const uint32_t* tile_offsets, const uint32_t* order, const uint32_t* ids,
                          const float4* mean, const float4* conic, const float4* color, const BatchView& b,
                          const PassOptions& o, Control* ctl, bool stats, cudaStream_t st) {

@@ -136,6 +136,11 @@ struct gs3d_pipeline {
   gs3d_tuning tuning{0u, 8u, 1u, 0u};
   BatchSummary* summary = nullptr;
   uint32_t last_chunks = 1;
+  BatchView last_bv{};  // batch table of the last launch sequence (device pointers)
+  // Profiling diagnostics scratch: tile-load sums, load histogram, zero-pixel count.
+  TileLoadSums* profile_sums = nullptr;
+  uint32_t* profile_hist = nullptr;
+  uint32_t* profile_zero = nullptr;
   struct GraphChunk {
     uint32_t first, count;
     size_t offset;
@@ -364,7 +369,7 @@ void release_all(gs3d_pipeline* p) {
   dfree(p->dk[0]); dfree(p->dk[1]); dfree(p->dv[0]); dfree(p->dv[1]); dfree(p->ordered); dfree(p->ioff);
   dfree(p->tk[0]); dfree(p->tk[1]); dfree(p->tv[0]); dfree(p->tv[1]);
   dfree(p->tile_offsets); dfree(p->tile_order); dfree(p->ctl); dfree(p->epoch_dev); dfree(p->output_state); dfree(p->status);
-  dfree(p->summary);
+  dfree(p->summary); dfree(p->profile_sums); dfree(p->profile_hist); dfree(p->profile_zero);
 }
 
 }  // namespace
@@ -642,6 +647,7 @@ void record_batch(gs3d_pipeline* p, const Plan& pl, unsigned char* dev, cudaStre
   bv.total_items = pl.items;
   bv.total_tiles = pl.tiles;
   bv.total_blocks = pl.blocks;
+  p->last_bv = bv;
 
   PassOptions o;
   memset(&o, 0, sizeof(o));
@@ -1119,6 +1125,83 @@ gs3d_status gs3d_pipeline_stage_times(gs3d_pipeline* p, float* ms, uint32_t* ren
     for (uint32_t s = 0; s < GS3D_STAGE_COUNT; ++s) ms[s] /= (float)n;
   if (renders) *renders = n;
   p->profiled = 0;
+  return GS3D_OK;
+}
+
+gs3d_status gs3d_pipeline_read_profile(gs3d_pipeline* p, gs3d_profile_stats* out) {
+  if (!p || !out) return GS3D_ERROR_INVALID_ARGUMENT;
+  if (!p->prepared) return fail(p, GS3D_ERROR_NOT_PREPARED, "render a frame before reading the profile");
+  cudaSetDevice(p->device);
+  cudaError_t e = cudaSuccess;
+  if (!p->profile_sums &&
+      ((e = dalloc(p->profile_sums, 1)) || (e = dalloc(p->profile_hist, 65536)) || (e = dalloc(p->profile_zero, 1))))
+    return cuda_fail(p, e, "allocating profile scratch");
+  cudaStream_t st = p->last_stream;
+  const uint32_t ntile = p->total_tiles, n = p->total_items;
+  cudaMemsetAsync(p->profile_sums, 0, sizeof(TileLoadSums), st);
+  cudaMemsetAsync(p->profile_hist, 0, 65536 * sizeof(uint32_t), st);
+  cudaMemsetAsync(p->profile_zero, 0, sizeof(uint32_t), st);
+  // PROFILE_TILE_CAPS (utils/profileStats.ts:7) and the configured cap.
+  const uint32_t caps[4] = {2048u, 4096u, 8192u, p->desc.max_rasterized_splats_per_tile};
+  launch_profile(p->mean, p->conic, p->last_bv, n, p->tile_offsets, ntile, caps, p->profile_sums, p->profile_hist,
+                 p->profile_zero, st);
+  TileLoadSums sums;
+  std::vector<uint32_t> hist(65536);
+  uint32_t zero = 0;
+  if ((e = cudaMemcpyAsync(&sums, p->profile_sums, sizeof(sums), cudaMemcpyDeviceToHost, st)) ||
+      (e = cudaMemcpyAsync(hist.data(), p->profile_hist, 65536 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st)) ||
+      (e = cudaMemcpyAsync(&zero, p->profile_zero, sizeof(uint32_t), cudaMemcpyDeviceToHost, st)) ||
+      (e = cudaStreamSynchronize(st)))
+    return cuda_fail(p, e, "reading the profile");
+  memset(out, 0, sizeof(*out));
+  out->zero_pixel_subpixel_splats = zero;
+  gs3d_tile_load_stats& L = out->tile_loads;
+  if (ntile) {
+    // The k-th smallest load from the histogram; loads past its last bin are
+    // read back exactly from the tile offsets.
+    std::vector<uint32_t> exact;
+    auto kth = [&](uint64_t k) -> uint32_t {
+      uint64_t run = 0;
+      for (uint32_t b = 0; b < 65535u; ++b) {
+        run += hist[b];
+        if (k < run) return b;
+      }
+      if (exact.empty()) {
+        std::vector<uint32_t> off(ntile + 1);
+        cudaMemcpy(off.data(), p->tile_offsets, (ntile + 1) * sizeof(uint32_t), cudaMemcpyDeviceToHost);
+        for (uint32_t t = 0; t < ntile; ++t)
+          if (off[t + 1] > off[t] && off[t + 1] - off[t] >= 65535u) exact.push_back(off[t + 1] - off[t]);
+        std::sort(exact.begin(), exact.end());
+      }
+      return exact.empty() ? 65535u : exact[std::min<uint64_t>(k - run, exact.size() - 1)];
+    };
+    L.max = sums.max;
+    L.mean = (double)sums.total / (double)ntile;
+    const uint32_t mid = ntile / 2;
+    L.median = (ntile % 2) ? (double)kth(mid) : ((double)kth(mid - 1) + (double)kth(mid)) * 0.5;
+    const auto pct = [&](double f) { return kth((uint64_t)std::max<int64_t>(0, (int64_t)std::ceil(ntile * f) - 1)); };
+    L.p95 = pct(0.95);
+    L.p99 = pct(0.99);
+    L.tiles_over_256 = sums.over[0];
+    L.tiles_over_512 = sums.over[1];
+    L.tiles_over_1024 = sums.over[2];
+    L.tiles_over_2048 = sums.over[3];
+    L.total_batches = sums.batches;
+    L.max_batches = sums.max_batches;
+  }
+  auto cap_stats = [&](int k, gs3d_tile_cap_stats* c) {
+    c->cap = caps[k];
+    c->rasterized_intersections = sums.cap_rasterized[k];
+    c->dropped_intersections = sums.cap_dropped[k];
+    const uint64_t emitted = sums.cap_rasterized[k] + sums.cap_dropped[k];
+    c->dropped_fraction = emitted == 0 ? 0.0 : (double)sums.cap_dropped[k] / (double)emitted;
+    c->affected_tiles = sums.cap_affected[k];
+    c->total_batches = sums.cap_batches[k];
+    c->max_batches = sums.cap_max_batches[k];
+  };
+  for (int k = 0; k < 3; ++k) cap_stats(k, &out->cap_estimates[k]);
+  out->has_applied_cap = caps[3] != 0u;
+  if (out->has_applied_cap) cap_stats(3, &out->applied_cap);
   return GS3D_OK;
 }
 

@@ -308,6 +308,47 @@ gs3d_status gs3d_pipeline_set_profiling(gs3d_pipeline* pipeline, int enabled);
 gs3d_status gs3d_pipeline_stage_times(gs3d_pipeline* pipeline, float* ms, uint32_t* renders);
 const char* gs3d_stage_name(uint32_t stage);
 
+/* Profiling diagnostics of the last launch sequence (the reference's
+ * profile stats, ProfileDiagnosticsStage.ts:22-116, utils/profileStats.ts,
+ * types.ts:105-148), computed on the device: tile loads over the tile
+ * offsets, cap estimates at 2048/4096/8192 records per tile and at the
+ * configured maxRasterizedSplatsPerTile, and the number of projected splats
+ * whose subpixel footprint holds no pixel centre. Synchronises the stream. */
+typedef struct gs3d_tile_load_stats {
+  uint32_t max;
+  uint32_t p95;
+  uint32_t p99;
+  uint32_t tiles_over_256;
+  uint32_t tiles_over_512;
+  uint32_t tiles_over_1024;
+  uint32_t tiles_over_2048;
+  uint32_t max_batches;      /* 256-record raster batches of the heaviest tile */
+  double mean;
+  double median;
+  uint64_t total_batches;    /* 256-record raster batches over all tiles */
+} gs3d_tile_load_stats;
+
+typedef struct gs3d_tile_cap_stats {
+  uint32_t cap;
+  uint32_t affected_tiles;
+  uint64_t rasterized_intersections;
+  uint64_t dropped_intersections;
+  double dropped_fraction;
+  uint64_t total_batches;
+  uint32_t max_batches;
+  uint32_t reserved;
+} gs3d_tile_cap_stats;
+
+typedef struct gs3d_profile_stats {
+  gs3d_tile_load_stats tile_loads;
+  gs3d_tile_cap_stats cap_estimates[3]; /* caps 2048, 4096, 8192 */
+  gs3d_tile_cap_stats applied_cap;      /* valid when has_applied_cap */
+  uint32_t has_applied_cap;
+  uint32_t zero_pixel_subpixel_splats;
+} gs3d_profile_stats;
+
+gs3d_status gs3d_pipeline_read_profile(gs3d_pipeline* pipeline, gs3d_profile_stats* out);
+
 /* On-device compact packer (the reference packs on the CPU:
  * rust/gaussian-backend/src/engine.rs:1801-1891 encode_attributes with the
  * compact layout, spark-lib splat_encode.rs:127-136,234-252, pack_sh

@@ -102,6 +102,8 @@ def lib():
             L.gso_pack_sh.argtypes = [_FP]
             L.gso_encode_oct101012.restype = _U
             L.gso_encode_oct101012.argtypes = [_FP]
+            L.gso_zero_pixel_flag.restype = _U
+            L.gso_zero_pixel_flag.argtypes = [_FP, _FP, _U, _U]
             L.gso_f16_bits.restype = _U
             L.gso_f16_bits.argtypes = [_F]
             L.gso_pack_splat.restype = None

@@ -561,6 +561,7 @@ void gso_decode_sh(uint32_t packed, float* out3) {
 }
 
 uint32_t gso_f16_bits(float x);
+uint32_t gso_zero_pixel_flag(const float* mean4, const float* conic4, uint32_t vw, uint32_t vh);
 
 // engine.rs:1801-1891 encode_attributes (compact layout) for one splat: the
 // packed means, scalesOpacity, rotation and C rgb8e8 SH words, on the CPU with
@@ -641,6 +642,31 @@ uint32_t gso_encode_oct101012(const float* q_in) {
 }
 
 uint32_t gso_f16_bits(float x) { return f16_bits_rne(x); }
+
+// kernels/profileDiagnostics.ts:8-64 profileSubpixelCoverageWGSL for one
+// projected splat (mean4, conic4 as the projection wrote them).
+uint32_t gso_zero_pixel_flag(const float* m, const float* c, uint32_t vw, uint32_t vh) {
+  if (m[3] < 0.0f) return 1u;
+  if (m[3] <= 0.0f) return 0u;
+  const float det = c[0] * c[2] - c[1] * c[1];
+  if (det <= 1e-12f) return 0u;
+  const float thr = gsdm::logf_(m[3] * 255.0f);
+  if (thr <= 0.0f) return 0u;
+  const float s00 = c[2] / det, s11 = c[0] / det;
+  const float ex = sqrtf(std::max((2.0f * thr) * s00, 0.0f)), ey = sqrtf(std::max((2.0f * thr) * s11, 0.0f));
+  if (ex * 2.0f > 1.0f || ey * 2.0f > 1.0f) return 0u;
+  const int x0 = std::max((int)ceilf((m[0] - ex) - 0.5f), 0), y0 = std::max((int)ceilf((m[1] - ey) - 0.5f), 0);
+  const int x1 = std::min((int)floorf((m[0] + ex) - 0.5f), (int)vw - 1);
+  const int y1 = std::min((int)floorf((m[1] + ey) - 0.5f), (int)vh - 1);
+  bool has = false;
+  for (int py = y0; py <= y1; ++py)
+    for (int px = x0; px <= x1; ++px) {
+      const float dx = ((float)px + 0.5f) - m[0], dy = ((float)py + 0.5f) - m[1];
+      const float sigma = 0.5f * ((c[0] * dx * dx + 2.0f * c[1] * dx * dy) + c[2] * dy * dy);
+      if (sigma <= thr) has = true;
+    }
+  return has ? 0u : 1u;
+}
 
 void gso_pack_splat(const float* center, const float* scale, float opacity, const float* quat, const float* rgb,
                     const float* sh_rest, uint32_t C, uint32_t object_id, float* means4, uint32_t* shape2,
