@@ -45,6 +45,8 @@ def parse():
     ap.add_argument("--latency-frames", type=int, default=240)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shape for the batched form")
+    ap.add_argument("--views-per-launch", type=int, default=None,
+                    help="fixed launch shape for the batched form instead of the autotuner's")
     ap.add_argument("--forms", default="all", choices=["all", "batched"],
                     help="'batched' skips the timed plain (one view per launch) form")
     ap.add_argument("--serve", action="store_true", help="serving-loop measurement (configuration 4)")
@@ -417,7 +419,9 @@ def main() -> None:
     # Launch shape from the autotuner (outputs do not depend on it), before
     # the untimed sizing render and the graph capture.
     tune_ms = None
-    if not args.no_autotune:
+    if args.views_per_launch is not None:
+        batched.set_tuning({"views_per_launch": args.views_per_launch})
+    elif not args.no_autotune:
         _, tune_ms = batched.autotune(views, trials=3)
     tuning = batched.get_tuning()
     batched.render_batch(views)  # size the workspaces, then capture the pass as a graph
