@@ -145,18 +145,11 @@ __global__ void __launch_bounds__(kBlock, 3)
     const uint32_t e = block_exclusive_scan<false>(tid < RADIX ? block_count : 0u, s_scan, &tot);
     if (tid < RADIX) s_block_excl[tid] = e;
   }
-  if (tid < RADIX) {
-    uint32_t prefix = 0;
-    if (tile > 0) {
-      prefix = window_lookback<kSortWindow>(status + tid, RADIX, tile, epoch, err);
-      st_release(status + (size_t)tile * RADIX + tid, pack_status(epoch, kFlagInclusive, prefix + block_count));
-    }
-    s_global_base[tid] = s_hist_excl[tid] + prefix;
-  }
   cp_async_commit_wait();
   __syncthreads();
 
-  // Stage keys and values in block-sorted order.
+  // Stage keys and values in block-sorted order (block-local prefixes only),
+  // so the keys and ranks leave registers before the look-back.
 #pragma unroll
   for (int j = 0; j < kSortItems; ++j) {
     const uint32_t idx = wbase + (uint32_t)j * 32u + lane;
@@ -166,6 +159,16 @@ __global__ void __launch_bounds__(kBlock, 3)
       s_keys[pos] = k[j];
       s_vals[pos] = vraw[(uint32_t)j * 32u + lane];
     }
+  }
+
+  // Global base of every digit: decoupled look-back over the predecessors.
+  if (tid < RADIX) {
+    uint32_t prefix = 0;
+    if (tile > 0) {
+      prefix = window_lookback<kSortWindow>(status + tid, RADIX, tile, epoch, err);
+      st_release(status + (size_t)tile * RADIX + tid, pack_status(epoch, kFlagInclusive, prefix + block_count));
+    }
+    s_global_base[tid] = s_hist_excl[tid] + prefix;
   }
   __syncthreads();
 
