@@ -444,31 +444,21 @@ struct EmitShared {
   uint32_t hist[kMaxSortPasses][256];
 };
 
-__global__ void __launch_bounds__(kBlock) k_emit(const uint32_t* __restrict__ ids, const float4* __restrict__ mean,
-                                                 const float4* __restrict__ conic,
-                                                 const uint32_t* __restrict__ ordered,
-                                                 const uint32_t* __restrict__ offsets, BatchView bv, PassOptions o,
-                                                 Control* __restrict__ ctl, uint32_t capacity,
-                                                 uint32_t* __restrict__ tile_keys, uint32_t* __restrict__ tile_vals,
-                                                 int passes, int digit_bits) {
-  if (ctl->state[3] != 0u) return;  // overflow: emission dispatch is zero
-  __shared__ EmitShared sm;
+// One group of kBlock depth ranks (32 per warp): stage each lane's box and
+// tile-test inputs for its warp, walk the union of the warp's boxes 32 box
+// tiles per round, place hits after the owner's earlier hits, pad with
+// sentinels. The lane's rank data were loaded by the caller.
+__device__ __forceinline__ void emit_group(EmitShared& sm, bool live, uint32_t g, float4 m, float4 c,
+                                           uint32_t reserved, uint32_t base_off, const BatchView& bv,
+                                           const PassOptions& o, uint32_t capacity, uint32_t* __restrict__ tile_keys,
+                                           uint32_t* __restrict__ tile_vals, int passes, int digit_bits) {
   const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-  const uint32_t n = ctl->visible_state[0];
-  if (blockIdx.x * kBlock >= n) return;  // whole block past the visible count
-  for (uint32_t i = tid; i < kMaxSortPasses * 256; i += kBlock) (&sm.hist[0][0])[i] = 0u;
-  const uint32_t r = blockIdx.x * kBlock + tid;
   const uint32_t mask = (1u << digit_bits) - 1u;
   const uint32_t sentinel = bv.total_tiles;
   const uint32_t lt = (1u << lane) - 1u;
-
-  // This lane's rank: its box and test inputs, staged for the whole warp.
-  uint32_t nbox = 0, reserved = 0;
-  if (r < n) {
-    const uint32_t g = ids[r];
+  uint32_t nbox = 0;
+  if (live) {
     const ViewDesc& v = bv.views[find_view(bv.item_base, bv.nviews, g)];
-    const float4 m = __ldg(mean + g);
-    const float4 c = __ldg(conic + g);
     const uint32_t packed = (uint32_t)c.w;
     const float rx = (float)(packed % 512u), ry = (float)(packed / 512u);
     const float thr = gsdm::logf_(m.w * 255.0f);
@@ -480,7 +470,6 @@ __global__ void __launch_bounds__(kBlock) k_emit(const uint32_t* __restrict__ id
     int tmaxy = (int)clampf(floorf((m.y + ry) / 16.0f), 0.0f, mty);
     if (o.axis == 1u) { tminx = 0; tmaxx = tiles_x - 1; }
     if (o.axis == 2u) { tminy = 0; tmaxy = tiles_y - 1; }
-    reserved = ordered[r];
     const uint32_t bw = (uint32_t)(tmaxx - tminx + 1);
     // A rank with nothing reserved emits nothing; its box takes no rounds.
     nbox = reserved ? bw * (uint32_t)(tmaxy - tminy + 1) : 0u;
@@ -490,7 +479,7 @@ __global__ void __launch_bounds__(kBlock) k_emit(const uint32_t* __restrict__ id
     sm.f[8][warp][lane] = v.vw; sm.f[9][warp][lane] = v.vh;
     sm.u[0][warp][lane] = (uint32_t)tminx; sm.u[1][warp][lane] = (uint32_t)tminy; sm.u[2][warp][lane] = bw;
     sm.u[3][warp][lane] = (uint32_t)tiles_x; sm.u[4][warp][lane] = v.tile_base;
-    sm.u[5][warp][lane] = offsets[r]; sm.u[6][warp][lane] = reserved; sm.u[7][warp][lane] = g;
+    sm.u[5][warp][lane] = base_off; sm.u[6][warp][lane] = reserved; sm.u[7][warp][lane] = g;
   }
   uint32_t incl = nbox;
 #pragma unroll
@@ -500,7 +489,7 @@ __global__ void __launch_bounds__(kBlock) k_emit(const uint32_t* __restrict__ id
   }
   sm.incl[warp][lane] = incl;
   sm.filled[warp][lane] = 0u;
-  __syncthreads();  // histogram cleared; warp tables written
+  __syncwarp();
   const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
 
   for (uint32_t j0 = 0; j0 < total; j0 += 32) {
@@ -542,15 +531,66 @@ __global__ void __launch_bounds__(kBlock) k_emit(const uint32_t* __restrict__ id
   }
 
   // Sentinel padding for reserved slots without a hit.
-  if (r < n) {
-    const uint32_t base = sm.u[5][warp][lane];
-    const uint32_t g = sm.u[7][warp][lane];
+  if (live) {
     for (uint32_t pad = sm.filled[warp][lane]; pad < reserved; ++pad)
-      if (base + pad < capacity) {
-        tile_keys[base + pad] = sentinel;
-        tile_vals[base + pad] = g;
+      if (base_off + pad < capacity) {
+        tile_keys[base_off + pad] = sentinel;
+        tile_vals[base_off + pad] = g;
         for (int p = 0; p < passes; ++p) atomicAdd(&sm.hist[p][(sentinel >> (p * digit_bits)) & mask], 1u);
       }
+  }
+  __syncwarp();  // the warp's tables are rewritten by the next group
+}
+
+// A block takes G groups of kBlock consecutive depth ranks and issues every
+// group's loads (ids, reserved counts, offsets, then the gathered mean and
+// conic) before working through the groups, so the gather latency of later
+// groups overlaps the earlier groups' work. Two groups pay off on large
+// launches (many blocks in flight anyway); one keeps small launches wide.
+constexpr uint32_t kEmitTwoGroupsFrom = 1u << 23;  // ranks per launch
+
+template <int G>
+__global__ void __launch_bounds__(kBlock) k_emit(const uint32_t* __restrict__ ids, const float4* __restrict__ mean,
+                                                 const float4* __restrict__ conic,
+                                                 const uint32_t* __restrict__ ordered,
+                                                 const uint32_t* __restrict__ offsets, BatchView bv, PassOptions o,
+                                                 Control* __restrict__ ctl, uint32_t capacity,
+                                                 uint32_t* __restrict__ tile_keys, uint32_t* __restrict__ tile_vals,
+                                                 int passes, int digit_bits) {
+  if (ctl->state[3] != 0u) return;  // overflow: emission dispatch is zero
+  __shared__ EmitShared sm;
+  const uint32_t tid = threadIdx.x;
+  const uint32_t n = ctl->visible_state[0];
+  const uint32_t first = blockIdx.x * kBlock * G;
+  if (first >= n) return;  // whole block past the visible count
+  for (uint32_t i = tid; i < kMaxSortPasses * 256; i += kBlock) (&sm.hist[0][0])[i] = 0u;
+  uint32_t g[G], res[G], off[G];
+  float4 m[G], c[G];
+#pragma unroll
+  for (int h = 0; h < G; ++h) {
+    const uint32_t r = first + (uint32_t)h * kBlock + tid;
+    g[h] = 0u; res[h] = 0u; off[h] = 0u;
+    if (r < n) {
+      g[h] = ids[r];
+      res[h] = ordered[r];
+      off[h] = offsets[r];
+    }
+  }
+#pragma unroll
+  for (int h = 0; h < G; ++h) {
+    const uint32_t r = first + (uint32_t)h * kBlock + tid;
+    m[h] = c[h] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (r < n) {
+      m[h] = __ldg(mean + g[h]);
+      c[h] = __ldg(conic + g[h]);
+    }
+  }
+  __syncthreads();  // histogram cleared
+#pragma unroll
+  for (int h = 0; h < G; ++h) {
+    const uint32_t r = first + (uint32_t)h * kBlock + tid;
+    emit_group(sm, r < n, g[h], m[h], c[h], res[h], off[h], bv, o, capacity, tile_keys, tile_vals, passes,
+               digit_bits);
   }
   __syncthreads();
   const uint32_t radix = 1u << digit_bits;
@@ -564,9 +604,15 @@ void launch_emit(const uint32_t* ids, uint32_t n_max, const float4* mean, const 
                  Control* ctl, uint32_t capacity, uint32_t* tile_keys, uint32_t* tile_vals, int passes,
                  int digit_bits, cudaStream_t st) {
   if (n_max == 0) return;
-  const uint32_t grid = (n_max + kBlock - 1) / kBlock;
-  k_emit<<<grid, kBlock, 0, st>>>(ids, mean, conic, ordered, offsets, b, o, ctl, capacity, tile_keys, tile_vals,
-                                  passes, digit_bits);
+  if (n_max >= kEmitTwoGroupsFrom) {
+    const uint32_t grid = (n_max + 2 * kBlock - 1) / (2 * kBlock);
+    k_emit<2><<<grid, kBlock, 0, st>>>(ids, mean, conic, ordered, offsets, b, o, ctl, capacity, tile_keys, tile_vals,
+                                       passes, digit_bits);
+  } else {
+    const uint32_t grid = (n_max + kBlock - 1) / kBlock;
+    k_emit<1><<<grid, kBlock, 0, st>>>(ids, mean, conic, ordered, offsets, b, o, ctl, capacity, tile_keys, tile_vals,
+                                       passes, digit_bits);
+  }
 }
 
 // ---------------------------------------------------------------------------
