@@ -272,8 +272,8 @@ void launch_emit(const uint32_t* sorted_ids, uint32_t n_max, const float4* mean,
                  const uint32_t* ordered, const uint32_t* offsets, const BatchView& b, const PassOptions& o,
                  Control* ctl, uint32_t capacity, uint32_t* tile_keys, uint32_t* tile_vals, int tile_passes,
                  int tile_digit_bits, cudaStream_t st);
-void launch_tile_ranges(const uint32_t* sorted_tiles, Control* ctl, uint32_t ntile, uint32_t* offsets, int sms,
-                        cudaStream_t st);
+void launch_tile_ranges(const uint32_t* sorted_tile_keys, Control* ctl, uint32_t ntile, uint32_t n_max,
+                        uint32_t* tile_offsets, cudaStream_t st);
 // Onesweep LSD pass. n is read from *n_ptr on the device.
 void launch_onesweep(int bits, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
                      uint32_t* vals_out, const uint32_t* n_ptr, uint32_t n_max, int shift, const uint32_t* hist,

@@ -619,21 +619,38 @@ void launch_emit(const uint32_t* ids, uint32_t n_max, const float4* mean, const 
 // Tile ranges (tileOffsets.ts:4-128): offsets[t] = first sorted index with
 // tile >= t, i.e. the reference's boundary detection followed by its
 // suffix-min fill, written directly (offsets[T] = first sentinel or count).
-__global__ void k_tile_ranges(const uint32_t* __restrict__ keys, const Control* __restrict__ ctl, uint32_t ntile,
-                              uint32_t* __restrict__ off) {
+__global__ void __launch_bounds__(kBlock) k_tile_ranges(const uint32_t* __restrict__ keys,
+                                                        const Control* __restrict__ ctl, uint32_t ntile,
+                                                        uint32_t* __restrict__ off) {
+  // Each thread owns 8 consecutive boundaries i in [i0, i0 + 8), reading the
+  // keys with two 16-byte loads (i0 is a multiple of 8).
   const uint32_t n = ctl->state[0];
-  const uint32_t stride = gridDim.x * blockDim.x;
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i <= n; i += stride) {
-    const uint32_t lo = i == 0 ? 0u : keys[i - 1] + 1u;
-    const uint32_t hi = i == n ? ntile : min(keys[i], ntile);
+  const uint32_t i0 = (blockIdx.x * kBlock + threadIdx.x) * 8u;
+  if (i0 > n) return;
+  uint32_t k[9];  // k[0] = keys[i0 - 1], k[1 + j] = keys[i0 + j]
+  k[0] = i0 ? keys[i0 - 1] : 0u;
+  if (i0 + 8u <= n) {
+    const uint4 a = *reinterpret_cast<const uint4*>(keys + i0);
+    const uint4 b = *reinterpret_cast<const uint4*>(keys + i0 + 4);
+    k[1] = a.x; k[2] = a.y; k[3] = a.z; k[4] = a.w; k[5] = b.x; k[6] = b.y; k[7] = b.z; k[8] = b.w;
+  } else {
+#pragma unroll
+    for (uint32_t j = 0; j < 8u; ++j) k[1 + j] = i0 + j < n ? keys[i0 + j] : 0u;
+  }
+#pragma unroll
+  for (uint32_t j = 0; j < 8u; ++j) {
+    const uint32_t i = i0 + j;
+    if (i > n) break;
+    const uint32_t lo = i == 0 ? 0u : k[j] + 1u;
+    const uint32_t hi = i == n ? ntile : min(k[1 + j], ntile);
     for (uint32_t t = lo; t <= hi; ++t) off[t] = i;
-    if (i == n) break;
   }
 }
 
-void launch_tile_ranges(const uint32_t* keys, Control* ctl, uint32_t ntile, uint32_t* offsets, int sms,
+void launch_tile_ranges(const uint32_t* keys, Control* ctl, uint32_t ntile, uint32_t n_max, uint32_t* offsets,
                         cudaStream_t st) {
-  k_tile_ranges<<<sms * 4, kBlock, 0, st>>>(keys, ctl, ntile, offsets);
+  const uint32_t grid = (uint32_t)(((uint64_t)n_max + 1 + 8ull * kBlock - 1) / (8ull * kBlock));
+  k_tile_ranges<<<grid, kBlock, 0, st>>>(keys, ctl, ntile, offsets);
 }
 
 // ---------------------------------------------------------------------------

@@ -727,7 +727,7 @@ void record_batch(gs3d_pipeline* p, const Plan& pl, unsigned char* dev, cudaStre
   p->tile_final = tcur;
   // Tile ranges and the raster work list.
   mark(p, GS3D_STAGE_RANGES, st);
-  launch_tile_ranges(p->tk[tcur], ctl, tile, p->tile_offsets, p->sms, st);
+  launch_tile_ranges(p->tk[tcur], ctl, tile, cap32, p->tile_offsets, st);
   ++launches;
   const bool ordered_tiles = p->tuning.work_order != 0u;
   if (ordered_tiles) {
