@@ -75,6 +75,8 @@ __device__ __forceinline__ uint32_t find_view(const uint32_t* base, uint32_t nvi
 }
 
 constexpr uint32_t kMaxSortPasses = 4;  // digit histograms held per sort
+constexpr uint32_t kScanItems = 8;                      // items per thread of the look-back scans
+constexpr uint32_t kScanTile = kBlock * kScanItems;     // items per look-back tile (compaction, scan)
 
 // Per-frame control block, zeroed before each render.
 struct Control {

@@ -250,8 +250,7 @@ void launch_project(const BatchView& b, const PassOptions& o, float4* mean, floa
 // Visibility compaction (scan.ts:9-83 + visibility.ts:9-61): one pass with
 // decoupled look-back. Writes visibleOffsets, the (depthKey, ordinal) records
 // in ordinal order, the visible state, and the depth sort's digit histograms.
-constexpr uint32_t kItems = 8;
-constexpr uint32_t kScanTile = kBlock * kItems;  // 2048 items per tile
+constexpr uint32_t kItems = kScanItems;
 
 __global__ void __launch_bounds__(kBlock) k_compact(const uint32_t* __restrict__ keys, uint32_t n,
                                                     uint32_t* __restrict__ vis_off, uint32_t* __restrict__ keys_out,

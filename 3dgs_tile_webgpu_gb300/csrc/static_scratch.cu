@@ -35,7 +35,7 @@ using namespace gs;
 
 namespace {
 
-constexpr uint32_t kCompactTile = 2048;  // items per look-back tile of k_compact
+constexpr uint32_t kCompactTile = kScanTile;  // items per look-back tile of k_compact
 constexpr size_t kControlWords = (sizeof(Control) + 7) / 8;
 constexpr size_t kStatusWords = GS3D_STATIC_COMPACT_MAX_ITEMS / kCompactTile + 1;
 constexpr size_t kStaticScratchWords = kControlWords + kStatusWords;
