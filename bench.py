@@ -161,6 +161,22 @@ def dist():
     return world, rank, local
 
 
+def max_over_ranks(value: float, world: int, device: str = "cuda") -> float:
+    """The slowest rank's value (replicas: the job ends with its last rank)."""
+    if world <= 1:
+        return float(value)
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_frames_per_s(steps: int, frames_per_step: int, world: int, seconds: float) -> float:
+    """Whole-job throughput: every replica renders its own frames_per_step
+    frames per step (weak scaling), timed by the slowest rank."""
+    return steps * frames_per_step * world / seconds
+
+
 def run_reference(args) -> None:
     """CPU restatement of the pass (the oracle) on all host threads."""
     world, rank, _ = dist()
@@ -400,16 +416,13 @@ def main() -> None:
         ms = e0.elapsed_time(e1)
         sm, prof = pipe_for_stages.stage_times()
         pipe_for_stages.set_profiling(False)
-        if world > 1:
-            t = torch.tensor([ms], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = max_over_ranks(ms, world)
         return ms, sm, prof, nl, ck
 
     fps_plain = stage_ms_plain = launches_plain = clocks_plain = None
     if args.forms == "all":
         ms_plain, stage_ms_plain, prof_plain, launches_plain, clocks_plain = timed(step_plain, plain)
-        fps_plain = args.steps * ncam * world / (ms_plain / 1000.0)
+        fps_plain = job_frames_per_s(args.steps, ncam, world, ms_plain / 1000.0)
 
     # Batched form: all cameras of a step in one launch sequence.
     batched = P.TiledGaussianPipeline(ds.data(), {"raster_precision": args.precision,
@@ -451,8 +464,8 @@ def main() -> None:
         step_graph()
     g1.record(gstream)
     torch.cuda.synchronize()
-    fps_graph = args.steps * ncam * world / (g0.elapsed_time(g1) / 1000.0)
-    fps = args.steps * ncam * world / (ms_total / 1000.0)
+    fps_graph = job_frames_per_s(args.steps, ncam, world, max_over_ranks(g0.elapsed_time(g1), world) / 1000.0)
+    fps = job_frames_per_s(args.steps, ncam, world, ms_total / 1000.0)
     bstats = batched.read_stats()
 
     # Latency distributions: one frame (plain) and one 16-camera batch, each
@@ -492,10 +505,7 @@ def main() -> None:
                 host.copy_(c, non_blocking=True)
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(e2e_s, world)
     frames_done = args.steps * ncam * world
     e2e_fps = frames_done / e2e_s
     h2d = ncam * (16 * 4 + 40 * 4)  # projection + one object row per view
