@@ -59,7 +59,35 @@ CASES = {
     "degree0": lambda: (sc.uniform_cloud(3000, seed=22, degree=0, log_scale=(-2.4, 0.6)), cam()),
     "degree2": lambda: (sc.uniform_cloud(3000, seed=23, degree=2, log_scale=(-2.4, 0.6)), cam()),
     "behind_camera": lambda: (cube(seed=24), cam(eye=(0, 0, 2.0), target=(0, 0, 10.0))),
+    "special_values": lambda: (special_values_scene(), cam()),
 }
+
+
+def special_values_scene():
+    """Packed inputs the format can carry but a healthy backend rarely
+    writes: NaN and infinite centres, f16 +-inf / NaN / extreme log-scales,
+    opacity f16 NaN / 0 / negative / above 1 / inf, arbitrary rotation and
+    rgb8e8 words, empty slots and object ids without a row. Every stage must
+    treat them exactly as the FP32 restatement does."""
+    scene = cube(4000, seed=25, log_scale=(-2.2, 0.5))
+    rng = np.random.Generator(np.random.PCG64(26))
+    m, shape, rot, sh = scene["means"], scene["shape"], scene["rotations"], scene["sh"]
+    nan, inf = np.float32(np.nan), np.float32(np.inf)
+    m[0, 0], m[1, 1], m[2, 2], m[3, 0], m[4, 2] = nan, nan, nan, inf, -inf
+    m[5, 3] = -1.0   # empty slot
+    m[6, 3] = 7.0    # object id without an object row
+    specials = np.array([0x7C00, 0xFC00, 0x7E00, 0x7BFF, 0xFBFF, 0x0001, 0x0000, 0x8000], np.uint32)
+    k = 10
+    for i, a in enumerate(specials):
+        for j, b in enumerate(specials):
+            shape[k, 0] = a | (b << 16)
+            shape[k, 1] = specials[(i + j) % 8] | (np.uint32([0x7E00, 0x0000, 0xBC00, 0x4000, 0x7C00, 0x3C00, 0x3800, 0x1400][(i * 3 + j) % 8]) << 16)
+            k += 1
+    rot[100:160] = rng.integers(0, 2 ** 32, 60, dtype=np.uint64).astype(np.uint32)
+    rot[160] = 0
+    C = 16
+    sh[200 * C:260 * C] = rng.integers(0, 2 ** 32, 60 * C, dtype=np.uint64).astype(np.uint32)
+    return scene
 
 
 @pytest.mark.parametrize("name", sorted(CASES))
