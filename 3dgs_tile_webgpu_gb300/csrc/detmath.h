@@ -6,8 +6,10 @@
 // src/renderer/kernels/projectionHelpers.ts:38-70,
 // src/renderer/pipeline/ProjectionStage.ts:536-547). Platform math libraries
 // differ in their last bits between CPU and GPU, so these functions are written
-// from the mathematics using only IEEE-754 add, sub, mul, div (correctly rounded
-// on both sides) plus exact bit manipulation:
+// from the mathematics using only IEEE-754 add, sub, mul, div and fused
+// multiply-add (all correctly rounded on both sides) plus exact bit
+// manipulation; the series are evaluated by Horner steps, each one fused
+// multiply-add:
 //
 //   exp   : Cody-Waite reduction x = n ln2 + r, |r| <= ln2/2, Taylor series of
 //           e^r to degree 8, scaling by 2^n through exact exponent arithmetic.
@@ -26,11 +28,20 @@
 // Bit-identical results on host and device need the two compilers to evaluate
 // the same operation sequence: device translation units that include this file
 // for exact stages are built with --fmad=false, host code with
-// -ffp-contract=off, and neither side uses fast-math or flush-to-zero.
+// -ffp-contract=off, and neither side uses fast-math or flush-to-zero; the
+// fused steps are explicit (GS_FMA: __fmaf_rn on the device, C99 fmaf on the
+// host, both the correctly rounded a * b + c).
 #pragma once
 
+#include <math.h>
 #include <stdint.h>
 #include <string.h>
+
+#if defined(__CUDA_ARCH__)
+#define GS_FMA(a, b, c) __fmaf_rn((a), (b), (c))
+#else
+#define GS_FMA(a, b, c) fmaf((a), (b), (c))
+#endif
 
 #if defined(__CUDACC__)
 #define GS_HD __host__ __device__ __forceinline__
@@ -100,14 +111,14 @@ GS_HD float expf_(float x) {
   float r = (x - n * LN2_HI) - n * LN2_LO;
   // Taylor coefficients 1/k!
   float p = 2.4801587301587302e-05f;                 // 1/8!
-  p = 1.9841269841269841e-04f + r * p;               // 1/7!
-  p = 1.3888888888888889e-03f + r * p;               // 1/6!
-  p = 8.3333333333333333e-03f + r * p;               // 1/5!
-  p = 4.1666666666666667e-02f + r * p;               // 1/4!
-  p = 1.6666666666666667e-01f + r * p;               // 1/3!
-  p = 0.5f + r * p;
-  p = 1.0f + r * p;
-  p = 1.0f + r * p;
+  p = GS_FMA(r, p, 1.9841269841269841e-04f);               // 1/7!
+  p = GS_FMA(r, p, 1.3888888888888889e-03f);               // 1/6!
+  p = GS_FMA(r, p, 8.3333333333333333e-03f);               // 1/5!
+  p = GS_FMA(r, p, 4.1666666666666667e-02f);               // 1/4!
+  p = GS_FMA(r, p, 1.6666666666666667e-01f);               // 1/3!
+  p = GS_FMA(r, p, 0.5f);
+  p = GS_FMA(r, p, 1.0f);
+  p = GS_FMA(r, p, 1.0f);
   return scale2(p, (int)n);
 }
 
@@ -135,10 +146,10 @@ GS_HD float logf_(float x) {
   float s = f / (2.0f + f);
   float z = s * s;
   float q = 9.0909090909090909e-02f;                 // 1/11
-  q = 1.1111111111111111e-01f + z * q;               // 1/9
-  q = 1.4285714285714286e-01f + z * q;               // 1/7
-  q = 2.0000000000000000e-01f + z * q;               // 1/5
-  q = 3.3333333333333333e-01f + z * q;               // 1/3
+  q = GS_FMA(z, q, 1.1111111111111111e-01f);               // 1/9
+  q = GS_FMA(z, q, 1.4285714285714286e-01f);               // 1/7
+  q = GS_FMA(z, q, 2.0000000000000000e-01f);               // 1/5
+  q = GS_FMA(z, q, 3.3333333333333333e-01f);               // 1/3
   q = z * q;
   float lm = f - (f * s - (2.0f * s) * q);
   const float LN2_HI = 0.693145751953125f;
@@ -151,22 +162,22 @@ GS_HD float logf_(float x) {
 GS_HD float sin_poly(float r) {
   float z = r * r;
   float p = -2.5052108385441720e-08f;                // -1/11!
-  p = 2.7557319223985891e-06f + z * p;               // 1/9!
-  p = -1.9841269841269841e-04f + z * p;              // -1/7!
-  p = 8.3333333333333333e-03f + z * p;               // 1/5!
-  p = -1.6666666666666667e-01f + z * p;              // -1/3!
-  return r + (r * z) * p;
+  p = GS_FMA(z, p, 2.7557319223985891e-06f);               // 1/9!
+  p = GS_FMA(z, p, -1.9841269841269841e-04f);              // -1/7!
+  p = GS_FMA(z, p, 8.3333333333333333e-03f);               // 1/5!
+  p = GS_FMA(z, p, -1.6666666666666667e-01f);              // -1/3!
+  return GS_FMA(r * z, p, r);
 }
 
 GS_HD float cos_poly(float r) {
   float z = r * r;
   float p = 2.0876756987868099e-09f;                 // 1/12!
-  p = -2.7557319223985891e-07f + z * p;              // -1/10!
-  p = 2.4801587301587302e-05f + z * p;               // 1/8!
-  p = -1.3888888888888889e-03f + z * p;              // -1/6!
-  p = 4.1666666666666667e-02f + z * p;               // 1/4!
-  p = -0.5f + z * p;
-  return 1.0f + z * p;
+  p = GS_FMA(z, p, -2.7557319223985891e-07f);              // -1/10!
+  p = GS_FMA(z, p, 2.4801587301587302e-05f);               // 1/8!
+  p = GS_FMA(z, p, -1.3888888888888889e-03f);              // -1/6!
+  p = GS_FMA(z, p, 4.1666666666666667e-02f);               // 1/4!
+  p = GS_FMA(z, p, -0.5f);
+  return GS_FMA(z, p, 1.0f);
 }
 
 // Reduce x to r in [-pi/4, pi/4] (approximately) and quadrant q = k mod 4.
@@ -212,16 +223,16 @@ GS_HD float cosf_(float x) {
 GS_HD float atan_poly(float t) {
   float z = t * t;
   float p = 4.7619047619047619e-02f;                 // 1/21
-  p = -5.2631578947368421e-02f + z * p;              // -1/19
-  p = 5.8823529411764706e-02f + z * p;               // 1/17
-  p = -6.6666666666666667e-02f + z * p;              // -1/15
-  p = 7.6923076923076923e-02f + z * p;               // 1/13
-  p = -9.0909090909090909e-02f + z * p;              // -1/11
-  p = 1.1111111111111111e-01f + z * p;               // 1/9
-  p = -1.4285714285714286e-01f + z * p;              // -1/7
-  p = 2.0000000000000000e-01f + z * p;               // 1/5
-  p = -3.3333333333333333e-01f + z * p;              // -1/3
-  return t + (t * z) * p;
+  p = GS_FMA(z, p, -5.2631578947368421e-02f);              // -1/19
+  p = GS_FMA(z, p, 5.8823529411764706e-02f);               // 1/17
+  p = GS_FMA(z, p, -6.6666666666666667e-02f);              // -1/15
+  p = GS_FMA(z, p, 7.6923076923076923e-02f);               // 1/13
+  p = GS_FMA(z, p, -9.0909090909090909e-02f);              // -1/11
+  p = GS_FMA(z, p, 1.1111111111111111e-01f);               // 1/9
+  p = GS_FMA(z, p, -1.4285714285714286e-01f);              // -1/7
+  p = GS_FMA(z, p, 2.0000000000000000e-01f);               // 1/5
+  p = GS_FMA(z, p, -3.3333333333333333e-01f);              // -1/3
+  return GS_FMA(t * z, p, t);
 }
 
 GS_HD float atan2f_(float y, float x) {
