@@ -1,6 +1,6 @@
 // Shared definitions of the CUDA pass: kernel parameter blocks, the per-frame
-// control block, and the decoupled look-back protocol used by the scan,
-// compaction and radix-sort kernels.
+// control block, and the decoupled look-back protocol used by the compaction
+// and scan kernels.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -80,7 +80,7 @@ constexpr uint32_t kScanTile = kBlock * kScanItems;     // items per look-back t
 
 // Per-frame control block, zeroed before each render.
 struct Control {
-  uint32_t tickets[16];          // dynamic tile ids of the look-back kernels
+  uint32_t tickets[2];           // dynamic tile ids of the look-back kernels (Ticket)
   uint32_t depth_hist[kMaxSortPasses][256];  // digit histograms of the depth sort
   uint32_t tile_hist[kMaxSortPasses][256];   // digit histograms of the tile sort
   uint32_t visible_state[4];     // visible, visible, radix blocks, 0
@@ -92,7 +92,7 @@ struct Control {
   uint32_t order_fill[34];
 };
 
-enum Ticket { kTicketCompact = 0, kTicketScan = 1, kTicketSortBase = 2 };
+enum Ticket { kTicketCompact = 0, kTicketScan = 1 };
 
 // ---------------------------------------------------------------------------
 // Decoupled look-back status words: [63:34] epoch, [33:32] flag, [31:0] value.
@@ -191,36 +191,6 @@ __device__ __forceinline__ uint32_t warp_lookback(const unsigned long long* stat
   return excl;
 }
 
-// Per-thread decoupled look-back over a strided status column (one radix
-// digit): W predecessor words are requested at once, so one round trip
-// covers W tiles.
-template <int W>
-__device__ __forceinline__ uint32_t window_lookback(const unsigned long long* column, uint32_t stride, uint32_t tile,
-                                                    uint32_t epoch, uint32_t* err) {
-  uint32_t excl = 0;
-  int64_t end = (int64_t)tile - 1;
-  while (end >= 0) {
-    unsigned long long v[W];
-#pragma unroll
-    for (int w = 0; w < W; ++w) {
-      const int64_t idx = end - w;
-      v[w] = idx >= 0 ? ld_acquire(column + (size_t)idx * stride) : 0ull;
-    }
-#pragma unroll
-    for (int w = 0; w < W; ++w) {
-      const int64_t idx = end - w;
-      if (idx < 0) return excl;
-      bool expired = false;
-      const unsigned long long x = wait_status(column + (size_t)idx * stride, v[w], epoch, err, &expired);
-      if (expired) return excl;
-      excl += (uint32_t)x;
-      if (((x >> 32) & 3ull) == kFlagInclusive) return excl;
-    }
-    end -= W;
-  }
-  return excl;
-}
-
 // ---------------------------------------------------------------------------
 // Block-wide exclusive scan of one value per thread (256 threads).
 template <bool SATURATE>
@@ -276,12 +246,16 @@ void launch_emit(const uint32_t* sorted_ids, uint32_t n_max, const float4* mean,
                  int tile_digit_bits, cudaStream_t st);
 void launch_tile_ranges(const uint32_t* sorted_tile_keys, Control* ctl, uint32_t ntile, uint32_t n_max,
                         uint32_t* tile_offsets, cudaStream_t st);
-// Onesweep LSD pass. n is read from *n_ptr on the device.
-void launch_onesweep(int bits, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
-                     uint32_t* vals_out, const uint32_t* n_ptr, uint32_t n_max, int shift, const uint32_t* hist,
-                     unsigned long long* status, uint32_t* ticket, Epoch epoch, uint32_t* err, cudaStream_t st);
-constexpr uint32_t kSortTile = 4096;  // items per onesweep block
-// Opt every onesweep instantiation into its shared-memory size (once per
+constexpr uint32_t kSortTile = 4096;  // items per sort tile
+// Chunked LSD pass (reduce, scan, scatter; no look-back chain): `chunks`
+// blocks, each walking a contiguous run of 4096-item tiles. counts holds
+// chunks x 2^bits words. n is read from *n_ptr on the device.
+constexpr uint32_t kChunkBlocksPerSm = 3;
+uint32_t chunk_pass_chunks(uint32_t n_max, int sms);
+void launch_chunk_pass(int bits, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
+                       uint32_t* vals_out, const uint32_t* n_ptr, int shift, const uint32_t* hist, uint32_t chunks,
+                       uint32_t* counts, cudaStream_t st);
+// Opt every sort-scatter instantiation into its shared-memory size (once per
 // device; call before any stream capture).
 void prepare_sort_kernels();
 // Raster work list: every tile of the batch, heaviest load class first.

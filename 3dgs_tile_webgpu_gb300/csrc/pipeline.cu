@@ -104,6 +104,8 @@ struct gs3d_pipeline {
   uint32_t* output_state = nullptr;
   unsigned long long* status = nullptr;
   size_t status_words = 0;
+  // Per-(chunk, digit) counts of the chunked sort passes.
+  uint32_t* chunk_counts = nullptr;
   uint32_t epoch = 0;
   // Batch-table staging (bases, view descriptors, object tables), a ring of
   // pinned host buffers each mirrored by a device buffer.
@@ -232,11 +234,11 @@ gs3d_status validate_data(gs3d_pipeline* p, const gs3d_gaussian_data* d) {
   return GS3D_OK;
 }
 
+// Look-back status words of the compaction and the ordered-count scan (one
+// per tile of at least 1024 items).
 size_t status_words_needed(uint32_t slots, uint64_t capacity) {
-  const size_t scan = (slots + 1023u) / 1024u + 1;
-  const size_t sort_slots = ((size_t)slots + kSortTile - 1) / kSortTile * 256 + 256;
-  const size_t sort_caps = (size_t)((capacity + kSortTile - 1) / kSortTile) * 256 + 256;
-  return std::max(scan, std::max(sort_slots, sort_caps));
+  (void)capacity;
+  return (slots + 1023u) / 1024u + 1;
 }
 
 gs3d_status ensure_status(gs3d_pipeline* p) {
@@ -369,6 +371,7 @@ void release_all(gs3d_pipeline* p) {
   dfree(p->dk[0]); dfree(p->dk[1]); dfree(p->dv[0]); dfree(p->dv[1]); dfree(p->ordered); dfree(p->ioff);
   dfree(p->tk[0]); dfree(p->tk[1]); dfree(p->tv[0]); dfree(p->tv[1]);
   dfree(p->tile_offsets); dfree(p->tile_order); dfree(p->ctl); dfree(p->epoch_dev); dfree(p->output_state); dfree(p->status);
+  dfree(p->chunk_counts);
   dfree(p->summary); dfree(p->profile_sums); dfree(p->profile_hist); dfree(p->profile_zero);
 }
 
@@ -435,7 +438,8 @@ gs3d_status gs3d_pipeline_create(const gs3d_pipeline_desc* desc, const gs3d_gaus
   cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, p->device);
   for (uint32_t i = 0; i < kObjectRing; ++i) cudaEventCreateWithFlags(&p->stage_ev[i], cudaEventDisableTiming);
   if ((e = dalloc(p->ctl, 1)) || (e = dalloc(p->output_state, 4)) || (e = dalloc(p->epoch_dev, 1)) ||
-      (e = dalloc(p->summary, 1))) {
+      (e = dalloc(p->summary, 1)) ||
+      (e = dalloc(p->chunk_counts, (size_t)kChunkBlocksPerSm * (size_t)p->sms * 256u))) {
     s = cuda_fail(p, e, "allocating control block");
     release_all(p);
     delete p;
@@ -688,12 +692,12 @@ void record_batch(gs3d_pipeline* p, const Plan& pl, unsigned char* dev, cudaStre
   // Depth sort.
   mark(p, GS3D_STAGE_DEPTH_SORT, st);
   int cur = 0;
+  const uint32_t depth_chunks = chunk_pass_chunks(N, p->sms);
   for (int pass = 0; pass < depth_passes; ++pass) {
-    launch_onesweep(8, p->dk[cur], p->dv[cur], p->dk[cur ^ 1], p->dv[cur ^ 1], &ctl->visible_state[0], N, 8 * pass,
-                    ctl->depth_hist[pass], p->status, &ctl->tickets[kTicketSortBase + pass], epoch(), &ctl->error,
-                    st);
+    launch_chunk_pass(8, p->dk[cur], p->dv[cur], p->dk[cur ^ 1], p->dv[cur ^ 1], &ctl->visible_state[0], 8 * pass,
+                      ctl->depth_hist[pass], depth_chunks, p->chunk_counts, st);
     cur ^= 1;
-    ++launches;
+    launches += 3;
   }
   p->depth_final = cur;
   // Ordered counts + saturating scan + dispatch/output state.
@@ -717,12 +721,12 @@ void record_batch(gs3d_pipeline* p, const Plan& pl, unsigned char* dev, cudaStre
   // Tile sort.
   mark(p, GS3D_STAGE_TILE_SORT, st);
   int tcur = 0;
+  const uint32_t tile_chunks = chunk_pass_chunks(cap32, p->sms);
   for (int pass = 0; pass < tile_passes; ++pass) {
-    launch_onesweep(digit_bits, p->tk[tcur], p->tv[tcur], p->tk[tcur ^ 1], p->tv[tcur ^ 1], &ctl->state[0], cap32,
-                    digit_bits * pass, ctl->tile_hist[pass], p->status, &ctl->tickets[kTicketSortBase + 4 + pass],
-                    epoch(), &ctl->error, st);
+    launch_chunk_pass(digit_bits, p->tk[tcur], p->tv[tcur], p->tk[tcur ^ 1], p->tv[tcur ^ 1], &ctl->state[0],
+                      digit_bits * pass, ctl->tile_hist[pass], tile_chunks, p->chunk_counts, st);
     tcur ^= 1;
-    ++launches;
+    launches += 3;
   }
   p->tile_final = tcur;
   // Tile ranges and the raster work list.

@@ -1,4 +1,4 @@
-// Onesweep-style stable LSD radix sort pass over (uint32 key, uint32 value).
+// Stable LSD radix sort pass over (uint32 key, uint32 value).
 //
 // Replaces the reference's 4-bit, 5-dispatch-per-pass radix sort
 // (src/renderer/kernels/radix.ts:10-263, src/renderer/pipeline/RadixSorter.ts:50-322),
@@ -6,27 +6,34 @@
 // (records enter in ordinal order for the depth sort and in depth-rank order
 // for the tile sort, TiledGaussianPipeline.ts:144,442-446).
 //
-// One pass = one kernel. The digit histograms of every pass were accumulated
-// by the kernel that produced the keys, so each block only:
-//   1. takes the next tile id from an atomic ticket (tiles are processed in
-//      launch order, which keeps the look-back deadlock-free);
-//   2. ranks its 4096 keys per digit within each warp by ballot bit-splitting
-//      (warp-striped layout: item j*32+lane of each warp's 512-item segment,
-//      so ranks follow index order and the sort is stable), while the values
-//      stream into shared memory with cp.async;
-//   3. publishes its per-digit counts and resolves its global per-digit base
-//      with decoupled look-back (one thread per digit, bounded waits);
-//   4. stages keys and values in shared memory in block-sorted order and
-//      writes each digit's run contiguously to global memory.
+// One pass = reduce, scan, scatter with no look-back chain (a single-kernel
+// decoupled look-back pass settles only a window of tiles per L2 round trip,
+// which bounds it far below HBM speed on passes of tens of millions of keys).
+// The items split into `chunks` contiguous runs of whole 4096-item tiles (one
+// split, derived from the device-side count, shared by the three kernels):
+//   k_chunk_count   keys of every (chunk, digit), by shared-memory atomics;
+//   k_chunk_offsets per digit, the exclusive prefix over chunks plus the
+//                   digit's global base from the pass histogram (accumulated
+//                   by the kernel that produced the keys);
+//   k_chunk_scatter one block per chunk walks its tiles in order with running
+//                   per-digit offsets: tile t+1 streams into shared memory by
+//                   cp.async while tile t is ranked per digit within each warp
+//                   by ballot bit-splitting (warp-striped layout: item
+//                   j*32+lane of each warp's 512-item segment, so ranks follow
+//                   index order), staged in place in block-sorted order, and
+//                   written out with each digit's run contiguous.
+// Stable: tiles in index order within a chunk, chunks in index order, ranks in
+// index order within a tile.
 #include <cuda_runtime.h>
 #include <stdint.h>
+
+#include <algorithm>
 
 #include "pass_common.cuh"
 
 namespace gs {
 
 constexpr int kSortWarps = 8;
-constexpr int kSortWindow = 8;  // predecessor tiles requested per look-back round trip, per digit
 constexpr int kSortItems = 16;  // kSortTile = 8 warps * 32 lanes * 16 items
 
 // Lanes of the warp holding the same BITS-bit digit, by ballot bit-splitting.
@@ -51,151 +58,239 @@ __device__ __forceinline__ void cp_async_commit_wait() {
   asm volatile("cp.async.wait_all;" ::: "memory");
 }
 
+// Tiles [t0, t1) of chunk c when n items split over `chunks` chunks.
+__device__ __forceinline__ void chunk_tiles(uint32_t n, uint32_t chunks, uint32_t c, uint32_t* t0, uint32_t* t1) {
+  const uint32_t tiles = (uint32_t)(((uint64_t)n + kSortTile - 1) / kSortTile);
+  const uint32_t per = (tiles + chunks - 1) / chunks;
+  *t0 = min(c * per, tiles);
+  *t1 = min(*t0 + per, tiles);
+}
+
+template <int BITS>
+__global__ void __launch_bounds__(kBlock) k_chunk_count(const uint32_t* __restrict__ keys,
+                                                        const uint32_t* __restrict__ n_ptr, int shift,
+                                                        uint32_t chunks, uint32_t* __restrict__ counts) {
+  constexpr uint32_t RADIX = 1u << BITS;
+  constexpr uint32_t MASK = RADIX - 1u;
+  __shared__ uint32_t s_hist[kSortWarps][RADIX];
+  const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+  for (uint32_t i = tid; i < kSortWarps * RADIX; i += kBlock) (&s_hist[0][0])[i] = 0u;
+  __syncthreads();
+  const uint32_t n = *n_ptr;
+  uint32_t t0, t1;
+  chunk_tiles(n, chunks, blockIdx.x, &t0, &t1);
+  const uint32_t begin = (uint32_t)min((uint64_t)t0 * kSortTile, (uint64_t)n);
+  const uint32_t end = (uint32_t)min((uint64_t)t1 * kSortTile, (uint64_t)n);
+  const uint32_t lt = (1u << lane) - 1u;
+  // Each warp takes 512-key runs: four 16-byte loads per lane in flight
+  // before any counting (begin is a multiple of 4096, so they are aligned).
+  constexpr uint32_t kRun = 512u;
+  for (uint32_t s = begin + warp * kRun; s < end; s += kSortWarps * kRun) {
+    uint32_t kk[16];
+#pragma unroll
+    for (uint32_t q = 0; q < 4u; ++q) {
+      const uint32_t i0 = s + q * 128u + 4u * lane;
+      if (i0 + 4u <= end) {
+        const uint4 v = *reinterpret_cast<const uint4*>(keys + i0);
+        kk[4 * q] = v.x; kk[4 * q + 1] = v.y; kk[4 * q + 2] = v.z; kk[4 * q + 3] = v.w;
+      } else {
+#pragma unroll
+        for (uint32_t e = 0; e < 4u; ++e) kk[4 * q + e] = i0 + e < end ? keys[i0 + e] : 0u;
+      }
+    }
+#pragma unroll
+    for (uint32_t q = 0; q < 16u; ++q) {
+      const bool ok = s + (q >> 2) * 128u + 4u * lane + (q & 3u) < end;
+      const uint32_t d = (kk[q] >> shift) & MASK;
+      const uint32_t d0 = __shfl_sync(0xffffffffu, d, 0);
+      if (__all_sync(0xffffffffu, ok && d == d0)) {
+        if (lane == 0u) atomicAdd(&s_hist[warp][d0], 32u);
+      } else if (ok) {
+        atomicAdd(&s_hist[warp][d], 1u);
+      }
+    }
+  }
+  __syncthreads();
+  for (uint32_t d = tid; d < RADIX; d += kBlock) {
+    uint32_t sum = 0;
+#pragma unroll
+    for (int w = 0; w < kSortWarps; ++w) sum += s_hist[w][d];
+    counts[(size_t)blockIdx.x * RADIX + d] = sum;
+  }
+}
+
+// One block per digit; counts[c][d] becomes the global position of the first
+// key of digit d in chunk c.
+template <int BITS>
+__global__ void __launch_bounds__(kBlock) k_chunk_offsets(const uint32_t* __restrict__ hist, uint32_t chunks,
+                                                          uint32_t* __restrict__ counts) {
+  constexpr uint32_t RADIX = 1u << BITS;
+  __shared__ uint32_t s_scan[kBlock / 32];
+  const uint32_t tid = threadIdx.x, d = blockIdx.x;
+  uint32_t base;
+  block_exclusive_scan<false>(tid < d ? hist[tid] : 0u, s_scan, &base);  // keys of the digits below d
+  const uint32_t per = (chunks + kBlock - 1) / kBlock;
+  const uint32_t c0 = min(tid * per, chunks), c1 = min(c0 + per, chunks);
+  uint32_t local = 0;
+  for (uint32_t c = c0; c < c1; ++c) local += counts[(size_t)c * RADIX + d];
+  uint32_t total;
+  uint32_t run = base + block_exclusive_scan<false>(local, s_scan, &total);
+  for (uint32_t c = c0; c < c1; ++c) {
+    const uint32_t v = counts[(size_t)c * RADIX + d];
+    counts[(size_t)c * RADIX + d] = run;
+    run += v;
+  }
+}
+
+// Issues the cp.async copies of one tile's keys and values into shared
+// memory (the ragged end with plain loads) and commits them as one group.
+__device__ __forceinline__ void load_tile_async(const uint32_t* __restrict__ keys_in,
+                                                const uint32_t* __restrict__ vals_in, uint32_t base, uint32_t n,
+                                                uint32_t* kb, uint32_t* vb) {
+  for (uint32_t c = threadIdx.x; c < kSortTile / 4u; c += kBlock) {
+    const uint32_t first = base + 4u * c;
+    if (first + 4u <= n) {
+      cp_async16(kb + 4u * c, keys_in + first);
+      cp_async16(vb + 4u * c, vals_in + first);
+    } else {
+      for (uint32_t e = 0; e < 4u; ++e)
+        if (first + e < n) {
+          kb[4u * c + e] = keys_in[first + e];
+          vb[4u * c + e] = vals_in[first + e];
+        }
+    }
+  }
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+template <int N>
+__device__ __forceinline__ void cp_async_wait_group() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+constexpr size_t kChunkDynSmem = 4 * kSortTile * sizeof(uint32_t);
+
 template <int BITS>
 __global__ void __launch_bounds__(kBlock, 3)
-    k_onesweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
-               uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, const uint32_t* __restrict__ n_ptr,
-               int shift, const uint32_t* __restrict__ hist, unsigned long long* __restrict__ status,
-               uint32_t* __restrict__ ticket, Epoch ep, uint32_t* __restrict__ err) {
+    k_chunk_scatter(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
+                    uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
+                    const uint32_t* __restrict__ n_ptr, int shift, uint32_t chunks,
+                    const uint32_t* __restrict__ offsets) {
   constexpr uint32_t RADIX = 1u << BITS;
   constexpr uint32_t MASK = RADIX - 1u;
   __shared__ uint32_t s_warp_hist[kSortWarps][RADIX];
   __shared__ uint32_t s_block_excl[RADIX];
-  __shared__ uint32_t s_global_base[RADIX];
-  __shared__ uint32_t s_hist_excl[RADIX];
-  extern __shared__ uint4 s_dyn[];  // keys, values, raw values: 3 x kSortTile words
-  uint32_t* s_keys = reinterpret_cast<uint32_t*>(s_dyn);
-  uint32_t* s_vals = s_keys + kSortTile;
-  uint32_t* s_vraw = s_vals + kSortTile;
+  __shared__ uint32_t s_run[RADIX];
   __shared__ uint32_t s_scan[kBlock / 32];
-  __shared__ uint32_t s_tile;
+  // Two tile buffers (keys, values): tile t+1 streams in while tile t is
+  // ranked and scattered; each tile is staged in place in its own buffer.
+  extern __shared__ uint4 s_dyn[];
+  uint32_t* s_buf = reinterpret_cast<uint32_t*>(s_dyn);
 
   const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-  if (tid == 0) s_tile = atomicAdd(ticket, 1u);
-  for (uint32_t i = tid; i < kSortWarps * RADIX; i += kBlock) (&s_warp_hist[0][0])[i] = 0u;
-  __syncthreads();
   const uint32_t n = *n_ptr;
-  const uint32_t tile = s_tile;
-  const uint32_t base = tile * kSortTile;
-  if (base >= n) return;
-  const uint32_t epoch = ep.get();
-  const uint32_t wbase = base + warp * 32u * kSortItems;
-
-  // Keys into registers (warp-striped: item j*32+lane of the warp's
-  // segment); values into shared memory asynchronously, in the same order.
-  uint32_t k[kSortItems];
-#pragma unroll
-  for (int j = 0; j < kSortItems; ++j) {
-    const uint32_t idx = wbase + (uint32_t)j * 32u + lane;
-    k[j] = idx < n ? keys_in[idx] : 0u;
-  }
-  uint32_t* vraw = s_vraw + warp * 32u * kSortItems;
-  for (uint32_t c = lane; c < 8u * kSortItems; c += 32u) {
-    const uint32_t first = wbase + 4u * c;
-    if (first + 4u <= n) {
-      cp_async16(vraw + 4u * c, vals_in + first);
-    } else {
-      for (uint32_t e = 0; e < 4u; ++e)
-        if (first + e < n) vraw[4u * c + e] = vals_in[first + e];
-    }
-  }
-
-  // Exclusive scan of the pass's global digit histogram.
-  {
-    const uint32_t h = tid < RADIX ? hist[tid] : 0u;
-    uint32_t tot;
-    const uint32_t e = block_exclusive_scan<false>(h, s_scan, &tot);
-    if (tid < RADIX) s_hist_excl[tid] = e;
-  }
-
-  // Rank: position among equal digits of this warp, in index order.
+  uint32_t t0, t1;
+  chunk_tiles(n, chunks, blockIdx.x, &t0, &t1);
+  if (t0 >= t1) return;
+  load_tile_async(keys_in, vals_in, t0 * kSortTile, n, s_buf, s_buf + kSortTile);
+  if (tid < RADIX) s_run[tid] = offsets[(size_t)blockIdx.x * RADIX + tid];
+  for (uint32_t i = tid; i < kSortWarps * RADIX; i += kBlock) (&s_warp_hist[0][0])[i] = 0u;
   const uint32_t lt = (1u << lane) - 1u;
-  uint32_t rank[kSortItems];
-#pragma unroll
-  for (int j = 0; j < kSortItems; ++j) {
-    const uint32_t idx = wbase + (uint32_t)j * 32u + lane;
-    const bool ok = idx < n;
-    const uint32_t valid = __ballot_sync(0xffffffffu, ok);
-    const uint32_t d = (k[j] >> shift) & MASK;
-    const uint32_t peers = match_digit<BITS>(d, valid);
-    const uint32_t before = __popc(peers & lt);
-    uint32_t cnt = 0;
-    if (ok) cnt = s_warp_hist[warp][d];
-    rank[j] = cnt + before;
-    __syncwarp();
-    if (ok && before == 0) s_warp_hist[warp][d] = cnt + __popc(peers);
-    __syncwarp();
-  }
-  __syncthreads();
 
-  // Per digit: exclusive offsets across warps and the block count; publish.
-  uint32_t block_count = 0;
-  if (tid < RADIX) {
-#pragma unroll
-    for (int w = 0; w < kSortWarps; ++w) {
-      const uint32_t c = s_warp_hist[w][tid];
-      s_warp_hist[w][tid] = block_count;
-      block_count += c;
+  for (uint32_t t = t0; t < t1; ++t) {
+    uint32_t* kb = s_buf + ((t - t0) & 1u) * 2u * kSortTile;
+    uint32_t* vb = kb + kSortTile;
+    if (t + 1u < t1) {
+      uint32_t* nb = s_buf + (((t - t0) & 1u) ^ 1u) * 2u * kSortTile;
+      load_tile_async(keys_in, vals_in, (t + 1u) * kSortTile, n, nb, nb + kSortTile);
+      cp_async_wait_group<1>();
+    } else {
+      cp_async_wait_group<0>();
     }
-    unsigned long long* mine = status + (size_t)tile * RADIX + tid;
-    st_release(mine, pack_status(epoch, tile == 0 ? kFlagInclusive : kFlagAggregate, block_count));
-  }
-  {
-    uint32_t tot;
-    const uint32_t e = block_exclusive_scan<false>(tid < RADIX ? block_count : 0u, s_scan, &tot);
-    if (tid < RADIX) s_block_excl[tid] = e;
-  }
-  cp_async_commit_wait();
-  __syncthreads();
-
-  // Stage keys and values in block-sorted order (block-local prefixes only),
-  // so the keys and ranks leave registers before the look-back.
+    __syncthreads();
+    const uint32_t base = t * kSortTile;
+    const uint32_t wofs = warp * 32u * kSortItems;  // warp-striped: item j*32+lane of the warp's segment
+    uint32_t k[kSortItems], rank[kSortItems];
 #pragma unroll
-  for (int j = 0; j < kSortItems; ++j) {
-    const uint32_t idx = wbase + (uint32_t)j * 32u + lane;
-    if (idx < n) {
+    for (int j = 0; j < kSortItems; ++j) k[j] = kb[wofs + (uint32_t)j * 32u + lane];
+#pragma unroll
+    for (int j = 0; j < kSortItems; ++j) {
+      const bool ok = base + wofs + (uint32_t)j * 32u + lane < n;
+      const uint32_t valid = __ballot_sync(0xffffffffu, ok);
       const uint32_t d = (k[j] >> shift) & MASK;
-      const uint32_t pos = s_block_excl[d] + s_warp_hist[warp][d] + rank[j];
-      s_keys[pos] = k[j];
-      s_vals[pos] = vraw[(uint32_t)j * 32u + lane];
+      const uint32_t peers = match_digit<BITS>(d, valid);
+      const uint32_t before = __popc(peers & lt);
+      uint32_t cnt = 0;
+      if (ok) cnt = s_warp_hist[warp][d];
+      rank[j] = cnt + before;
+      __syncwarp();
+      if (ok && before == 0) s_warp_hist[warp][d] = cnt + __popc(peers);
+      __syncwarp();
     }
-  }
+    __syncthreads();
 
-  // Global base of every digit: decoupled look-back over the predecessors.
-  if (tid < RADIX) {
-    uint32_t prefix = 0;
-    if (tile > 0) {
-      prefix = window_lookback<kSortWindow>(status + tid, RADIX, tile, epoch, err);
-      st_release(status + (size_t)tile * RADIX + tid, pack_status(epoch, kFlagInclusive, prefix + block_count));
+    uint32_t block_count = 0;
+    if (tid < RADIX) {
+#pragma unroll
+      for (int w = 0; w < kSortWarps; ++w) {
+        const uint32_t c = s_warp_hist[w][tid];
+        s_warp_hist[w][tid] = block_count;
+        block_count += c;
+      }
     }
-    s_global_base[tid] = s_hist_excl[tid] + prefix;
-  }
-  __syncthreads();
+    {
+      uint32_t tot;
+      const uint32_t e = block_exclusive_scan<false>(tid < RADIX ? block_count : 0u, s_scan, &tot);
+      if (tid < RADIX) s_block_excl[tid] = e;
+    }
+    __syncthreads();
 
-  // Scatter: consecutive positions of one digit go to consecutive addresses.
-  const uint32_t count = min(kSortTile, n - base);
-  for (uint32_t i = tid; i < count; i += kBlock) {
-    const uint32_t key = s_keys[i];
-    const uint32_t dig = (key >> shift) & MASK;
-    const uint32_t dst = s_global_base[dig] + (i - s_block_excl[dig]);
-    keys_out[dst] = key;
-    vals_out[dst] = s_vals[i];
+    // Keys first (every raw key is already in registers), then the values
+    // (read raw into registers, then written once every thread has read).
+#pragma unroll
+    for (int j = 0; j < kSortItems; ++j) {
+      if (base + wofs + (uint32_t)j * 32u + lane < n) {
+        const uint32_t d = (k[j] >> shift) & MASK;
+        rank[j] += s_block_excl[d] + s_warp_hist[warp][d];
+        kb[rank[j]] = k[j];
+      }
+    }
+    uint32_t v[kSortItems];
+#pragma unroll
+    for (int j = 0; j < kSortItems; ++j) v[j] = vb[wofs + (uint32_t)j * 32u + lane];
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < kSortItems; ++j)
+      if (base + wofs + (uint32_t)j * 32u + lane < n) vb[rank[j]] = v[j];
+    __syncthreads();
+
+    const uint32_t count = min(kSortTile, n - base);
+    for (uint32_t i = tid; i < count; i += kBlock) {
+      const uint32_t key = kb[i];
+      const uint32_t dig = (key >> shift) & MASK;
+      const uint32_t dst = s_run[dig] + (i - s_block_excl[dig]);
+      keys_out[dst] = key;
+      vals_out[dst] = vb[i];
+    }
+    for (uint32_t i = tid; i < kSortWarps * RADIX; i += kBlock) (&s_warp_hist[0][0])[i] = 0u;
+    __syncthreads();
+    if (tid < RADIX) s_run[tid] += block_count;
   }
 }
 
-constexpr size_t kSortDynSmem = 3 * kSortTile * sizeof(uint32_t);
-
 template <int B>
-void launch_bits(uint32_t grid, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
-                 uint32_t* vals_out, const uint32_t* n_ptr, int shift, const uint32_t* hist,
-                 unsigned long long* status, uint32_t* ticket, Epoch epoch, uint32_t* err, cudaStream_t st) {
-  k_onesweep<B><<<grid, kBlock, kSortDynSmem, st>>>(keys_in, vals_in, keys_out, vals_out, n_ptr, shift, hist, status,
-                                                    ticket, epoch, err);
+void launch_chunk_bits(uint32_t chunks, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
+                       uint32_t* vals_out, const uint32_t* n_ptr, int shift, const uint32_t* hist, uint32_t* counts,
+                       cudaStream_t st) {
+  k_chunk_count<B><<<chunks, kBlock, 0, st>>>(keys_in, n_ptr, shift, chunks, counts);
+  k_chunk_offsets<B><<<1u << B, kBlock, 0, st>>>(hist, chunks, counts);
+  k_chunk_scatter<B><<<chunks, kBlock, kChunkDynSmem, st>>>(keys_in, vals_in, keys_out, vals_out, n_ptr, shift,
+                                                           chunks, counts);
 }
 
 template <int B>
 void configure_bits() {
-  cudaFuncSetAttribute(k_onesweep<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSortDynSmem);
+  cudaFuncSetAttribute(k_chunk_scatter<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kChunkDynSmem);
 }
 
 void prepare_sort_kernels() {
@@ -203,27 +298,30 @@ void prepare_sort_kernels() {
   configure_bits<5>(); configure_bits<6>(); configure_bits<7>(); configure_bits<8>();
 }
 
-void launch_onesweep(int bits, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
-                     uint32_t* vals_out, const uint32_t* n_ptr, uint32_t n_max, int shift, const uint32_t* hist,
-                     unsigned long long* status, uint32_t* ticket, Epoch epoch, uint32_t* err, cudaStream_t st) {
-  const uint32_t grid = n_max == 0 ? 1u : (uint32_t)(((uint64_t)n_max + kSortTile - 1) / kSortTile);
-#define GS_SWEEP(B)                                                                                      \
-  case B:                                                                                                \
-    launch_bits<B>(grid, keys_in, vals_in, keys_out, vals_out, n_ptr, shift, hist, status, ticket, epoch, \
-                   err, st);                                                                             \
+uint32_t chunk_pass_chunks(uint32_t n_max, int sms) {
+  const uint64_t tiles = ((uint64_t)n_max + kSortTile - 1) / kSortTile;
+  return (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(tiles, (uint64_t)kChunkBlocksPerSm * (uint64_t)sms));
+}
+
+void launch_chunk_pass(int bits, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
+                       uint32_t* vals_out, const uint32_t* n_ptr, int shift, const uint32_t* hist, uint32_t chunks,
+                       uint32_t* counts, cudaStream_t st) {
+#define GS_CHUNK(B)                                                                                             \
+  case B:                                                                                                       \
+    launch_chunk_bits<B>(chunks, keys_in, vals_in, keys_out, vals_out, n_ptr, shift, hist, counts, st);         \
     break;
   switch (bits) {
-    GS_SWEEP(1)
-    GS_SWEEP(2)
-    GS_SWEEP(3)
-    GS_SWEEP(4)
-    GS_SWEEP(5)
-    GS_SWEEP(6)
-    GS_SWEEP(7)
+    GS_CHUNK(1)
+    GS_CHUNK(2)
+    GS_CHUNK(3)
+    GS_CHUNK(4)
+    GS_CHUNK(5)
+    GS_CHUNK(6)
+    GS_CHUNK(7)
     default:
-      GS_SWEEP(8)
+      GS_CHUNK(8)
   }
-#undef GS_SWEEP
+#undef GS_CHUNK
 }
 
 }  // namespace gs
