@@ -168,113 +168,141 @@ __device__ __forceinline__ void cp_async_wait_group() {
   asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
-constexpr size_t kChunkDynSmem = 4 * kSortTile * sizeof(uint32_t);
+// Tile buffers of the scatter (keys and values each): with two, tile t+1
+// streams in while tile t is ranked and scattered.
+constexpr int kScatterBuffers = 2;
+constexpr size_t kChunkDynSmem = 2 * kScatterBuffers * kSortTile * sizeof(uint32_t);
 
 template <int BITS>
-__global__ void __launch_bounds__(kBlock, 3)
+struct ScatterShared {
+  uint32_t warp_hist[kSortWarps][1u << BITS];
+  uint32_t block_excl[1u << BITS];
+  uint32_t run[1u << BITS];  // global position of the next key of each digit
+  uint32_t scan[kBlock / 32];
+};
+
+// Ranks the tile held in kb/vb (items base .. base + 4096, those below n),
+// stages it in place in block-sorted order and writes each digit's run to its
+// global position. FULL: every item of the tile is below n. Leaves warp_hist
+// zeroed and run advanced past the tile.
+template <int BITS, bool FULL>
+__device__ __forceinline__ void scatter_tile(ScatterShared<BITS>& sm, uint32_t* kb, uint32_t* vb, uint32_t base,
+                                             uint32_t n, int shift, uint32_t* __restrict__ keys_out,
+                                             uint32_t* __restrict__ vals_out) {
+  constexpr uint32_t RADIX = 1u << BITS;
+  constexpr uint32_t MASK = RADIX - 1u;
+  const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+  const uint32_t lt = (1u << lane) - 1u;
+  const uint32_t wofs = warp * 32u * kSortItems;  // warp-striped: item j*32+lane of the warp's segment
+  uint32_t k[kSortItems], rank[kSortItems];
+#pragma unroll
+  for (int j = 0; j < kSortItems; ++j) k[j] = kb[wofs + (uint32_t)j * 32u + lane];
+#pragma unroll
+  for (int j = 0; j < kSortItems; ++j) {
+    const bool ok = FULL || base + wofs + (uint32_t)j * 32u + lane < n;
+    const uint32_t valid = FULL ? 0xffffffffu : __ballot_sync(0xffffffffu, ok);
+    const uint32_t d = (k[j] >> shift) & MASK;
+    const uint32_t peers = match_digit<BITS>(d, valid);
+    const uint32_t before = __popc(peers & lt);
+    uint32_t cnt = 0;
+    if (ok) cnt = sm.warp_hist[warp][d];
+    rank[j] = cnt + before;
+    __syncwarp();
+    if (ok && before == 0) sm.warp_hist[warp][d] = cnt + __popc(peers);
+    __syncwarp();
+  }
+  __syncthreads();
+
+  uint32_t block_count = 0;
+  if (tid < RADIX) {
+#pragma unroll
+    for (int w = 0; w < kSortWarps; ++w) {
+      const uint32_t c = sm.warp_hist[w][tid];
+      sm.warp_hist[w][tid] = block_count;
+      block_count += c;
+    }
+  }
+  {
+    uint32_t tot;
+    const uint32_t e = block_exclusive_scan<false>(tid < RADIX ? block_count : 0u, sm.scan, &tot);
+    if (tid < RADIX) sm.block_excl[tid] = e;
+  }
+  __syncthreads();
+
+  // Keys first (every raw key is already in registers), then the values
+  // (read raw into registers, then written once every thread has read).
+#pragma unroll
+  for (int j = 0; j < kSortItems; ++j) {
+    if (FULL || base + wofs + (uint32_t)j * 32u + lane < n) {
+      const uint32_t d = (k[j] >> shift) & MASK;
+      rank[j] += sm.block_excl[d] + sm.warp_hist[warp][d];
+      kb[rank[j]] = k[j];
+    }
+  }
+  uint32_t v[kSortItems];
+#pragma unroll
+  for (int j = 0; j < kSortItems; ++j) v[j] = vb[wofs + (uint32_t)j * 32u + lane];
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < kSortItems; ++j)
+    if (FULL || base + wofs + (uint32_t)j * 32u + lane < n) vb[rank[j]] = v[j];
+  __syncthreads();
+
+  const uint32_t count = FULL ? kSortTile : min(kSortTile, n - base);
+#pragma unroll 4
+  for (uint32_t i = tid; i < count; i += kBlock) {
+    const uint32_t key = kb[i];
+    const uint32_t dig = (key >> shift) & MASK;
+    const uint32_t dst = sm.run[dig] + (i - sm.block_excl[dig]);
+    keys_out[dst] = key;
+    vals_out[dst] = vb[i];
+  }
+  for (uint32_t i = tid; i < kSortWarps * RADIX; i += kBlock) (&sm.warp_hist[0][0])[i] = 0u;
+  __syncthreads();
+  if (tid < RADIX) sm.run[tid] += block_count;
+}
+
+template <int BITS>
+__global__ void __launch_bounds__(kBlock, kChunkBlocksPerSm)
     k_chunk_scatter(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
                     uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
                     const uint32_t* __restrict__ n_ptr, int shift, uint32_t chunks,
                     const uint32_t* __restrict__ offsets) {
   constexpr uint32_t RADIX = 1u << BITS;
-  constexpr uint32_t MASK = RADIX - 1u;
-  __shared__ uint32_t s_warp_hist[kSortWarps][RADIX];
-  __shared__ uint32_t s_block_excl[RADIX];
-  __shared__ uint32_t s_run[RADIX];
-  __shared__ uint32_t s_scan[kBlock / 32];
-  // Two tile buffers (keys, values): tile t+1 streams in while tile t is
-  // ranked and scattered; each tile is staged in place in its own buffer.
+  __shared__ ScatterShared<BITS> sm;
   extern __shared__ uint4 s_dyn[];
   uint32_t* s_buf = reinterpret_cast<uint32_t*>(s_dyn);
 
-  const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+  const uint32_t tid = threadIdx.x;
   const uint32_t n = *n_ptr;
   uint32_t t0, t1;
   chunk_tiles(n, chunks, blockIdx.x, &t0, &t1);
   if (t0 >= t1) return;
-  load_tile_async(keys_in, vals_in, t0 * kSortTile, n, s_buf, s_buf + kSortTile);
-  if (tid < RADIX) s_run[tid] = offsets[(size_t)blockIdx.x * RADIX + tid];
-  for (uint32_t i = tid; i < kSortWarps * RADIX; i += kBlock) (&s_warp_hist[0][0])[i] = 0u;
-  const uint32_t lt = (1u << lane) - 1u;
+  if (kScatterBuffers == 2) load_tile_async(keys_in, vals_in, t0 * kSortTile, n, s_buf, s_buf + kSortTile);
+  if (tid < RADIX) sm.run[tid] = offsets[(size_t)blockIdx.x * RADIX + tid];
+  for (uint32_t i = tid; i < kSortWarps * RADIX; i += kBlock) (&sm.warp_hist[0][0])[i] = 0u;
 
   for (uint32_t t = t0; t < t1; ++t) {
-    uint32_t* kb = s_buf + ((t - t0) & 1u) * 2u * kSortTile;
+    uint32_t* kb = s_buf + (kScatterBuffers == 2 ? ((t - t0) & 1u) : 0u) * 2u * kSortTile;
     uint32_t* vb = kb + kSortTile;
-    if (t + 1u < t1) {
-      uint32_t* nb = s_buf + (((t - t0) & 1u) ^ 1u) * 2u * kSortTile;
-      load_tile_async(keys_in, vals_in, (t + 1u) * kSortTile, n, nb, nb + kSortTile);
-      cp_async_wait_group<1>();
+    if (kScatterBuffers == 2) {
+      if (t + 1u < t1) {
+        uint32_t* nb = s_buf + (((t - t0) & 1u) ^ 1u) * 2u * kSortTile;
+        load_tile_async(keys_in, vals_in, (t + 1u) * kSortTile, n, nb, nb + kSortTile);
+        cp_async_wait_group<1>();
+      } else {
+        cp_async_wait_group<0>();
+      }
     } else {
+      load_tile_async(keys_in, vals_in, t * kSortTile, n, kb, vb);
       cp_async_wait_group<0>();
     }
     __syncthreads();
     const uint32_t base = t * kSortTile;
-    const uint32_t wofs = warp * 32u * kSortItems;  // warp-striped: item j*32+lane of the warp's segment
-    uint32_t k[kSortItems], rank[kSortItems];
-#pragma unroll
-    for (int j = 0; j < kSortItems; ++j) k[j] = kb[wofs + (uint32_t)j * 32u + lane];
-#pragma unroll
-    for (int j = 0; j < kSortItems; ++j) {
-      const bool ok = base + wofs + (uint32_t)j * 32u + lane < n;
-      const uint32_t valid = __ballot_sync(0xffffffffu, ok);
-      const uint32_t d = (k[j] >> shift) & MASK;
-      const uint32_t peers = match_digit<BITS>(d, valid);
-      const uint32_t before = __popc(peers & lt);
-      uint32_t cnt = 0;
-      if (ok) cnt = s_warp_hist[warp][d];
-      rank[j] = cnt + before;
-      __syncwarp();
-      if (ok && before == 0) s_warp_hist[warp][d] = cnt + __popc(peers);
-      __syncwarp();
-    }
-    __syncthreads();
-
-    uint32_t block_count = 0;
-    if (tid < RADIX) {
-#pragma unroll
-      for (int w = 0; w < kSortWarps; ++w) {
-        const uint32_t c = s_warp_hist[w][tid];
-        s_warp_hist[w][tid] = block_count;
-        block_count += c;
-      }
-    }
-    {
-      uint32_t tot;
-      const uint32_t e = block_exclusive_scan<false>(tid < RADIX ? block_count : 0u, s_scan, &tot);
-      if (tid < RADIX) s_block_excl[tid] = e;
-    }
-    __syncthreads();
-
-    // Keys first (every raw key is already in registers), then the values
-    // (read raw into registers, then written once every thread has read).
-#pragma unroll
-    for (int j = 0; j < kSortItems; ++j) {
-      if (base + wofs + (uint32_t)j * 32u + lane < n) {
-        const uint32_t d = (k[j] >> shift) & MASK;
-        rank[j] += s_block_excl[d] + s_warp_hist[warp][d];
-        kb[rank[j]] = k[j];
-      }
-    }
-    uint32_t v[kSortItems];
-#pragma unroll
-    for (int j = 0; j < kSortItems; ++j) v[j] = vb[wofs + (uint32_t)j * 32u + lane];
-    __syncthreads();
-#pragma unroll
-    for (int j = 0; j < kSortItems; ++j)
-      if (base + wofs + (uint32_t)j * 32u + lane < n) vb[rank[j]] = v[j];
-    __syncthreads();
-
-    const uint32_t count = min(kSortTile, n - base);
-    for (uint32_t i = tid; i < count; i += kBlock) {
-      const uint32_t key = kb[i];
-      const uint32_t dig = (key >> shift) & MASK;
-      const uint32_t dst = s_run[dig] + (i - s_block_excl[dig]);
-      keys_out[dst] = key;
-      vals_out[dst] = vb[i];
-    }
-    for (uint32_t i = tid; i < kSortWarps * RADIX; i += kBlock) (&s_warp_hist[0][0])[i] = 0u;
-    __syncthreads();
-    if (tid < RADIX) s_run[tid] += block_count;
+    if ((uint64_t)base + kSortTile <= n)
+      scatter_tile<BITS, true>(sm, kb, vb, base, n, shift, keys_out, vals_out);
+    else
+      scatter_tile<BITS, false>(sm, kb, vb, base, n, shift, keys_out, vals_out);
   }
 }
 
