@@ -27,7 +27,7 @@ struct ViewDesc {
   uint32_t count, active, degree, C;
   uint32_t object_count, color_half;
   uint32_t tiles_x, tiles_y;
-  uint32_t item_base, tile_base, block_base, pad0;
+  uint32_t item_base, tile_base, pad0, pad1;
   float P[16];             // projection, column-major
   float vw, vh, vnear, vfar;
 };
@@ -49,19 +49,23 @@ struct PassOptions {
   uint32_t proj_fp64;      // 1: FP64 far-origin mean transform and near-singular conic
 };
 
-// The batch table in device memory: three ascending base arrays (nviews + 1
-// entries each, the last one the total) followed by the view descriptors and
-// the per-frame parameters (attempt, reset_valid).
+// The batch table in device memory: the per-frame parameters (attempt,
+// reset_valid), four ascending arrays (nviews + 1 entries each), then the view
+// descriptors. Consecutive views that render the same packed scene form a view
+// group, projected together (group_block: first projection block of each
+// group; group_view: first view of each group; ngroups + 1 entries used).
 struct BatchView {
   const uint32_t* item_base;
   const uint32_t* tile_base;
-  const uint32_t* block_base;
+  const uint32_t* group_block;
+  const uint32_t* group_view;
   const ViewDesc* views;
   const uint32_t* frame_params;  // attempt, reset_valid
   uint32_t nviews;
+  uint32_t ngroups;
   uint32_t total_items;
   uint32_t total_tiles;
-  uint32_t total_blocks;
+  uint32_t total_blocks;         // projection blocks over the groups
 };
 
 // Index of the view whose [base[v], base[v+1]) range holds x.

@@ -14,11 +14,13 @@ namespace gs {
 
 // ---------------------------------------------------------------------------
 // K1: decode + project + cull + SH + tile count, one thread per active ordinal
-// of every view (ProjectionStage.ts:385-649). Writes the projected
-// mean/conic/colour/count like the reference, plus the depth sort key (or
-// kInvisibleKey), which the compaction consumes instead of re-reading the
-// 16-byte means. Each block belongs to one view; the padding items after a
-// view's last ordinal are written as invisible.
+// of every view group (ProjectionStage.ts:385-649): consecutive views of a
+// batch that render the same packed scene form a group, and each thread
+// decodes its splat once and projects it into every view of the group. Writes
+// the projected mean/conic/colour/count like the reference, plus the depth
+// sort key (or kInvisibleKey), which the compaction consumes instead of
+// re-reading the 16-byte means. Each block belongs to one group; the padding
+// items after a view's last ordinal are written as invisible.
 __device__ __forceinline__ void load_sh(const uint32_t* __restrict__ p, uint32_t degree, uint32_t* co) {
   if (degree == 3) {
     const uint4* v = reinterpret_cast<const uint4*>(p);
@@ -95,155 +97,192 @@ __device__ __forceinline__ uint32_t count_tiles_warp(CountShared& sm, uint32_t n
   return sm.cnt[warp][lane];
 }
 
-template <bool FP64>
+// GROUPED: some group holds several views (decode once, before the view
+// loop); otherwise every group is one view and the decode stays inside the
+// per-view chain, after the object tests, where it costs fewest registers.
+template <bool FP64, bool GROUPED>
 __global__ void __launch_bounds__(kBlock, 4) k_project(BatchView b, PassOptions o, float4* __restrict__ mean_out,
                                                     float4* __restrict__ conic_out, float4* __restrict__ color_out,
                                                     uint32_t* __restrict__ count_out, uint32_t* __restrict__ key_out,
                                                     float4* __restrict__ rec_out) {
   __shared__ float s_snorm[256];
-  __shared__ uint32_t s_view;
+  __shared__ uint32_t s_group;
   __shared__ CountShared s_count;
   s_snorm[threadIdx.x] = snorm8_value(threadIdx.x);
-  if (threadIdx.x == 0) s_view = find_view(b.block_base, b.nviews, blockIdx.x);
+  if (threadIdx.x == 0) s_group = find_view(b.group_block, b.ngroups, blockIdx.x);
   __syncthreads();
-  const ViewDesc& v = b.views[s_view];
+  const uint32_t g = s_group;
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-  const uint32_t gid = (blockIdx.x - v.block_base) * kBlock + threadIdx.x;  // ordinal within the view
-  const uint32_t item = v.item_base + gid;
-  const float vw = v.vw, vh = v.vh;
-  float4 mo4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-  uint32_t cnt = 0, key = kInvisibleKey, nbox = 0, slot = 0;
-  Projected pr = {};
-  float op = 0.0f, rx = 0.0f, ry = 0.0f;
-  f3 vdir = {0.0f, 0.0f, 0.0f};
-  // Decode, project and cull; a splat that survives gets its tile box.
-  do {
-    if (gid >= v.active) break;  // padding up to the view's next block boundary
-    const uint32_t C = v.C;
-    slot = __ldg(v.sh + (size_t)v.count * C + gid);
-    if (slot >= v.count) break;  // out-of-range tail entries never draw
-    const float4 mo = __ldg(v.means + slot);
-    if (mo.w < 0.0f) break;  // empty slot (ProjectionStage.ts:408-410)
-    const uint32_t obj = (uint32_t)mo.w;
-    if (obj >= v.object_count) break;  // unwritten object rows are zero
-    const float* ot = v.objects + 40 * (size_t)obj;
-    if (!(__ldg(ot + 36) > 0.0f)) break;  // object visibility (:445-450)
-    const float4 so = decode_scale_opacity(__ldg(v.shape + slot));
-    const float4 q = decode_rotation(__ldg(v.rot + slot));
-    float mv[16];
-#pragma unroll
-    for (int i = 0; i < 16; ++i) mv[i] = __ldg(ot + 16 + i);
-    const float camx = __ldg(ot + 32), camy = __ldg(ot + 33), camz = __ldg(ot + 34);
-    // viewDirection = normalize(positionLocal - cameraLocal) (:469)
-    const float ddx = mo.x - camx, ddy = mo.y - camy, ddz = mo.z - camz;
-    const float dlen = sqrtf((ddx * ddx + ddy * ddy) + ddz * ddz);
-    vdir = {ddx / dlen, ddy / dlen, ddz / dlen};
-    // view = modelView * (p, 1) (:479-482); the FP64 form evaluates it in
-    // double so far-origin coordinates do not cancel against the translation.
-    double vxd = 0.0, vyd = 0.0, vzd = 0.0;
-    float vx, vy, vz;
-    if (FP64) {
-      vxd = (((double)mv[0] * mo.x + (double)mv[4] * mo.y) + (double)mv[8] * mo.z) + (double)mv[12];
-      vyd = (((double)mv[1] * mo.x + (double)mv[5] * mo.y) + (double)mv[9] * mo.z) + (double)mv[13];
-      vzd = (((double)mv[2] * mo.x + (double)mv[6] * mo.y) + (double)mv[10] * mo.z) + (double)mv[14];
-      vx = (float)vxd; vy = (float)vyd; vz = (float)vzd;
-    } else {
-      vx = ((mv[0] * mo.x + mv[4] * mo.y) + mv[8] * mo.z) + mv[12] * 1.0f;
-      vy = ((mv[1] * mo.x + mv[5] * mo.y) + mv[9] * mo.z) + mv[13] * 1.0f;
-      vz = ((mv[2] * mo.x + mv[6] * mo.y) + mv[10] * mo.z) + mv[14] * 1.0f;
-    }
-    m3 l2v;
-#pragma unroll
-    for (int c = 0; c < 3; ++c)
-#pragma unroll
-      for (int r = 0; r < 3; ++r) l2v.m[c][r] = mv[4 * c + r];
-    const m3 cv = view_covariance(so, q, l2v);
-    float P[16];
-#pragma unroll
-    for (int i = 0; i < 16; ++i) P[i] = v.P[i];
-    pr = project({vx, vy, vz}, cv, P, vw, vh, v.vnear, v.vfar, o.filter);
-    if (FP64) {
-      // Near-singular in FP32 (tiny anti-aliasing factor, high condition
-      // number, or rejected past the depth test): redo the chain in double.
-      const float cond_num = (pr.cov_x + pr.cov_z) * (pr.cov_x + pr.cov_z);
-      const bool redo = !pr.ok ? (-vz > v.vnear && -vz < v.vfar)
-                               : (pr.orig_det < 1e-2f * pr.det || !(cond_num <= 4e3f * pr.det));
-      if (redo) pr = project_fp64(vxd, vyd, vzd, so, q, mv, P, vw, vh, v.vnear, v.vfar, o.filter);
-    }
-    if (!pr.ok) break;
-    op = clampf(so.w, 0.0f, 1.0f);
-    if (o.antialias == 0u) op = op * sqrtf(clampf(pr.orig_det / pr.det, 0.0f, 1.0f));
-    if (op < (float)(1.0 / 255.0) || op != op) break;
-    const float thr = gsdm::logf_(op * 255.0f);
-    const float ex = sqrtf((thr * 2.0f) * clampf(pr.cov_x, 1e-12f, 1e4f));
-    const float ey = sqrtf((thr * 2.0f) * clampf(pr.cov_z, 1e-12f, 1e4f));
-    rx = ceilf(ex);
-    ry = ceilf(ey);
-    if (rx <= 0.0f || ry <= 0.0f) break;
-    const float bminx = pr.cx - rx, bminy = pr.cy - ry, bmaxx = pr.cx + rx, bmaxy = pr.cy + ry;
-    if ((o.axis != 1u && (bmaxx < 0.0f || bminx >= vw)) || (o.axis != 2u && (bmaxy < 0.0f || bminy >= vh)))
-      break;
-    if (o.subpixel != 0u &&
-        !subpixel_has_sample(pr.cx, pr.cy, pr.conic_x, pr.conic_y, pr.conic_z, thr, ex, ey, (uint32_t)vw,
-                             (uint32_t)vh, o.axis)) {
-      mo4 = make_float4(pr.cx, pr.cy, pr.depth, -1.0f);  // subpixel marker (:572-587)
-      break;
-    }
-    const int tiles_x = (int)v.tiles_x, tiles_y = (int)v.tiles_y;
-    const float mtx = (float)(tiles_x - 1), mty = (float)(tiles_y - 1);
-    int tminx = (int)clampf(floorf(bminx / 16.0f), 0.0f, mtx);
-    int tminy = (int)clampf(floorf(bminy / 16.0f), 0.0f, mty);
-    int tmaxx = (int)clampf(floorf(bmaxx / 16.0f), 0.0f, mtx);
-    int tmaxy = (int)clampf(floorf(bmaxy / 16.0f), 0.0f, mty);
-    if (o.axis == 1u) { tminx = 0; tmaxx = tiles_x - 1; }
-    if (o.axis == 2u) { tminy = 0; tmaxy = tiles_y - 1; }
-    const uint32_t bw = (uint32_t)(tmaxx - tminx + 1);
-    nbox = bw * (uint32_t)(tmaxy - tminy + 1);
-    s_count.f[0][warp][lane] = pr.cx; s_count.f[1][warp][lane] = pr.cy;
-    s_count.f[2][warp][lane] = pr.conic_x; s_count.f[3][warp][lane] = pr.conic_y;
-    s_count.f[4][warp][lane] = pr.conic_z; s_count.f[5][warp][lane] = thr;
-    s_count.f[6][warp][lane] = rx; s_count.f[7][warp][lane] = ry;
-    s_count.u[0][warp][lane] = (uint32_t)tminx; s_count.u[1][warp][lane] = (uint32_t)tminy;
-    s_count.u[2][warp][lane] = bw;
-  } while (false);
-  // Tiles passing the tile test (projectionHelpers.ts:223-236), counted by the whole warp.
-  cnt = count_tiles_warp(s_count, nbox, vw, vh, o.axis);
-  if (cnt > 0) {
-    uint32_t co[16];
-    load_sh(v.sh + (size_t)slot * v.C, v.degree, co);
-    const f3 col = eval_sh_any(v.degree, co, vdir, s_snorm);
-    mo4 = make_float4(pr.cx, pr.cy, pr.depth, op);
-    conic_out[item] = make_float4(pr.conic_x, pr.conic_y, pr.conic_z, rx + ry * 512.0f);
-    color_out[item] = make_float4(col.x, col.y, col.z, __uint_as_float(slot ^ kActiveTag));
-    if (rec_out) {
-      // Packed raster record of the fast forms (layout in pass_common.cuh).
-      const float log2op = __log2f(op);
-      const __half2 rg = __floats2half2_rn(col.x, col.y);
-      const __half2 bl = __floats2half2_rn(col.z, fminf(log2op, kLog2MaxAlpha));
-      rec_out[2 * (size_t)item] = make_float4(pr.cx, pr.cy, -0.5f * kLog2e * pr.conic_x, -kLog2e * pr.conic_y);
-      rec_out[2 * (size_t)item + 1] =
-          make_float4(-0.5f * kLog2e * pr.conic_z, log2op, __uint_as_float(*reinterpret_cast<const uint32_t*>(&rg)),
-                      __uint_as_float(*reinterpret_cast<const uint32_t*>(&bl)));
-    }
-    if (o.depth_mode == 0u) {
-      key = __float_as_uint(pr.depth);  // visibility.ts:139
-    } else {
-      float t = clampf((pr.depth - v.vnear) / (v.vfar - v.vnear), 0.0f, 1.0f);
-      key = (uint32_t)gsdm::round_even_small(t * 65535.0f);  // visibility.ts:140-144
-    }
+  const uint32_t gid = (blockIdx.x - __ldg(b.group_block + g)) * kBlock + threadIdx.x;  // ordinal in each view
+  const uint32_t v_first = __ldg(b.group_view + g);
+  const uint32_t v_end = GROUPED ? __ldg(b.group_view + g + 1) : v_first + 1u;
+
+  // Decode the splat once for every view of the group (the views share the
+  // packed scene, so the active tail, means, shape and rotation are common).
+  bool live = false;
+  uint32_t slot = 0;
+  float4 mo = make_float4(0.0f, 0.0f, 0.0f, 0.0f), so = mo, q = mo;
+  m3 local = {};
+  {
+    const ViewDesc& v = b.views[v_first];
+    do {
+      if (gid >= v.active) break;  // padding up to the view's next block boundary
+      slot = __ldg(v.sh + (size_t)v.count * v.C + gid);
+      if (slot >= v.count) break;  // out-of-range tail entries never draw
+      mo = __ldg(v.means + slot);
+      if (mo.w < 0.0f) break;  // empty slot (ProjectionStage.ts:408-410)
+      if (GROUPED) {
+        so = decode_scale_opacity(__ldg(v.shape + slot));
+        q = decode_rotation(__ldg(v.rot + slot));
+        local = local_covariance(so, q);
+      }
+      live = true;
+    } while (false);
   }
-  mean_out[item] = mo4;
-  count_out[item] = cnt;
-  key_out[item] = key;
+
+  for (uint32_t vi = v_first; vi < v_end; ++vi) {
+    const ViewDesc& v = b.views[vi];
+    const uint32_t item = v.item_base + gid;
+    const float vw = v.vw, vh = v.vh;
+    float4 mo4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    uint32_t cnt = 0, key = kInvisibleKey, nbox = 0;
+    Projected pr = {};
+    float op = 0.0f, rx = 0.0f, ry = 0.0f;
+    f3 vdir = {0.0f, 0.0f, 0.0f};
+    // Project and cull; a splat that survives gets its tile box.
+    do {
+      if (!live) break;
+      const uint32_t obj = (uint32_t)mo.w;
+      if (obj >= v.object_count) break;  // unwritten object rows are zero
+      const float* ot = v.objects + 40 * (size_t)obj;
+      if (!(__ldg(ot + 36) > 0.0f)) break;  // object visibility (:445-450)
+      if (!GROUPED) {
+        so = decode_scale_opacity(__ldg(v.shape + slot));
+        q = decode_rotation(__ldg(v.rot + slot));
+      }
+      float mv[16];
+#pragma unroll
+      for (int i = 0; i < 16; ++i) mv[i] = __ldg(ot + 16 + i);
+      const float camx = __ldg(ot + 32), camy = __ldg(ot + 33), camz = __ldg(ot + 34);
+      // viewDirection = normalize(positionLocal - cameraLocal) (:469)
+      const float ddx = mo.x - camx, ddy = mo.y - camy, ddz = mo.z - camz;
+      const float dlen = sqrtf((ddx * ddx + ddy * ddy) + ddz * ddz);
+      vdir = {ddx / dlen, ddy / dlen, ddz / dlen};
+      // view = modelView * (p, 1) (:479-482); the FP64 form evaluates it in
+      // double so far-origin coordinates do not cancel against the translation.
+      double vxd = 0.0, vyd = 0.0, vzd = 0.0;
+      float vx, vy, vz;
+      if (FP64) {
+        vxd = (((double)mv[0] * mo.x + (double)mv[4] * mo.y) + (double)mv[8] * mo.z) + (double)mv[12];
+        vyd = (((double)mv[1] * mo.x + (double)mv[5] * mo.y) + (double)mv[9] * mo.z) + (double)mv[13];
+        vzd = (((double)mv[2] * mo.x + (double)mv[6] * mo.y) + (double)mv[10] * mo.z) + (double)mv[14];
+        vx = (float)vxd; vy = (float)vyd; vz = (float)vzd;
+      } else {
+        vx = ((mv[0] * mo.x + mv[4] * mo.y) + mv[8] * mo.z) + mv[12] * 1.0f;
+        vy = ((mv[1] * mo.x + mv[5] * mo.y) + mv[9] * mo.z) + mv[13] * 1.0f;
+        vz = ((mv[2] * mo.x + mv[6] * mo.y) + mv[10] * mo.z) + mv[14] * 1.0f;
+      }
+      m3 l2v;
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int r = 0; r < 3; ++r) l2v.m[c][r] = mv[4 * c + r];
+      const m3 cv = view_covariance(GROUPED ? local : local_covariance(so, q), l2v);
+      float P[16];
+#pragma unroll
+      for (int i = 0; i < 16; ++i) P[i] = v.P[i];
+      pr = project({vx, vy, vz}, cv, P, vw, vh, v.vnear, v.vfar, o.filter);
+      if (FP64) {
+        // Near-singular in FP32 (tiny anti-aliasing factor, high condition
+        // number, or rejected past the depth test): redo the chain in double.
+        const float cond_num = (pr.cov_x + pr.cov_z) * (pr.cov_x + pr.cov_z);
+        const bool redo = !pr.ok ? (-vz > v.vnear && -vz < v.vfar)
+                                 : (pr.orig_det < 1e-2f * pr.det || !(cond_num <= 4e3f * pr.det));
+        if (redo) pr = project_fp64(vxd, vyd, vzd, so, q, mv, P, vw, vh, v.vnear, v.vfar, o.filter);
+      }
+      if (!pr.ok) break;
+      op = clampf(so.w, 0.0f, 1.0f);
+      if (o.antialias == 0u) op = op * sqrtf(clampf(pr.orig_det / pr.det, 0.0f, 1.0f));
+      if (op < (float)(1.0 / 255.0) || op != op) break;
+      const float thr = gsdm::logf_(op * 255.0f);
+      const float ex = sqrtf((thr * 2.0f) * clampf(pr.cov_x, 1e-12f, 1e4f));
+      const float ey = sqrtf((thr * 2.0f) * clampf(pr.cov_z, 1e-12f, 1e4f));
+      rx = ceilf(ex);
+      ry = ceilf(ey);
+      if (rx <= 0.0f || ry <= 0.0f) break;
+      const float bminx = pr.cx - rx, bminy = pr.cy - ry, bmaxx = pr.cx + rx, bmaxy = pr.cy + ry;
+      if ((o.axis != 1u && (bmaxx < 0.0f || bminx >= vw)) || (o.axis != 2u && (bmaxy < 0.0f || bminy >= vh)))
+        break;
+      if (o.subpixel != 0u &&
+          !subpixel_has_sample(pr.cx, pr.cy, pr.conic_x, pr.conic_y, pr.conic_z, thr, ex, ey, (uint32_t)vw,
+                               (uint32_t)vh, o.axis)) {
+        mo4 = make_float4(pr.cx, pr.cy, pr.depth, -1.0f);  // subpixel marker (:572-587)
+        break;
+      }
+      const int tiles_x = (int)v.tiles_x, tiles_y = (int)v.tiles_y;
+      const float mtx = (float)(tiles_x - 1), mty = (float)(tiles_y - 1);
+      int tminx = (int)clampf(floorf(bminx / 16.0f), 0.0f, mtx);
+      int tminy = (int)clampf(floorf(bminy / 16.0f), 0.0f, mty);
+      int tmaxx = (int)clampf(floorf(bmaxx / 16.0f), 0.0f, mtx);
+      int tmaxy = (int)clampf(floorf(bmaxy / 16.0f), 0.0f, mty);
+      if (o.axis == 1u) { tminx = 0; tmaxx = tiles_x - 1; }
+      if (o.axis == 2u) { tminy = 0; tmaxy = tiles_y - 1; }
+      const uint32_t bw = (uint32_t)(tmaxx - tminx + 1);
+      nbox = bw * (uint32_t)(tmaxy - tminy + 1);
+      s_count.f[0][warp][lane] = pr.cx; s_count.f[1][warp][lane] = pr.cy;
+      s_count.f[2][warp][lane] = pr.conic_x; s_count.f[3][warp][lane] = pr.conic_y;
+      s_count.f[4][warp][lane] = pr.conic_z; s_count.f[5][warp][lane] = thr;
+      s_count.f[6][warp][lane] = rx; s_count.f[7][warp][lane] = ry;
+      s_count.u[0][warp][lane] = (uint32_t)tminx; s_count.u[1][warp][lane] = (uint32_t)tminy;
+      s_count.u[2][warp][lane] = bw;
+    } while (false);
+    // Tiles passing the tile test (projectionHelpers.ts:223-236), counted by the whole warp.
+    cnt = count_tiles_warp(s_count, nbox, vw, vh, o.axis);
+    if (cnt > 0) {
+      uint32_t co[16];
+      load_sh(v.sh + (size_t)slot * v.C, v.degree, co);
+      const f3 col = eval_sh_any(v.degree, co, vdir, s_snorm);
+      mo4 = make_float4(pr.cx, pr.cy, pr.depth, op);
+      conic_out[item] = make_float4(pr.conic_x, pr.conic_y, pr.conic_z, rx + ry * 512.0f);
+      color_out[item] = make_float4(col.x, col.y, col.z, __uint_as_float(slot ^ kActiveTag));
+      if (rec_out) {
+        // Packed raster record of the fast forms (layout in pass_common.cuh).
+        const float log2op = __log2f(op);
+        const __half2 rg = __floats2half2_rn(col.x, col.y);
+        const __half2 bl = __floats2half2_rn(col.z, fminf(log2op, kLog2MaxAlpha));
+        rec_out[2 * (size_t)item] = make_float4(pr.cx, pr.cy, -0.5f * kLog2e * pr.conic_x, -kLog2e * pr.conic_y);
+        rec_out[2 * (size_t)item + 1] =
+            make_float4(-0.5f * kLog2e * pr.conic_z, log2op, __uint_as_float(*reinterpret_cast<const uint32_t*>(&rg)),
+                        __uint_as_float(*reinterpret_cast<const uint32_t*>(&bl)));
+      }
+      if (o.depth_mode == 0u) {
+        key = __float_as_uint(pr.depth);  // visibility.ts:139
+      } else {
+        float t = clampf((pr.depth - v.vnear) / (v.vfar - v.vnear), 0.0f, 1.0f);
+        key = (uint32_t)gsdm::round_even_small(t * 65535.0f);  // visibility.ts:140-144
+      }
+    }
+    mean_out[item] = mo4;
+    count_out[item] = cnt;
+    key_out[item] = key;
+  }
 }
 
 void launch_project(const BatchView& b, const PassOptions& o, float4* mean, float4* conic, float4* color,
                     uint32_t* counts, uint32_t* keys, float4* rec, cudaStream_t st) {
-  if (b.total_blocks == 0) return;
-  if (o.proj_fp64)
-    k_project<true><<<b.total_blocks, kBlock, 0, st>>>(b, o, mean, conic, color, counts, keys, rec);
-  else
-    k_project<false><<<b.total_blocks, kBlock, 0, st>>>(b, o, mean, conic, color, counts, keys, rec);
+  if (b.total_blocks == 0) return;  // projection blocks over the view groups
+  const bool grouped = b.ngroups < b.nviews;
+  if (o.proj_fp64) {
+    if (grouped)
+      k_project<true, true><<<b.total_blocks, kBlock, 0, st>>>(b, o, mean, conic, color, counts, keys, rec);
+    else
+      k_project<true, false><<<b.total_blocks, kBlock, 0, st>>>(b, o, mean, conic, color, counts, keys, rec);
+  } else {
+    if (grouped)
+      k_project<false, true><<<b.total_blocks, kBlock, 0, st>>>(b, o, mean, conic, color, counts, keys, rec);
+    else
+      k_project<false, false><<<b.total_blocks, kBlock, 0, st>>>(b, o, mean, conic, color, counts, keys, rec);
+  }
 }
 
 // ---------------------------------------------------------------------------

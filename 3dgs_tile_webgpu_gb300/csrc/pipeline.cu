@@ -515,17 +515,39 @@ namespace {
 size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
 
 struct Plan {
-  uint32_t n = 0;
+  uint32_t n = 0, ngroups = 0;
   uint32_t items = 0, tiles = 0, blocks = 0;
   size_t objects = 0;
   size_t views_off = 0, objects_off = 0, stage_bytes = 0;
 };
+
+// Byte layout of a staged batch table of n views holding `objects` object
+// rows: frame parameters and the four base arrays, view descriptors, object
+// rows.
+void layout_plan(Plan* pl, uint32_t n, size_t objects) {
+  const size_t header = 16 + align16(4 * (size_t)(n + 1) * sizeof(uint32_t));
+  pl->views_off = header;
+  pl->objects_off = align16(header + (size_t)n * sizeof(ViewDesc));
+  pl->stage_bytes = pl->objects_off + objects * 40 * sizeof(float);
+}
+
+// Consecutive views of a batch that render the same packed scene (same
+// buffers, counts and SH degree) form a view group: the projection decodes
+// each splat once for the whole group.
+bool same_scene(const gs3d_view& a, const gs3d_view& b) {
+  const gs3d_gaussian_data& x = *a.data;
+  const gs3d_gaussian_data& y = *b.data;
+  return x.means == y.means && x.scales_opacity == y.scales_opacity && x.rotations == y.rotations &&
+         x.sh_coefficients == y.sh_coefficients && x.count == y.count && x.active_count == y.active_count &&
+         x.sh_degree == y.sh_degree;
+}
 
 // Validate a batch, grow every workspace it needs and lay out its batch
 // table. Not capturable (it may allocate).
 gs3d_status plan_batch(gs3d_pipeline* p, const gs3d_view* views, uint32_t n, Plan* out) {
   if (n == 0 || n > kMaxViews) return fail(p, GS3D_ERROR_RANGE, "a batch holds 1 to 4096 views");
   uint64_t items = 0, tiles = 0, blocks = 0;
+  uint32_t ngroups = 0;
   size_t objects = 0;
   for (uint32_t i = 0; i < n; ++i) {
     const gs3d_view& v = views[i];
@@ -542,7 +564,10 @@ gs3d_status plan_batch(gs3d_pipeline* p, const gs3d_view* views, uint32_t n, Pla
     // TiledGaussianPipeline.ts:294-296
     if (tx > 65535u || ty > 65535u) return fail(p, GS3D_ERROR_RANGE, "Render size exceeds WebGPU's tile dispatch limit");
     const uint64_t b = ((uint64_t)v.data->active_count + kBlock - 1) / kBlock;
-    blocks += b;
+    if (i == 0 || !same_scene(views[i - 1], v)) {
+      blocks += b;
+      ++ngroups;
+    }
     items += b * kBlock;
     tiles += (uint64_t)tx * ty;
     objects += v.camera->object_count;
@@ -558,19 +583,18 @@ gs3d_status plan_batch(gs3d_pipeline* p, const gs3d_view* views, uint32_t n, Pla
   if ((s = ensure_status(p)) != GS3D_OK) return s;
   if ((s = ensure_tiles(p, tiles)) != GS3D_OK) return s;
   out->n = n;
+  out->ngroups = ngroups;
   out->items = (uint32_t)items;
   out->tiles = (uint32_t)tiles;
   out->blocks = (uint32_t)blocks;
   out->objects = objects;
-  const size_t header = 16 + align16(3 * (size_t)(n + 1) * sizeof(uint32_t));
-  out->views_off = header;
-  out->objects_off = align16(header + (size_t)n * sizeof(ViewDesc));
-  out->stage_bytes = out->objects_off + objects * 40 * sizeof(float);
+  layout_plan(out, n, objects);
   return GS3D_OK;
 }
 
 // Fill a host copy of the batch table whose device copy will live at `dev`:
-// frame parameters, the three base arrays, view descriptors, object tables.
+// frame parameters, the item/tile base arrays, the view-group arrays, view
+// descriptors, object tables.
 void stage_batch(gs3d_pipeline* p, const gs3d_view* views, const Plan& pl, uint32_t attempt, int reset_valid,
                  unsigned char* host, unsigned char* dev) {
   const uint32_t n = pl.n;
@@ -580,7 +604,9 @@ void stage_batch(gs3d_pipeline* p, const gs3d_view* views, const Plan& pl, uint3
   params[2] = params[3] = 0u;
   uint32_t* h_item = params + 4;
   uint32_t* h_tile = h_item + (n + 1);
-  uint32_t* h_block = h_tile + (n + 1);
+  uint32_t* h_gblock = h_tile + (n + 1);
+  uint32_t* h_gview = h_gblock + (n + 1);
+  uint32_t ngroups = 0;
   ViewDesc* h_views = (ViewDesc*)(host + pl.views_off);
   float* h_obj = (float*)(host + pl.objects_off);
   uint32_t item = 0, tile = 0, block = 0;
@@ -609,7 +635,6 @@ void stage_batch(gs3d_pipeline* p, const gs3d_view* views, const Plan& pl, uint3
     w.tiles_y = tiles_for(v.height);
     w.item_base = item;
     w.tile_base = tile;
-    w.block_base = block;
     memcpy(w.P, v.camera->projection, sizeof(w.P));
     w.vw = (float)v.width;
     w.vh = (float)v.height;
@@ -619,18 +644,25 @@ void stage_batch(gs3d_pipeline* p, const gs3d_view* views, const Plan& pl, uint3
       memcpy(h_obj + obj * 40, v.camera->object_table, (size_t)v.camera->object_count * 40 * sizeof(float));
     h_item[i] = item;
     h_tile[i] = tile;
-    h_block[i] = block;
     p->item_bases[i] = item;
     p->tile_bases[i] = tile;
     const uint32_t b = (d.active_count + kBlock - 1) / kBlock;
-    block += b;
+    if (i == 0 || !same_scene(views[i - 1], v)) {
+      h_gblock[ngroups] = block;
+      h_gview[ngroups] = i;
+      ++ngroups;
+      block += b;
+    }
     item += b * kBlock;
     tile += w.tiles_x * w.tiles_y;
     obj += v.camera->object_count;
   }
   h_item[n] = item;
   h_tile[n] = tile;
-  h_block[n] = block;
+  for (uint32_t g = ngroups; g <= n; ++g) {
+    h_gblock[g] = block;
+    h_gview[g] = n;
+  }
   p->item_bases[n] = item;
   p->tile_bases[n] = tile;
   p->total_items = item;
@@ -645,7 +677,9 @@ void record_batch(gs3d_pipeline* p, const Plan& pl, unsigned char* dev, cudaStre
   bv.frame_params = (const uint32_t*)dev;
   bv.item_base = bv.frame_params + 4;
   bv.tile_base = bv.item_base + (n + 1);
-  bv.block_base = bv.tile_base + (n + 1);
+  bv.group_block = bv.tile_base + (n + 1);
+  bv.group_view = bv.group_block + (n + 1);
+  bv.ngroups = pl.ngroups;
   bv.views = (const ViewDesc*)(dev + pl.views_off);
   bv.nviews = n;
   bv.total_items = pl.items;
@@ -925,10 +959,7 @@ gs3d_status gs3d_pipeline_launch_graph(gs3d_pipeline* p, const gs3d_camera* came
     pl.n = ch.count;
     size_t objects = 0;
     for (uint32_t i = 0; i < ch.count; ++i) objects += cameras[ch.first + i].object_count;
-    const size_t header = 16 + align16(3 * (size_t)(ch.count + 1) * sizeof(uint32_t));
-    pl.views_off = header;
-    pl.objects_off = align16(header + (size_t)ch.count * sizeof(ViewDesc));
-    pl.stage_bytes = pl.objects_off + objects * 40 * sizeof(float);
+    layout_plan(&pl, ch.count, objects);
     stage_batch(p, p->graph_views.data() + ch.first, pl, attempt, reset_valid, p->graph_pinned[g] + ch.offset,
                 p->graph_dev[g] + ch.offset);
   }

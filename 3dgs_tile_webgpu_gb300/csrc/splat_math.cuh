@@ -101,8 +101,9 @@ __device__ __forceinline__ float4 decode_rotation(uint32_t packed) {
   return make_float4(ax * s, ay * s, az * s, gsdm::cosf_(half));
 }
 
-// projectionHelpers.ts:4-35. mv holds the model-view's first three columns.
-__device__ __forceinline__ m3 view_covariance(float4 so, float4 q_in, const m3& l2v) {
+// projectionHelpers.ts:4-35, first half: the object-space 3D covariance
+// R S^2 R^T, which depends on the splat alone (shared by every view of it).
+__device__ __forceinline__ m3 local_covariance(float4 so, float4 q_in) {
   float sx = maxf(so.x, 1e-7f), sy = maxf(so.y, 1e-7f), sz = maxf(so.z, 1e-7f);
   float d = ((q_in.x * q_in.x + q_in.y * q_in.y) + q_in.z * q_in.z) + q_in.w * q_in.w;
   float len = sqrtf(d);
@@ -118,7 +119,12 @@ __device__ __forceinline__ m3 view_covariance(float4 so, float4 q_in, const m3& 
   sc.m[0][0] = sx * sx; sc.m[0][1] = 0.0f; sc.m[0][2] = 0.0f;
   sc.m[1][0] = 0.0f; sc.m[1][1] = sy * sy; sc.m[1][2] = 0.0f;
   sc.m[2][0] = 0.0f; sc.m[2][1] = 0.0f; sc.m[2][2] = sz * sz;
-  m3 local = mul33(mul33(rot, sc), transpose33(rot));
+  return mul33(mul33(rot, sc), transpose33(rot));
+}
+
+// projectionHelpers.ts:4-35, second half: L (R S^2 R^T) L^T with L the
+// model-view's upper 3x3.
+__device__ __forceinline__ m3 view_covariance(const m3& local, const m3& l2v) {
   return mul33(mul33(l2v, local), transpose33(l2v));
 }
 
