@@ -85,8 +85,8 @@ constexpr uint32_t kScanTile = kBlock * kScanItems;     // items per look-back t
 // Per-frame control block, zeroed before each render.
 struct Control {
   uint32_t tickets[2];           // dynamic tile ids of the look-back kernels (Ticket)
-  uint32_t depth_hist[kMaxSortPasses][256];  // digit histograms of the depth sort
-  uint32_t tile_hist[kMaxSortPasses][256];   // digit histograms of the tile sort
+  uint32_t depth_hist[kMaxSortPasses][256];  // digit histograms of the depth sort (its count kernels)
+  uint32_t tile_hist[kMaxSortPasses][256];   // digit histograms of the tile sort (its count kernels)
   uint32_t visible_state[4];     // visible, visible, radix blocks, 0
   uint32_t state[4];             // count, total, radix blocks, overflow
   uint32_t error;                // bit 0: look-back wait expired
@@ -239,25 +239,25 @@ void launch_project(const BatchView& b, const PassOptions& o, float4* mean, floa
                     uint32_t* counts, uint32_t* keys, float4* rec, cudaStream_t st);
 void launch_epoch_begin(uint32_t* epoch_base, cudaStream_t st);
 void launch_compact(const uint32_t* keys, uint32_t n, uint32_t* vis_off, uint32_t* keys_out, uint32_t* vals_out,
-                    Control* ctl, unsigned long long* status, Epoch epoch, int depth_passes, cudaStream_t st);
+                    Control* ctl, unsigned long long* status, Epoch epoch, cudaStream_t st);
 void launch_scan_counts(const uint32_t* sorted_ids, const uint32_t* tile_counts, uint32_t n_max,
                         uint32_t* ordered, uint32_t* offsets, Control* ctl, unsigned long long* status,
                         Epoch epoch, uint32_t capacity, const uint32_t* frame_params, uint32_t* output_state,
                         cudaStream_t st);
 void launch_emit(const uint32_t* sorted_ids, uint32_t n_max, const float4* mean, const float4* conic,
                  const uint32_t* ordered, const uint32_t* offsets, const BatchView& b, const PassOptions& o,
-                 Control* ctl, uint32_t capacity, uint32_t* tile_keys, uint32_t* tile_vals, int tile_passes,
-                 int tile_digit_bits, cudaStream_t st);
+                 Control* ctl, uint32_t capacity, uint32_t* tile_keys, uint32_t* tile_vals, cudaStream_t st);
 void launch_tile_ranges(const uint32_t* sorted_tile_keys, Control* ctl, uint32_t ntile, uint32_t n_max,
                         uint32_t* tile_offsets, cudaStream_t st);
 constexpr uint32_t kSortTile = 4096;  // items per sort tile
 // Chunked LSD pass (reduce, scan, scatter; no look-back chain): `chunks`
 // blocks, each walking a contiguous run of 4096-item tiles. counts holds
-// chunks x 2^bits words. n is read from *n_ptr on the device.
+// chunks x 2^bits words; hist (2^bits words, zero on entry) receives the
+// pass's digit histogram. n is read from *n_ptr on the device.
 constexpr uint32_t kChunkBlocksPerSm = 3;
 uint32_t chunk_pass_chunks(uint32_t n_max, int sms);
 void launch_chunk_pass(int bits, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
-                       uint32_t* vals_out, const uint32_t* n_ptr, int shift, const uint32_t* hist, uint32_t chunks,
+                       uint32_t* vals_out, const uint32_t* n_ptr, int shift, uint32_t* hist, uint32_t chunks,
                        uint32_t* counts, cudaStream_t st);
 // Opt every sort-scatter instantiation into its shared-memory size (once per
 // device; call before any stream capture).

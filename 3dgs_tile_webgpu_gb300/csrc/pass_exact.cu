@@ -288,21 +288,18 @@ void launch_project(const BatchView& b, const PassOptions& o, float4* mean, floa
 // ---------------------------------------------------------------------------
 // Visibility compaction (scan.ts:9-83 + visibility.ts:9-61): one pass with
 // decoupled look-back. Writes visibleOffsets, the (depthKey, ordinal) records
-// in ordinal order, the visible state, and the depth sort's digit histograms.
+// in ordinal order and the visible state.
 constexpr uint32_t kItems = kScanItems;
 
 __global__ void __launch_bounds__(kBlock) k_compact(const uint32_t* __restrict__ keys, uint32_t n,
                                                     uint32_t* __restrict__ vis_off, uint32_t* __restrict__ keys_out,
                                                     uint32_t* __restrict__ vals_out, Control* __restrict__ ctl,
-                                                    unsigned long long* __restrict__ status, Epoch ep,
-                                                    int passes) {
+                                                    unsigned long long* __restrict__ status, Epoch ep) {
   const uint32_t epoch = ep.get();
   __shared__ uint32_t s_tile, s_prefix;
   __shared__ uint32_t s_warp[kBlock / 32];
-  __shared__ uint32_t s_hist[kMaxSortPasses][256];
   const uint32_t tid = threadIdx.x;
   if (tid == 0) s_tile = atomicAdd(&ctl->tickets[kTicketCompact], 1u);
-  for (uint32_t i = tid; i < kMaxSortPasses * 256; i += kBlock) (&s_hist[0][0])[i] = 0u;
   __syncthreads();
   const uint32_t tile = s_tile;
   const uint32_t ntiles = n == 0 ? 1u : (n + kScanTile - 1) / kScanTile;
@@ -353,14 +350,9 @@ __global__ void __launch_bounds__(kBlock) k_compact(const uint32_t* __restrict__
     if (k[i] != kInvisibleKey) {
       keys_out[off] = k[i];
       vals_out[off] = idx;
-      for (int p = 0; p < passes; ++p) atomicAdd(&s_hist[p][(k[i] >> (8 * p)) & 255u], 1u);
       ++off;
     }
   }
-  __syncthreads();
-  for (uint32_t d = tid; d < 256; d += kBlock)
-    for (int p = 0; p < passes; ++p)
-      if (s_hist[p][d]) atomicAdd(&ctl->depth_hist[p][d], s_hist[p][d]);
 }
 
 __global__ void k_epoch_begin(uint32_t* base) {
@@ -372,9 +364,9 @@ __global__ void k_epoch_begin(uint32_t* base) {
 void launch_epoch_begin(uint32_t* epoch_base, cudaStream_t st) { k_epoch_begin<<<1, 1, 0, st>>>(epoch_base); }
 
 void launch_compact(const uint32_t* keys, uint32_t n, uint32_t* vis_off, uint32_t* keys_out, uint32_t* vals_out,
-                    Control* ctl, unsigned long long* status, Epoch epoch, int passes, cudaStream_t st) {
+                    Control* ctl, unsigned long long* status, Epoch epoch, cudaStream_t st) {
   const uint32_t grid = n == 0 ? 1u : (n + kScanTile - 1) / kScanTile;
-  k_compact<<<grid, kBlock, 0, st>>>(keys, n, vis_off, keys_out, vals_out, ctl, status, epoch, passes);
+  k_compact<<<grid, kBlock, 0, st>>>(keys, n, vis_off, keys_out, vals_out, ctl, status, epoch);
 }
 
 // ---------------------------------------------------------------------------
@@ -460,8 +452,7 @@ void launch_scan_counts(const uint32_t* ids, const uint32_t* tile_counts, uint32
 // (tile, item) record for every tile the splat contributes to, written at the
 // rank's scanned offset; sentinel padding if fewer hits than reserved. Tile
 // ids are global over the batch (the view's tile_base + local id; the
-// sentinel is the batch's tile total). Also accumulates the tile sort's digit
-// histograms.
+// sentinel is the batch's tile total).
 //
 // Warp-cooperative: a warp owns 32 consecutive depth ranks and spreads the
 // union of their bounding-box tiles over its lanes, 32 box tiles per round,
@@ -479,7 +470,6 @@ struct EmitShared {
   uint32_t u[8][kEmitWarps][32];   // tminx, tminy, box width, tiles_x, tile_base, base, reserved, item
   uint32_t incl[kEmitWarps][32];   // inclusive box-tile counts
   uint32_t filled[kEmitWarps][32]; // records placed so far per rank
-  uint32_t hist[kMaxSortPasses][256];
 };
 
 // One group of kBlock depth ranks (32 per warp): stage each lane's box and
@@ -489,9 +479,8 @@ struct EmitShared {
 __device__ __forceinline__ void emit_group(EmitShared& sm, bool live, uint32_t g, float4 m, float4 c,
                                            uint32_t reserved, uint32_t base_off, const BatchView& bv,
                                            const PassOptions& o, uint32_t capacity, uint32_t* __restrict__ tile_keys,
-                                           uint32_t* __restrict__ tile_vals, int passes, int digit_bits) {
+                                           uint32_t* __restrict__ tile_vals) {
   const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-  const uint32_t mask = (1u << digit_bits) - 1u;
   const uint32_t sentinel = bv.total_tiles;
   const uint32_t lt = (1u << lane) - 1u;
   uint32_t nbox = 0;
@@ -559,7 +548,6 @@ __device__ __forceinline__ void emit_group(EmitShared& sm, bool live, uint32_t g
       if (local < sm.u[6][warp][owner] && base + local < capacity) {
         tile_keys[base + local] = t;
         tile_vals[base + local] = sm.u[7][warp][owner];
-        for (int p = 0; p < passes; ++p) atomicAdd(&sm.hist[p][(t >> (p * digit_bits)) & mask], 1u);
       }
     }
     __syncwarp();
@@ -574,7 +562,6 @@ __device__ __forceinline__ void emit_group(EmitShared& sm, bool live, uint32_t g
       if (base_off + pad < capacity) {
         tile_keys[base_off + pad] = sentinel;
         tile_vals[base_off + pad] = g;
-        for (int p = 0; p < passes; ++p) atomicAdd(&sm.hist[p][(sentinel >> (p * digit_bits)) & mask], 1u);
       }
   }
   __syncwarp();  // the warp's tables are rewritten by the next group
@@ -593,15 +580,13 @@ __global__ void __launch_bounds__(kBlock) k_emit(const uint32_t* __restrict__ id
                                                  const uint32_t* __restrict__ ordered,
                                                  const uint32_t* __restrict__ offsets, BatchView bv, PassOptions o,
                                                  Control* __restrict__ ctl, uint32_t capacity,
-                                                 uint32_t* __restrict__ tile_keys, uint32_t* __restrict__ tile_vals,
-                                                 int passes, int digit_bits) {
+                                                 uint32_t* __restrict__ tile_keys, uint32_t* __restrict__ tile_vals) {
   if (ctl->state[3] != 0u) return;  // overflow: emission dispatch is zero
   __shared__ EmitShared sm;
   const uint32_t tid = threadIdx.x;
   const uint32_t n = ctl->visible_state[0];
   const uint32_t first = blockIdx.x * kBlock * G;
   if (first >= n) return;  // whole block past the visible count
-  for (uint32_t i = tid; i < kMaxSortPasses * 256; i += kBlock) (&sm.hist[0][0])[i] = 0u;
   uint32_t g[G], res[G], off[G];
   float4 m[G], c[G];
 #pragma unroll
@@ -623,33 +608,25 @@ __global__ void __launch_bounds__(kBlock) k_emit(const uint32_t* __restrict__ id
       c[h] = __ldg(conic + g[h]);
     }
   }
-  __syncthreads();  // histogram cleared
 #pragma unroll
   for (int h = 0; h < G; ++h) {
     const uint32_t r = first + (uint32_t)h * kBlock + tid;
-    emit_group(sm, r < n, g[h], m[h], c[h], res[h], off[h], bv, o, capacity, tile_keys, tile_vals, passes,
-               digit_bits);
+    emit_group(sm, r < n, g[h], m[h], c[h], res[h], off[h], bv, o, capacity, tile_keys, tile_vals);
   }
-  __syncthreads();
-  const uint32_t radix = 1u << digit_bits;
-  for (uint32_t d = tid; d < radix; d += kBlock)
-    for (int p = 0; p < passes; ++p)
-      if (sm.hist[p][d]) atomicAdd(&ctl->tile_hist[p][d], sm.hist[p][d]);
 }
 
 void launch_emit(const uint32_t* ids, uint32_t n_max, const float4* mean, const float4* conic,
                  const uint32_t* ordered, const uint32_t* offsets, const BatchView& b, const PassOptions& o,
-                 Control* ctl, uint32_t capacity, uint32_t* tile_keys, uint32_t* tile_vals, int passes,
-                 int digit_bits, cudaStream_t st) {
+                 Control* ctl, uint32_t capacity, uint32_t* tile_keys, uint32_t* tile_vals, cudaStream_t st) {
   if (n_max == 0) return;
   if (n_max >= kEmitTwoGroupsFrom) {
     const uint32_t grid = (n_max + 2 * kBlock - 1) / (2 * kBlock);
-    k_emit<2><<<grid, kBlock, 0, st>>>(ids, mean, conic, ordered, offsets, b, o, ctl, capacity, tile_keys, tile_vals,
-                                       passes, digit_bits);
+    k_emit<2><<<grid, kBlock, 0, st>>>(ids, mean, conic, ordered, offsets, b, o, ctl, capacity, tile_keys,
+                                       tile_vals);
   } else {
     const uint32_t grid = (n_max + kBlock - 1) / kBlock;
-    k_emit<1><<<grid, kBlock, 0, st>>>(ids, mean, conic, ordered, offsets, b, o, ctl, capacity, tile_keys, tile_vals,
-                                       passes, digit_bits);
+    k_emit<1><<<grid, kBlock, 0, st>>>(ids, mean, conic, ordered, offsets, b, o, ctl, capacity, tile_keys,
+                                       tile_vals);
   }
 }
 

@@ -721,7 +721,7 @@ void record_batch(gs3d_pipeline* p, const Plan& pl, unsigned char* dev, cudaStre
   // Visibility compaction.
   mark(p, GS3D_STAGE_COMPACT, st);
   const int depth_passes = p->desc.depth_sort_mode == GS3D_DEPTH_FLOAT32 ? 4 : 2;
-  launch_compact(p->keys, N, p->vis_off, p->dk[0], p->dv[0], ctl, p->status, epoch(), depth_passes, st);
+  launch_compact(p->keys, N, p->vis_off, p->dk[0], p->dv[0], ctl, p->status, epoch(), st);
   ++launches;
   // Depth sort.
   mark(p, GS3D_STAGE_DEPTH_SORT, st);
@@ -749,8 +749,7 @@ void record_batch(gs3d_pipeline* p, const Plan& pl, unsigned char* dev, cudaStre
   const uint32_t max_digit = p->tuning.tile_digit_bits;
   const int tile_passes = (int)std::min<uint32_t>(kMaxSortPasses, (tile_bits + max_digit - 1) / max_digit);
   const int digit_bits = (int)((tile_bits + tile_passes - 1) / tile_passes);
-  launch_emit(p->dv[cur], N, p->mean, p->conic, p->ordered, p->ioff, bv, o, ctl, cap32, p->tk[0], p->tv[0],
-              tile_passes, digit_bits, st);
+  launch_emit(p->dv[cur], N, p->mean, p->conic, p->ordered, p->ioff, bv, o, ctl, cap32, p->tk[0], p->tv[0], st);
   launches += N ? 1 : 0;
   // Tile sort.
   mark(p, GS3D_STAGE_TILE_SORT, st);

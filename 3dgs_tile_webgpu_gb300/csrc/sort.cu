@@ -11,10 +11,10 @@
 // which bounds it far below HBM speed on passes of tens of millions of keys).
 // The items split into `chunks` contiguous runs of whole 4096-item tiles (one
 // split, derived from the device-side count, shared by the three kernels):
-//   k_chunk_count   keys of every (chunk, digit), by shared-memory atomics;
+//   k_chunk_count   keys of every (chunk, digit), by shared-memory atomics,
+//                   also summed into the pass's global digit histogram;
 //   k_chunk_offsets per digit, the exclusive prefix over chunks plus the
-//                   digit's global base from the pass histogram (accumulated
-//                   by the kernel that produced the keys);
+//                   digit's global base from that histogram;
 //   k_chunk_scatter one block per chunk walks its tiles in order with running
 //                   per-digit offsets: tile t+1 streams into shared memory by
 //                   cp.async while tile t is ranked per digit within each warp
@@ -69,7 +69,8 @@ __device__ __forceinline__ void chunk_tiles(uint32_t n, uint32_t chunks, uint32_
 template <int BITS>
 __global__ void __launch_bounds__(kBlock) k_chunk_count(const uint32_t* __restrict__ keys,
                                                         const uint32_t* __restrict__ n_ptr, int shift,
-                                                        uint32_t chunks, uint32_t* __restrict__ counts) {
+                                                        uint32_t chunks, uint32_t* __restrict__ counts,
+                                                        uint32_t* __restrict__ hist) {
   constexpr uint32_t RADIX = 1u << BITS;
   constexpr uint32_t MASK = RADIX - 1u;
   __shared__ uint32_t s_hist[kSortWarps][RADIX];
@@ -116,6 +117,7 @@ __global__ void __launch_bounds__(kBlock) k_chunk_count(const uint32_t* __restri
 #pragma unroll
     for (int w = 0; w < kSortWarps; ++w) sum += s_hist[w][d];
     counts[(size_t)blockIdx.x * RADIX + d] = sum;
+    if (sum) atomicAdd(hist + d, sum);
   }
 }
 
@@ -308,9 +310,9 @@ __global__ void __launch_bounds__(kBlock, kChunkBlocksPerSm)
 
 template <int B>
 void launch_chunk_bits(uint32_t chunks, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
-                       uint32_t* vals_out, const uint32_t* n_ptr, int shift, const uint32_t* hist, uint32_t* counts,
+                       uint32_t* vals_out, const uint32_t* n_ptr, int shift, uint32_t* hist, uint32_t* counts,
                        cudaStream_t st) {
-  k_chunk_count<B><<<chunks, kBlock, 0, st>>>(keys_in, n_ptr, shift, chunks, counts);
+  k_chunk_count<B><<<chunks, kBlock, 0, st>>>(keys_in, n_ptr, shift, chunks, counts, hist);
   k_chunk_offsets<B><<<1u << B, kBlock, 0, st>>>(hist, chunks, counts);
   k_chunk_scatter<B><<<chunks, kBlock, kChunkDynSmem, st>>>(keys_in, vals_in, keys_out, vals_out, n_ptr, shift,
                                                            chunks, counts);
@@ -332,7 +334,7 @@ uint32_t chunk_pass_chunks(uint32_t n_max, int sms) {
 }
 
 void launch_chunk_pass(int bits, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
-                       uint32_t* vals_out, const uint32_t* n_ptr, int shift, const uint32_t* hist, uint32_t chunks,
+                       uint32_t* vals_out, const uint32_t* n_ptr, int shift, uint32_t* hist, uint32_t chunks,
                        uint32_t* counts, cudaStream_t st) {
 #define GS_CHUNK(B)                                                                                             \
   case B:                                                                                                       \

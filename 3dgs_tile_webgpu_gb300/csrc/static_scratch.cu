@@ -87,7 +87,7 @@ extern "C" gs3d_status gs3d_compact_visible_static(const uint32_t* keys, uint32_
   Control* ctl = reinterpret_cast<Control*>(scratch);
   unsigned long long* status = scratch + kControlWords;
   if (cudaMemsetAsync(ctl, 0, sizeof(Control), st) != cudaSuccess) return GS3D_ERROR_CUDA;
-  launch_compact(keys, n, visible_offsets, keys_out, ids_out, ctl, status, Epoch{nullptr, epoch}, 0, st);
+  launch_compact(keys, n, visible_offsets, keys_out, ids_out, ctl, status, Epoch{nullptr, epoch}, st);
   if (cudaMemcpyAsync(result, &ctl->visible_state[0], sizeof(uint32_t), cudaMemcpyDeviceToDevice, st) !=
           cudaSuccess ||
       cudaMemcpyAsync(result + 1, &ctl->error, sizeof(uint32_t), cudaMemcpyDeviceToDevice, st) != cudaSuccess)

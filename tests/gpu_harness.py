@@ -107,13 +107,20 @@ def psnr(a: np.ndarray, b: np.ndarray) -> float:
 
 
 def render_batch(scenes_frames: list, precision: str = "exact", capacity: int = 1 << 22,
-                 color_format: str = "rgba32f") -> list:
+                 color_format: str = "rgba32f", share_scenes: bool = False) -> list:
     """Render (scene, frame) pairs in one batch and split every buffer per view.
 
     Each view's result uses the view's own ordinals and local tile ids, so it
-    compares directly with a single-view oracle render of that view."""
+    compares directly with a single-view oracle render of that view. With
+    share_scenes, pairs holding the same scene object render from one resident
+    copy (one set of device buffers), so consecutive ones form a view group."""
     import torch
-    dss = [dev.DeviceScene(s) for s, _ in scenes_frames]
+    if share_scenes:
+        resident = {}
+        dss = [resident.setdefault(id(s), dev.DeviceScene(s)) if id(s) not in resident else resident[id(s)]
+               for s, _ in scenes_frames]
+    else:
+        dss = [dev.DeviceScene(s) for s, _ in scenes_frames]
     pipe = P.TiledGaussianPipeline(dss[0].data(), pipeline_options(scenes_frames[0][1], precision, capacity))
     targets, views = [], []
     for ds, (scene, frame) in zip(dss, scenes_frames):

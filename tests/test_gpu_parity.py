@@ -249,19 +249,60 @@ def test_batched_views_match_single_view_renders():
              (clouds[1], frames[4])]
     views, stats = render_batch(pairs, "exact")
     for (scene, frame), g in zip(pairs, views):
-        o = oracle.render(scene, frame, 0)
-        vis = o["tile_counts"] > 0
-        assert np.array_equal(g["tile_counts"], o["tile_counts"])
-        assert np.array_equal(g["proj_mean"].view(np.uint32), o["proj_mean"].view(np.uint32))
-        assert np.array_equal(g["proj_conic"][vis].view(np.uint32), o["proj_conic"][vis].view(np.uint32))
-        assert np.array_equal(g["proj_color"][vis].view(np.uint32), o["proj_color"][vis].view(np.uint32))
-        assert np.array_equal(g["visible_offsets"], o["visible_offsets"])
-        assert np.array_equal(g["depth_sorted"], o["depth_sorted"])
-        assert np.array_equal(g["ordered_counts"], o["ordered_counts"])
-        assert np.array_equal(g["sorted_records"], o["sorted_records"])
-        assert np.array_equal(g["tile_offsets"], o["tile_offsets"])
-        assert np.array_equal(g["rgba"].view(np.uint32), o["rgba"].view(np.uint32))
-        assert np.array_equal(g["depth"].view(np.uint32), o["depth"].view(np.uint32))
+        assert_view_matches_oracle(g, oracle.render(scene, frame, 0))
+
+
+def assert_view_matches_oracle(g, o):
+    vis = o["tile_counts"] > 0
+    assert np.array_equal(g["tile_counts"], o["tile_counts"])
+    assert np.array_equal(g["proj_mean"].view(np.uint32), o["proj_mean"].view(np.uint32))
+    assert np.array_equal(g["proj_conic"][vis].view(np.uint32), o["proj_conic"][vis].view(np.uint32))
+    assert np.array_equal(g["proj_color"][vis].view(np.uint32), o["proj_color"][vis].view(np.uint32))
+    assert np.array_equal(g["visible_offsets"], o["visible_offsets"])
+    assert np.array_equal(g["depth_sorted"], o["depth_sorted"])
+    assert np.array_equal(g["ordered_counts"], o["ordered_counts"])
+    assert np.array_equal(g["sorted_records"], o["sorted_records"])
+    assert np.array_equal(g["tile_offsets"], o["tile_offsets"])
+    assert np.array_equal(g["rgba"].view(np.uint32), o["rgba"].view(np.uint32))
+    assert np.array_equal(g["depth"].view(np.uint32), o["depth"].view(np.uint32))
+
+
+def test_view_groups_match_single_view_renders():
+    # Consecutive views of one resident scene form a view group: the
+    # projection decodes each splat once and projects it into every view of
+    # the group. Groups of three and two around a single view of another
+    # scene, mixed resolutions; every view bit-exact against the oracle.
+    from gpu_harness import render_batch
+    clouds = [cube(5000, seed=44), cube(3000, seed=45, log_scale=(-2.0, 0.5))]
+    frames = [cam(w=200, h=120), cam(eye=(3, 2, 9), w=97, h=64), cam(eye=(-4, 1, 10), w=160, h=96),
+              cam(eye=(0, 6, 8), w=33, h=17), cam(w=128, h=128), cam(eye=(2, -3, 9), w=64, h=100)]
+    pairs = [(clouds[0], frames[0]), (clouds[0], frames[1]), (clouds[0], frames[2]), (clouds[1], frames[3]),
+             (clouds[0], frames[4]), (clouds[0], frames[5])]
+    views, _ = render_batch(pairs, "exact", share_scenes=True)
+    for (scene, frame), g in zip(pairs, views):
+        assert_view_matches_oracle(g, oracle.render(scene, frame, 0))
+
+
+def test_view_groups_fp64_projection_match_single_views():
+    # The FP64 projection form over a view group equals single-view FP64
+    # renders bit for bit (the grouped decode feeds the same double chain).
+    from gpu_harness import render_batch
+    scene = sc.clustered_cloud(6000, seed=46, log_scale=(-2.0, 1.0), degenerate_fraction=0.5, centre_extent=5.0)
+    frames = [dict(cam(eye=e, w=w, h=h), projection_precision="fp64")
+              for e, w, h in [((0, 5, 30), 160, 96), ((4, 2, 25), 120, 80), ((-3, 6, 28), 97, 64)]]
+    views, _ = render_batch([(scene, f) for f in frames], "exact", share_scenes=True)
+    for frame, g in zip(frames, views):
+        run = GpuRun(scene, frame, "exact")
+        s = run.render(frame)
+        run.close()
+        vis = s["tile_counts"] > 0
+        assert vis.sum() > 100
+        assert np.array_equal(g["tile_counts"], s["tile_counts"])
+        assert np.array_equal(g["proj_mean"].view(np.uint32), s["proj_mean"].view(np.uint32))
+        assert np.array_equal(g["proj_conic"][vis].view(np.uint32), s["proj_conic"][vis].view(np.uint32))
+        assert np.array_equal(g["proj_color"][vis].view(np.uint32), s["proj_color"][vis].view(np.uint32))
+        assert np.array_equal(g["sorted_records"], s["sorted_records"])
+        assert np.array_equal(g["rgba"].view(np.uint32), s["rgba"].view(np.uint32))
 
 
 @pytest.mark.parametrize("name", ["default", "chunked", "capped"])
