@@ -79,8 +79,10 @@ __device__ __forceinline__ uint32_t find_view(const uint32_t* base, uint32_t nvi
 }
 
 constexpr uint32_t kMaxSortPasses = 4;  // digit histograms held per sort
-constexpr uint32_t kScanItems = 8;                      // items per thread of the look-back scans
-constexpr uint32_t kScanTile = kBlock * kScanItems;     // items per look-back tile (compaction, scan)
+// Persistent blocks per SM of the chunked look-back scans (compaction and
+// ordered-count scan); scan_chunks() = their grid for n_max items.
+constexpr uint32_t kScanBlocksPerSm = 4;
+uint32_t scan_chunks(uint32_t n_max, int sms);
 
 // Per-frame control block, zeroed before each render.
 struct Control {
@@ -239,10 +241,10 @@ void launch_project(const BatchView& b, const PassOptions& o, float4* mean, floa
                     uint32_t* counts, uint32_t* keys, float4* rec, cudaStream_t st);
 void launch_epoch_begin(uint32_t* epoch_base, cudaStream_t st);
 void launch_compact(const uint32_t* keys, uint32_t n, uint32_t* vis_off, uint32_t* keys_out, uint32_t* vals_out,
-                    Control* ctl, unsigned long long* status, Epoch epoch, cudaStream_t st);
-void launch_scan_counts(const uint32_t* sorted_ids, const uint32_t* tile_counts, uint32_t n_max,
-                        uint32_t* ordered, uint32_t* offsets, Control* ctl, unsigned long long* status,
-                        Epoch epoch, uint32_t capacity, const uint32_t* frame_params, uint32_t* output_state,
+                    Control* ctl, unsigned long long* status, Epoch epoch, uint32_t chunks, cudaStream_t st);
+void launch_scan_counts(const uint32_t* sorted_ids, const uint32_t* tile_counts, uint32_t* ordered,
+                        uint32_t* offsets, Control* ctl, unsigned long long* status, Epoch epoch,
+                        uint32_t capacity, const uint32_t* frame_params, uint32_t* output_state, uint32_t chunks,
                         cudaStream_t st);
 void launch_emit(const uint32_t* sorted_ids, uint32_t n_max, const float4* mean, const float4* conic,
                  const uint32_t* ordered, const uint32_t* offsets, const BatchView& b, const PassOptions& o,

@@ -6,6 +6,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
+
 #include "pass_common.cuh"
 #include "raster_impl.cuh"
 #include "splat_math.cuh"
@@ -286,53 +288,102 @@ void launch_project(const BatchView& b, const PassOptions& o, float4* mean, floa
 }
 
 // ---------------------------------------------------------------------------
-// Visibility compaction (scan.ts:9-83 + visibility.ts:9-61): one pass with
-// decoupled look-back. Writes visibleOffsets, the (depthKey, ordinal) records
-// in ordinal order and the visible state.
-constexpr uint32_t kItems = kScanItems;
+// Chunked look-back scans (visibility compaction, ordered-count scan): a
+// persistent grid of `chunks` blocks; chunk c (tickets give launch order) is a
+// contiguous run of 256-item units, split into one contiguous slice per warp.
+// Phase 1 reduces each warp's slice, warp 0 combines the warps and resolves
+// the chunk's prefix by decoupled look-back (one chain step per chunk, not per
+// 2048 items), and phase 2 walks the slice again writing every output with
+// the warp's running offset. A unit is 8 rows of 32 consecutive items, so
+// every load and store of a row is one coalesced 128-byte access.
+constexpr uint32_t kUnit = 256;
+constexpr uint32_t kUnitRows = kUnit / 32;
+constexpr uint32_t kScanWarps = kBlock / 32;
 
+__device__ __forceinline__ void chunk_units(uint32_t n, uint32_t chunks, uint32_t c, uint32_t* u0, uint32_t* u1) {
+  const uint32_t units = (uint32_t)(((uint64_t)n + kUnit - 1) / kUnit);
+  const uint32_t per = (units + chunks - 1) / chunks;
+  *u0 = min(c * per, units);
+  *u1 = min(*u0 + per, units);
+}
+
+__device__ __forceinline__ void warp_units(uint32_t u0, uint32_t u1, uint32_t warp, uint32_t* w0, uint32_t* w1) {
+  const uint32_t m = u1 - u0, per = (m + kScanWarps - 1) / kScanWarps;
+  *w0 = u0 + min(warp * per, m);
+  *w1 = u0 + min((warp + 1) * per, m);
+}
+
+// Called by all 32 lanes of warp 0: combines the warps' sums in s_warp
+// (replaced by each warp's exclusive base), publishes chunk c and looks back.
+// Every lane gets the chunk's exclusive prefix and its total.
+template <bool SAT>
+__device__ __forceinline__ void chunk_publish(uint32_t* s_warp, unsigned long long* status, uint32_t c,
+                                              uint32_t epoch, uint32_t* err, uint32_t* prefix_out,
+                                              uint32_t* total_out) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t wc = lane < kScanWarps ? s_warp[lane] : 0u;
+  uint32_t incl = wc;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= (uint32_t)d) incl = SAT ? sat_add(y, incl) : y + incl;
+  }
+  const uint32_t total = __shfl_sync(0xffffffffu, incl, kScanWarps - 1);
+  const uint32_t up = __shfl_up_sync(0xffffffffu, incl, 1);
+  const uint32_t excl = lane ? up : 0u;
+  unsigned long long* mine = status + c;
+  uint32_t prefix = 0;
+  if (c == 0) {
+    if (lane == 0) st_release(mine, pack_status(epoch, kFlagInclusive, total));
+  } else {
+    if (lane == 0) st_release(mine, pack_status(epoch, kFlagAggregate, total));
+    prefix = warp_lookback<SAT>(status, c, epoch, err);
+    if (lane == 0) st_release(mine, pack_status(epoch, kFlagInclusive, SAT ? sat_add(prefix, total) : prefix + total));
+  }
+  if (lane < kScanWarps) s_warp[lane] = SAT ? sat_add(prefix, excl) : prefix + excl;
+  *prefix_out = prefix;
+  *total_out = total;
+}
+
+// Visibility compaction (scan.ts:9-83 + visibility.ts:9-61). Writes
+// visibleOffsets, the (depthKey, ordinal) records in ordinal order and the
+// visible state.
 __global__ void __launch_bounds__(kBlock) k_compact(const uint32_t* __restrict__ keys, uint32_t n,
                                                     uint32_t* __restrict__ vis_off, uint32_t* __restrict__ keys_out,
                                                     uint32_t* __restrict__ vals_out, Control* __restrict__ ctl,
-                                                    unsigned long long* __restrict__ status, Epoch ep) {
-  const uint32_t epoch = ep.get();
-  __shared__ uint32_t s_tile, s_prefix;
-  __shared__ uint32_t s_warp[kBlock / 32];
-  const uint32_t tid = threadIdx.x;
-  if (tid == 0) s_tile = atomicAdd(&ctl->tickets[kTicketCompact], 1u);
+                                                    unsigned long long* __restrict__ status, Epoch ep,
+                                                    uint32_t chunks) {
+  __shared__ uint32_t s_chunk;
+  __shared__ uint32_t s_warp[kScanWarps];
+  const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+  if (tid == 0) s_chunk = atomicAdd(&ctl->tickets[kTicketCompact], 1u);
   __syncthreads();
-  const uint32_t tile = s_tile;
-  const uint32_t ntiles = n == 0 ? 1u : (n + kScanTile - 1) / kScanTile;
-  if (tile >= ntiles) return;
-  const uint32_t base = tile * kScanTile + tid * kItems;
-  uint32_t k[kItems];
-  if (base + kItems <= n) {
+  const uint32_t c = s_chunk;
+  uint32_t u0, u1;
+  chunk_units(n, chunks, c, &u0, &u1);
+  if (u0 >= u1 && !(n == 0 && c == 0)) return;  // chunks past the last item do nothing
+  const bool last = (uint64_t)u1 * kUnit >= n;
+  uint32_t w0, w1;
+  warp_units(u0, u1, warp, &w0, &w1);
+  const uint32_t lt = (1u << lane) - 1u;
+
+  uint32_t cnt = 0;
+  for (uint32_t u = w0; u < w1; ++u) {
+    uint32_t k[kUnitRows];
 #pragma unroll
-    for (uint32_t q = 0; q < kItems / 4; ++q) {
-      const uint4 w = *reinterpret_cast<const uint4*>(keys + base + 4 * q);
-      k[4 * q] = w.x; k[4 * q + 1] = w.y; k[4 * q + 2] = w.z; k[4 * q + 3] = w.w;
+    for (uint32_t j = 0; j < kUnitRows; ++j) {
+      const uint32_t idx = u * kUnit + j * 32u + lane;
+      k[j] = idx < n ? keys[idx] : kInvisibleKey;
     }
-  } else {
 #pragma unroll
-    for (uint32_t i = 0; i < kItems; ++i) k[i] = base + i < n ? keys[base + i] : kInvisibleKey;
+    for (uint32_t j = 0; j < kUnitRows; ++j) cnt += __popc(__ballot_sync(0xffffffffu, k[j] != kInvisibleKey));
   }
-  uint32_t c = 0;
-#pragma unroll
-  for (uint32_t i = 0; i < kItems; ++i) c += k[i] != kInvisibleKey ? 1u : 0u;
-  uint32_t total;
-  const uint32_t excl = block_exclusive_scan<false>(c, s_warp, &total);
-  if (tid < 32) {
-    unsigned long long* mine = status + tile;
-    uint32_t prefix = 0;
-    if (tile == 0) {
-      if (tid == 0) st_release(mine, pack_status(epoch, kFlagInclusive, total));
-    } else {
-      if (tid == 0) st_release(mine, pack_status(epoch, kFlagAggregate, total));
-      prefix = warp_lookback<false>(status, tile, epoch, &ctl->error);
-      if (tid == 0) st_release(mine, pack_status(epoch, kFlagInclusive, prefix + total));
-    }
-    if (tid == 0) s_prefix = prefix;
-    if (tid == 0 && tile == ntiles - 1) {
+  if (lane == 0) s_warp[warp] = cnt;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t prefix, total;
+    chunk_publish<false>(s_warp, status, c, ep.get(), &ctl->error, &prefix, &total);
+    if (lane == 0 && last) {
       const uint32_t v = prefix + total;
       ctl->visible_state[0] = v;
       ctl->visible_state[1] = v;
@@ -341,16 +392,29 @@ __global__ void __launch_bounds__(kBlock) k_compact(const uint32_t* __restrict__
     }
   }
   __syncthreads();
-  uint32_t off = s_prefix + excl;
+
+  uint32_t run = s_warp[warp];
+  for (uint32_t u = w0; u < w1; ++u) {
+    uint32_t k[kUnitRows];
 #pragma unroll
-  for (uint32_t i = 0; i < kItems; ++i) {
-    const uint32_t idx = base + i;
-    if (idx >= n) break;
-    vis_off[idx] = off;
-    if (k[i] != kInvisibleKey) {
-      keys_out[off] = k[i];
-      vals_out[off] = idx;
-      ++off;
+    for (uint32_t j = 0; j < kUnitRows; ++j) {
+      const uint32_t idx = u * kUnit + j * 32u + lane;
+      k[j] = idx < n ? keys[idx] : kInvisibleKey;
+    }
+#pragma unroll
+    for (uint32_t j = 0; j < kUnitRows; ++j) {
+      const uint32_t idx = u * kUnit + j * 32u + lane;
+      const bool vis = k[j] != kInvisibleKey;
+      const uint32_t bal = __ballot_sync(0xffffffffu, vis);
+      const uint32_t pos = run + __popc(bal & lt);
+      if (idx < n) {
+        vis_off[idx] = pos;
+        if (vis) {
+          keys_out[pos] = k[j];
+          vals_out[pos] = idx;
+        }
+      }
+      run += __popc(bal);
     }
   }
 }
@@ -363,54 +427,68 @@ __global__ void k_epoch_begin(uint32_t* base) {
 
 void launch_epoch_begin(uint32_t* epoch_base, cudaStream_t st) { k_epoch_begin<<<1, 1, 0, st>>>(epoch_base); }
 
-void launch_compact(const uint32_t* keys, uint32_t n, uint32_t* vis_off, uint32_t* keys_out, uint32_t* vals_out,
-                    Control* ctl, unsigned long long* status, Epoch epoch, cudaStream_t st) {
-  const uint32_t grid = n == 0 ? 1u : (n + kScanTile - 1) / kScanTile;
-  k_compact<<<grid, kBlock, 0, st>>>(keys, n, vis_off, keys_out, vals_out, ctl, status, epoch);
+uint32_t scan_chunks(uint32_t n_max, int sms) {
+  const uint64_t units = ((uint64_t)n_max + kUnit - 1) / kUnit;
+  return (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(units, (uint64_t)kScanBlocksPerSm * (uint64_t)sms));
 }
 
-// ---------------------------------------------------------------------------
+void launch_compact(const uint32_t* keys, uint32_t n, uint32_t* vis_off, uint32_t* keys_out, uint32_t* vals_out,
+                    Control* ctl, unsigned long long* status, Epoch epoch, uint32_t chunks, cudaStream_t st) {
+  k_compact<<<chunks, kBlock, 0, st>>>(keys, n, vis_off, keys_out, vals_out, ctl, status, epoch, chunks);
+}
+
 // Depth-ordered tile counts + saturating exclusive scan + prepare_dispatch +
 // prepare_intersection_output (visibility.ts:63-76, scan.ts:9-99,
-// intersections.ts:10-41,114-133) in one look-back pass over visible ranks.
+// intersections.ts:10-41,114-133) over the visible ranks. Phase 1 gathers
+// each rank's tile count, writes it (the ordered counts) and reduces; phase 2
+// re-reads the ordered counts and writes the saturating offsets.
 __global__ void __launch_bounds__(kBlock) k_scan_counts(const uint32_t* __restrict__ ids,
                                                         const uint32_t* __restrict__ tile_counts,
                                                         uint32_t* __restrict__ ordered,
                                                         uint32_t* __restrict__ offsets, Control* __restrict__ ctl,
                                                         unsigned long long* __restrict__ status, Epoch ep,
                                                         uint32_t capacity, const uint32_t* __restrict__ frame_params,
-                                                        uint32_t* __restrict__ output_state) {
-  const uint32_t epoch = ep.get();
-  __shared__ uint32_t s_tile, s_prefix;
-  __shared__ uint32_t s_warp[kBlock / 32];
-  const uint32_t tid = threadIdx.x;
-  if (tid == 0) s_tile = atomicAdd(&ctl->tickets[kTicketScan], 1u);
+                                                        uint32_t* __restrict__ output_state, uint32_t chunks) {
+  __shared__ uint32_t s_chunk;
+  __shared__ uint32_t s_warp[kScanWarps];
+  const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+  if (tid == 0) s_chunk = atomicAdd(&ctl->tickets[kTicketScan], 1u);
   __syncthreads();
   const uint32_t n = ctl->visible_state[0];
-  const uint32_t tile = s_tile;
-  const uint32_t ntiles = n == 0 ? 1u : (n + kScanTile - 1) / kScanTile;
-  if (tile >= ntiles) return;
-  const uint32_t base = tile * kScanTile + tid * kItems;
-  uint32_t c[kItems];
-#pragma unroll
-  for (uint32_t i = 0; i < kItems; ++i) c[i] = base + i < n ? __ldg(tile_counts + ids[base + i]) : 0u;
+  const uint32_t c = s_chunk;
+  uint32_t u0, u1;
+  chunk_units(n, chunks, c, &u0, &u1);
+  if (u0 >= u1 && !(n == 0 && c == 0)) return;
+  const bool last = (uint64_t)u1 * kUnit >= n;
+  uint32_t w0, w1;
+  warp_units(u0, u1, warp, &w0, &w1);
+
   uint32_t sum = 0;
+  for (uint32_t u = w0; u < w1; ++u) {
+    uint32_t id[kUnitRows];
 #pragma unroll
-  for (uint32_t i = 0; i < kItems; ++i) sum = sat_add(sum, c[i]);
-  uint32_t total;
-  const uint32_t excl = block_exclusive_scan<true>(sum, s_warp, &total);
-  if (tid < 32) {
-    unsigned long long* mine = status + tile;
-    uint32_t prefix = 0;
-    if (tile == 0) {
-      if (tid == 0) st_release(mine, pack_status(epoch, kFlagInclusive, total));
-    } else {
-      if (tid == 0) st_release(mine, pack_status(epoch, kFlagAggregate, total));
-      prefix = warp_lookback<true>(status, tile, epoch, &ctl->error);
-      if (tid == 0) st_release(mine, pack_status(epoch, kFlagInclusive, sat_add(prefix, total)));
+    for (uint32_t j = 0; j < kUnitRows; ++j) {
+      const uint32_t r = u * kUnit + j * 32u + lane;
+      id[j] = r < n ? ids[r] : 0u;
     }
-    if (tid == 0) s_prefix = prefix;
-    if (tid == 0 && tile == ntiles - 1) {
+#pragma unroll
+    for (uint32_t j = 0; j < kUnitRows; ++j) {
+      const uint32_t r = u * kUnit + j * 32u + lane;
+      if (r < n) {
+        const uint32_t cnt = __ldg(tile_counts + id[j]);
+        ordered[r] = cnt;
+        sum = sat_add(sum, cnt);
+      }
+    }
+  }
+#pragma unroll
+  for (int d = 16; d >= 1; d >>= 1) sum = sat_add(sum, __shfl_xor_sync(0xffffffffu, sum, d));
+  if (lane == 0) s_warp[warp] = sum;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t prefix, total;
+    chunk_publish<true>(s_warp, status, c, ep.get(), &ctl->error, &prefix, &total);
+    if (lane == 0 && last) {
       const uint32_t all = sat_add(prefix, total);
       const bool overflow = all > capacity;
       const uint32_t count = overflow ? 0u : all;
@@ -427,24 +505,36 @@ __global__ void __launch_bounds__(kBlock) k_scan_counts(const uint32_t* __restri
     }
   }
   __syncthreads();
-  uint32_t run = sat_add(s_prefix, excl);
+
+  uint32_t run = s_warp[warp];
+  for (uint32_t u = w0; u < w1; ++u) {
+    uint32_t cnt[kUnitRows];
 #pragma unroll
-  for (uint32_t i = 0; i < kItems; ++i) {
-    const uint32_t idx = base + i;
-    if (idx < n) {
-      ordered[idx] = c[i];
-      offsets[idx] = run;
+    for (uint32_t j = 0; j < kUnitRows; ++j) {
+      const uint32_t r = u * kUnit + j * 32u + lane;
+      cnt[j] = r < n ? ordered[r] : 0u;  // written by this thread in phase 1
     }
-    run = sat_add(run, c[i]);
+#pragma unroll
+    for (uint32_t j = 0; j < kUnitRows; ++j) {
+      const uint32_t r = u * kUnit + j * 32u + lane;
+      uint32_t incl = cnt[j];
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= (uint32_t)d) incl = sat_add(y, incl);
+      }
+      const uint32_t excl = __shfl_up_sync(0xffffffffu, incl, 1);
+      if (r < n) offsets[r] = sat_add(run, lane ? excl : 0u);
+      run = sat_add(run, __shfl_sync(0xffffffffu, incl, 31));
+    }
   }
 }
 
-void launch_scan_counts(const uint32_t* ids, const uint32_t* tile_counts, uint32_t n_max, uint32_t* ordered,
-                        uint32_t* offsets, Control* ctl, unsigned long long* status, Epoch epoch,
-                        uint32_t capacity, const uint32_t* frame_params, uint32_t* output_state, cudaStream_t st) {
-  const uint32_t grid = n_max == 0 ? 1u : (n_max + kScanTile - 1) / kScanTile;
-  k_scan_counts<<<grid, kBlock, 0, st>>>(ids, tile_counts, ordered, offsets, ctl, status, epoch, capacity,
-                                         frame_params, output_state);
+void launch_scan_counts(const uint32_t* ids, const uint32_t* tile_counts, uint32_t* ordered, uint32_t* offsets,
+                        Control* ctl, unsigned long long* status, Epoch epoch, uint32_t capacity,
+                        const uint32_t* frame_params, uint32_t* output_state, uint32_t chunks, cudaStream_t st) {
+  k_scan_counts<<<chunks, kBlock, 0, st>>>(ids, tile_counts, ordered, offsets, ctl, status, epoch, capacity,
+                                           frame_params, output_state, chunks);
 }
 
 // ---------------------------------------------------------------------------

@@ -234,11 +234,11 @@ gs3d_status validate_data(gs3d_pipeline* p, const gs3d_gaussian_data* d) {
   return GS3D_OK;
 }
 
-// Look-back status words of the compaction and the ordered-count scan (one
-// per tile of at least 1024 items).
+// Look-back status words of the compaction and the ordered-count scan: one
+// per chunk, at most one chunk per 256 items.
 size_t status_words_needed(uint32_t slots, uint64_t capacity) {
   (void)capacity;
-  return (slots + 1023u) / 1024u + 1;
+  return (slots + 255u) / 256u + 1;
 }
 
 gs3d_status ensure_status(gs3d_pipeline* p) {
@@ -721,7 +721,8 @@ void record_batch(gs3d_pipeline* p, const Plan& pl, unsigned char* dev, cudaStre
   // Visibility compaction.
   mark(p, GS3D_STAGE_COMPACT, st);
   const int depth_passes = p->desc.depth_sort_mode == GS3D_DEPTH_FLOAT32 ? 4 : 2;
-  launch_compact(p->keys, N, p->vis_off, p->dk[0], p->dv[0], ctl, p->status, epoch(), st);
+  const uint32_t scan_grid = scan_chunks(N, p->sms);
+  launch_compact(p->keys, N, p->vis_off, p->dk[0], p->dv[0], ctl, p->status, epoch(), scan_grid, st);
   ++launches;
   // Depth sort.
   mark(p, GS3D_STAGE_DEPTH_SORT, st);
@@ -737,8 +738,8 @@ void record_batch(gs3d_pipeline* p, const Plan& pl, unsigned char* dev, cudaStre
   // Ordered counts + saturating scan + dispatch/output state.
   mark(p, GS3D_STAGE_SCAN, st);
   const uint32_t cap32 = (uint32_t)p->capacity;
-  launch_scan_counts(p->dv[cur], p->counts, N, p->ordered, p->ioff, ctl, p->status, epoch(), cap32,
-                     bv.frame_params, p->output_state, st);
+  launch_scan_counts(p->dv[cur], p->counts, p->ordered, p->ioff, ctl, p->status, epoch(), cap32, bv.frame_params,
+                     p->output_state, scan_grid, st);
   ++launches;
   // Emission + tile-sort histograms.
   mark(p, GS3D_STAGE_EMIT, st);

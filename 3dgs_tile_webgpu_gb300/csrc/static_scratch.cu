@@ -10,7 +10,7 @@
 // words and the per-call control block) lives in the fixed device array
 // below instead of memory allocated per pipeline.
 //
-// Cost of the array: kStaticScratchWords * 8 bytes (about 140 KB), held on
+// Cost of the array: kStaticScratchWords * 8 bytes (about 40 KB), held on
 // every GPU that loads the library until the process exits.
 //
 // Rules for callers:
@@ -26,6 +26,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <mutex>
 
 #include "../../include/gs3d.h"
@@ -35,9 +36,8 @@ using namespace gs;
 
 namespace {
 
-constexpr uint32_t kCompactTile = kScanTile;  // items per look-back tile of k_compact
 constexpr size_t kControlWords = (sizeof(Control) + 7) / 8;
-constexpr size_t kStatusWords = GS3D_STATIC_COMPACT_MAX_ITEMS / kCompactTile + 1;
+constexpr size_t kStatusWords = 4096;  // one per chunk of k_compact; the grid is capped to this
 constexpr size_t kStaticScratchWords = kControlWords + kStatusWords;
 static_assert(sizeof(Control) % 8 == 0, "control block must be a whole number of words");
 
@@ -48,6 +48,7 @@ constexpr int kMaxDevices = 64;
 std::mutex g_mutex;
 unsigned long long* g_scratch_ptr[kMaxDevices] = {};
 uint32_t g_epoch[kMaxDevices] = {};
+int g_sms[kMaxDevices] = {};
 
 }  // namespace
 
@@ -63,6 +64,7 @@ extern "C" gs3d_status gs3d_compact_visible_static(const uint32_t* keys, uint32_
   cudaStream_t st = (cudaStream_t)stream;
   unsigned long long* scratch = nullptr;
   uint32_t epoch = 0;
+  int sms = 1;
   {
     std::lock_guard<std::mutex> lock(g_mutex);
     if (!g_scratch_ptr[device]) {
@@ -73,8 +75,14 @@ extern "C" gs3d_status gs3d_compact_visible_static(const uint32_t* keys, uint32_
         return GS3D_ERROR_CUDA;
       }
       g_scratch_ptr[device] = (unsigned long long*)p;
+      if (cudaDeviceGetAttribute(&g_sms[device], cudaDevAttrMultiProcessorCount, device) != cudaSuccess) {
+        cudaGetLastError();
+        g_scratch_ptr[device] = nullptr;
+        return GS3D_ERROR_CUDA;
+      }
     }
     scratch = g_scratch_ptr[device];
+    sms = g_sms[device];
     uint32_t e = (g_epoch[device] + 1u) & ((1u << 30) - 1u);
     if (e == 0) {
       // Epoch wrapped: clear the status words so no stale word can match.
@@ -87,7 +95,8 @@ extern "C" gs3d_status gs3d_compact_visible_static(const uint32_t* keys, uint32_
   Control* ctl = reinterpret_cast<Control*>(scratch);
   unsigned long long* status = scratch + kControlWords;
   if (cudaMemsetAsync(ctl, 0, sizeof(Control), st) != cudaSuccess) return GS3D_ERROR_CUDA;
-  launch_compact(keys, n, visible_offsets, keys_out, ids_out, ctl, status, Epoch{nullptr, epoch}, st);
+  const uint32_t chunks = std::min<uint32_t>(scan_chunks(n, sms), (uint32_t)kStatusWords);
+  launch_compact(keys, n, visible_offsets, keys_out, ids_out, ctl, status, Epoch{nullptr, epoch}, chunks, st);
   if (cudaMemcpyAsync(result, &ctl->visible_state[0], sizeof(uint32_t), cudaMemcpyDeviceToDevice, st) !=
           cudaSuccess ||
       cudaMemcpyAsync(result + 1, &ctl->error, sizeof(uint32_t), cudaMemcpyDeviceToDevice, st) != cudaSuccess)

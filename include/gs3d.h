@@ -382,7 +382,7 @@ gs3d_status gs3d_pack_splats(const gs3d_splat_source* source, uint32_t first_slo
  * where they enqueue work: code running during CUDA graph capture, hosts that
  * route all device memory through their own arena, real-time loops that must
  * not stall on the allocator. The caller passes every input and output; the
- * kernel's scratch is a static device array of about 140 KB per GPU, held
+ * kernel's scratch is a static device array of about 40 KB per GPU, held
  * until the process exits.
  *   keys[n]            per-ordinal depth key, 0xffffffff = not visible
  *   visible_offsets[n] exclusive count of visible ordinals before each one
