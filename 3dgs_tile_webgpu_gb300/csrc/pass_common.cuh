@@ -47,6 +47,7 @@ struct PassOptions {
   float depth_alpha_threshold;
   float invalid_depth;
   uint32_t proj_fp64;      // 1: FP64 far-origin mean transform and near-singular conic
+  uint32_t any_depth;      // some view of the launch has a depth target
 };
 
 // The batch table in device memory: the per-frame parameters (attempt,

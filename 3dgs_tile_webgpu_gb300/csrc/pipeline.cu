@@ -516,6 +516,7 @@ size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
 
 struct Plan {
   uint32_t n = 0, ngroups = 0;
+  bool any_depth = false;
   uint32_t items = 0, tiles = 0, blocks = 0;
   size_t objects = 0;
   size_t views_off = 0, objects_off = 0, stage_bytes = 0;
@@ -548,6 +549,7 @@ gs3d_status plan_batch(gs3d_pipeline* p, const gs3d_view* views, uint32_t n, Pla
   if (n == 0 || n > kMaxViews) return fail(p, GS3D_ERROR_RANGE, "a batch holds 1 to 4096 views");
   uint64_t items = 0, tiles = 0, blocks = 0;
   uint32_t ngroups = 0;
+  bool any_depth = false;
   size_t objects = 0;
   for (uint32_t i = 0; i < n; ++i) {
     const gs3d_view& v = views[i];
@@ -560,6 +562,7 @@ gs3d_status plan_batch(gs3d_pipeline* p, const gs3d_view* views, uint32_t n, Pla
     if (!(v.camera->depth_near >= 0.0f) || !(v.camera->depth_far > v.camera->depth_near))
       return fail(p, GS3D_ERROR_RANGE, "depth range must satisfy 0 <= near < far");
     if (v.width == 0 || v.height == 0) return fail(p, GS3D_ERROR_RANGE, "render size must be positive");
+    any_depth = any_depth || v.targets.depth != nullptr;
     const uint32_t tx = tiles_for(v.width), ty = tiles_for(v.height);
     // TiledGaussianPipeline.ts:294-296
     if (tx > 65535u || ty > 65535u) return fail(p, GS3D_ERROR_RANGE, "Render size exceeds WebGPU's tile dispatch limit");
@@ -584,6 +587,7 @@ gs3d_status plan_batch(gs3d_pipeline* p, const gs3d_view* views, uint32_t n, Pla
   if ((s = ensure_tiles(p, tiles)) != GS3D_OK) return s;
   out->n = n;
   out->ngroups = ngroups;
+  out->any_depth = any_depth;
   out->items = (uint32_t)items;
   out->tiles = (uint32_t)tiles;
   out->blocks = (uint32_t)blocks;
@@ -698,6 +702,7 @@ void record_batch(gs3d_pipeline* p, const Plan& pl, unsigned char* dev, cudaStre
   o.max_per_tile = p->desc.max_rasterized_splats_per_tile;
   o.depth_encoding = p->desc.depth_encoding;
   o.proj_fp64 = p->desc.projection_precision == GS3D_PROJECTION_FP64 ? 1u : 0u;
+  o.any_depth = pl.any_depth ? 1u : 0u;
   memcpy(o.background, p->desc.background, sizeof(o.background));
   o.t_threshold = p->desc.raster_transmittance_threshold;
   o.depth_alpha_threshold = p->desc.depth_alpha_threshold;

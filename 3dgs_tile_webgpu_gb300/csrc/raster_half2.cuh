@@ -56,18 +56,21 @@ struct WarpStage {
   uint8_t idx[32]; // lane (record offset within the group) of each staged record
 };
 
+// DEPTH: some view of the launch has a depth target (otherwise the depth sum
+// is never read and is not accumulated).
+template <bool DEPTH>
 __device__ __forceinline__ void blend_pixel(float alpha, const float4& col, float depth, PixelAcc& a) {
   const float contrib = a.t * alpha;
   a.r = a.r + col.x * contrib;
   a.g = a.g + col.y * contrib;
   a.b = a.b + col.z * contrib;
-  a.d = a.d + depth * contrib;
+  if (DEPTH) a.d = a.d + depth * contrib;
   a.t = a.t - contrib;
 }
 
 // Blend records [s0, s1) of the tile into this warp's two pixels per lane.
 // Warp-level: needs no other warp of the block.
-template <bool HALF, bool PERIODIC, bool STATS>
+template <bool HALF, bool PERIODIC, bool STATS, bool DEPTH>
 __device__ __forceinline__ void blend_range_h2(uint32_t begin, uint32_t source_count, uint32_t raster_count,
                                                uint32_t s0, uint32_t s1, bool capped,
                                                const uint32_t* __restrict__ ids, const float4* __restrict__ mean,
@@ -94,7 +97,7 @@ __device__ __forceinline__ void blend_range_h2(uint32_t begin, uint32_t source_c
       r0 = __ldg(rec + 2 * (size_t)g);  // one 32-byte record
       r1 = __ldg(rec + 2 * (size_t)g + 1);
       if (!HALF) col32 = __ldg(color + g);
-      if (need_depth) depth = __ldg(&mean[g].z);
+      if (DEPTH && need_depth) depth = __ldg(&mean[g].z);
       reach = PERIODIC || patch_reach(r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, patch_x0 + 0.5f, patch_y0 + 0.5f,
                                           7.0f, 7.0f);
     }
@@ -152,14 +155,14 @@ __device__ __forceinline__ void blend_range_h2(uint32_t begin, uint32_t source_c
       }
       const float4 col = ws.col[j];
       if (use0) {
-        blend_pixel(al.x, col, c.w, a0);
+        blend_pixel<DEPTH>(al.x, col, c.w, a0);
         if (STATS) {
           ++c0n.blended;
           if (a0.t < f.t_threshold && stop0 == s1) stop0 = b + ws.idx[j] + 1;
         }
       }
       if (use1) {
-        blend_pixel(al.y, col, c.w, a1);
+        blend_pixel<DEPTH>(al.y, col, c.w, a1);
         if (STATS) {
           ++c1n.blended;
           if (a1.t < f.t_threshold && stop1 == s1) stop1 = b + ws.idx[j] + 1;
@@ -196,7 +199,7 @@ __device__ __forceinline__ void store_pixel(const ViewDesc& v, const PassOptions
   if (v.depth) v.depth[off] = finalize_depth(a.d, a.t, o, v.vnear, v.vfar);
 }
 
-template <bool HALF, bool PERIODIC, bool STATS>
+template <bool HALF, bool PERIODIC, bool STATS, bool DEPTH>
 __global__ void __launch_bounds__(kHalfThreads, HALF ? 9 : 8) k_raster_h2(const uint32_t* __restrict__ tile_offsets,
                                                            const uint32_t* __restrict__ order,
                                                            const uint32_t* __restrict__ ids,
@@ -235,7 +238,7 @@ __global__ void __launch_bounds__(kHalfThreads, HALF ? 9 : 8) k_raster_h2(const 
   PixelAcc a0 = {0.0f, 0.0f, 0.0f, 1.0f, 0.0f}, a1 = a0;
   RasterCounters n0 = {0u, 0u}, n1 = {0u, 0u};
   if (!chunked) {
-    blend_range_h2<HALF, PERIODIC, STATS>(begin, source_count, raster_count, 0, raster_count, capped, ids, mean,
+    blend_range_h2<HALF, PERIODIC, STATS, DEPTH>(begin, source_count, raster_count, 0, raster_count, capped, ids, mean,
                                           color, rec, need_depth, f, (float)patch_x, (float)patch_y, pxc, pyc0, !active0, !active1, a0,
                                     a1, ws, n0, n1);
   } else {
@@ -245,7 +248,7 @@ __global__ void __launch_bounds__(kHalfThreads, HALF ? 9 : 8) k_raster_h2(const 
       if (__all_sync(0xffffffffu, fin0 && fin1)) break;
       const uint32_t s0 = ch * chunk, s1 = min(s0 + chunk, raster_count);
       PixelAcc p0 = {0.0f, 0.0f, 0.0f, 1.0f, 0.0f}, p1 = p0;
-      blend_range_h2<HALF, PERIODIC, STATS>(begin, source_count, raster_count, s0, s1, capped, ids, mean, color,
+      blend_range_h2<HALF, PERIODIC, STATS, DEPTH>(begin, source_count, raster_count, s0, s1, capped, ids, mean, color,
                                             rec, need_depth,
                                       f, (float)patch_x, (float)patch_y, pxc, pyc0, fin0, fin1, p0, p1, ws, n0, n1);
       if (!fin0) {
@@ -281,29 +284,36 @@ __global__ void __launch_bounds__(kHalfThreads, HALF ? 9 : 8) k_raster_h2(const 
   if (active1) store_pixel(v, o, px, py1, a1);
 }
 
-// half = true: packed half2 form; false: FP32 form.
+// half = true: packed half2 form; false: FP32 form. o.any_depth: some view
+// of the launch has a depth target.
+template <bool HALF, bool PERIODIC>
+inline void launch_raster_pairs_t(const uint32_t* tile_offsets, const uint32_t* order, const uint32_t* ids,
+                                  const float4* mean, const float4* color, const float4* rec, const BatchView& b,
+                                  const PassOptions& o, Control* ctl, bool stats, cudaStream_t st) {
+#define GS_RASTER_H2(S, D)                                                                                       \
+  k_raster_h2<HALF, PERIODIC, S, D><<<b.total_tiles, kHalfThreads, 0, st>>>(tile_offsets, order, ids, mean, color, \
+                                                                           rec, b, o, ctl)
+  const bool depth = o.any_depth != 0u;
+  if (stats) {
+    if (depth) GS_RASTER_H2(true, true); else GS_RASTER_H2(true, false);
+  } else {
+    if (depth) GS_RASTER_H2(false, true); else GS_RASTER_H2(false, false);
+  }
+#undef GS_RASTER_H2
+}
+
 inline void launch_raster_pairs(bool half, const uint32_t* tile_offsets, const uint32_t* order, const uint32_t* ids,
                                 const float4* mean, const float4* color, const float4* rec, const BatchView& b,
                                 const PassOptions& o, Control* ctl, bool stats, cudaStream_t st) {
   if (b.total_tiles == 0) return;
-#define GS_RASTER_H2(H, P, S)                                                                                   \
-  k_raster_h2<H, P, S><<<b.total_tiles, kHalfThreads, 0, st>>>(tile_offsets, order, ids, mean, color, rec, b, o, \
-                                                               ctl)
   const bool periodic = o.axis != 0u;
   if (half) {
-    if (periodic) {
-      if (stats) GS_RASTER_H2(true, true, true); else GS_RASTER_H2(true, true, false);
-    } else {
-      if (stats) GS_RASTER_H2(true, false, true); else GS_RASTER_H2(true, false, false);
-    }
+    if (periodic) launch_raster_pairs_t<true, true>(tile_offsets, order, ids, mean, color, rec, b, o, ctl, stats, st);
+    else launch_raster_pairs_t<true, false>(tile_offsets, order, ids, mean, color, rec, b, o, ctl, stats, st);
   } else {
-    if (periodic) {
-      if (stats) GS_RASTER_H2(false, true, true); else GS_RASTER_H2(false, true, false);
-    } else {
-      if (stats) GS_RASTER_H2(false, false, true); else GS_RASTER_H2(false, false, false);
-    }
+    if (periodic) launch_raster_pairs_t<false, true>(tile_offsets, order, ids, mean, color, rec, b, o, ctl, stats, st);
+    else launch_raster_pairs_t<false, false>(tile_offsets, order, ids, mean, color, rec, b, o, ctl, stats, st);
   }
-#undef GS_RASTER_H2
 }
 
 }  // namespace gs
