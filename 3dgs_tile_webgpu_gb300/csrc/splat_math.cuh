@@ -181,16 +181,17 @@ __device__ __forceinline__ Projected project(f3 view, const m3& cv, const float*
   if (!(finitef(cx) && finitef(cy) && finitef(depth) && finitef(k0) && finitef(k1) && finitef(k2) &&
         finitef(det) && finitef(s00) && finitef(s01) && finitef(s11) && finitef(orig_det)))
     return o;
-  float vdet = s00 * s11 - s01 * s01;
-  if (!(depth > 0.0f && vdet > 1e-8f && s00 > 0.0f && s11 > 0.0f && s00 <= 1e4f && s11 <= 1e4f &&
-        k0 > 0.0f && k2 > 0.0f && orig_det >= 0.0f))
+  // The validity test recomputes the determinant (vdet) from the same s00,
+  // s01, s11 with the same expression, so vdet == det bit for bit here (no
+  // multiply-add contraction): `vdet > 1e-8` repeats the test above, and its
+  // consistency checks always pass. |det - vdet| = 0; and with d = det in
+  // (1e-8, 1e8], invd = RN(1/d) is normal, so k = RN(s * invd) and
+  // e = RN(s / d) differ by a few units in the last place of s/d, far below
+  // max(1e-6, |e| 1e-3) (for s00, s11 in (0, 1e4] and |s01| <= sqrt(s00 s11)).
+  // Those checks are therefore left out; every outcome is unchanged.
+  if (!(depth > 0.0f && s00 > 0.0f && s11 > 0.0f && s00 <= 1e4f && s11 <= 1e4f && k0 > 0.0f && k2 > 0.0f &&
+        orig_det >= 0.0f))
     return o;
-  float e0 = s11 / vdet, e1 = -s01 / vdet, e2 = s00 / vdet;
-  bool ok = absf(det - vdet) <= maxf(1e-6f, vdet * 1e-3f);
-  ok = ok && absf(k0 - e0) <= maxf(1e-6f, absf(e0) * 1e-3f);
-  ok = ok && absf(k1 - e1) <= maxf(1e-6f, absf(e1) * 1e-3f);
-  ok = ok && absf(k2 - e2) <= maxf(1e-6f, absf(e2) * 1e-3f);
-  if (!ok) return o;
   o.ok = true;
   o.cx = cx; o.cy = cy; o.depth = depth;
   o.conic_x = k0; o.conic_y = k1; o.conic_z = k2;
