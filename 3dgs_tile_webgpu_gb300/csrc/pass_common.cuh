@@ -238,8 +238,11 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* s
 //   [0] cx, cy, -a/2 log2 e, -b log2 e
 //   [1] -c/2 log2 e, log2 opacity, half2(r, g) bits, half2(b, min(log2 opacity, log2 0.99)) bits
 // where (a, b, c) is the conic. Written by the projection when `rec` is not null.
+// rec: packed raster records of the fast forms (null for EXACT); erec: the
+// emission records, two float4 per item: (cx, cy, conic a, conic b),
+// (conic c, log(opacity * 255), rx + 512 ry, 0), written for visible items.
 void launch_project(const BatchView& b, const PassOptions& o, float4* mean, float4* conic, float4* color,
-                    uint32_t* counts, uint32_t* keys, float4* rec, cudaStream_t st);
+                    uint32_t* counts, uint32_t* keys, float4* rec, float4* erec, cudaStream_t st);
 void launch_epoch_begin(uint32_t* epoch_base, cudaStream_t st);
 void launch_compact(const uint32_t* keys, uint32_t n, uint32_t* vis_off, uint32_t* keys_out, uint32_t* vals_out,
                     Control* ctl, unsigned long long* status, Epoch epoch, uint32_t chunks, cudaStream_t st);
@@ -247,9 +250,9 @@ void launch_scan_counts(const uint32_t* sorted_ids, const uint32_t* tile_counts,
                         uint32_t* offsets, Control* ctl, unsigned long long* status, Epoch epoch,
                         uint32_t capacity, const uint32_t* frame_params, uint32_t* output_state, uint32_t chunks,
                         cudaStream_t st);
-void launch_emit(const uint32_t* sorted_ids, uint32_t n_max, const float4* mean, const float4* conic,
-                 const uint32_t* ordered, const uint32_t* offsets, const BatchView& b, const PassOptions& o,
-                 Control* ctl, uint32_t capacity, uint32_t* tile_keys, uint32_t* tile_vals, cudaStream_t st);
+void launch_emit(const uint32_t* sorted_ids, uint32_t n_max, const float4* erec, const uint32_t* ordered,
+                 const uint32_t* offsets, const BatchView& b, const PassOptions& o, Control* ctl, uint32_t capacity,
+                 uint32_t* tile_keys, uint32_t* tile_vals, cudaStream_t st);
 void launch_tile_ranges(const uint32_t* sorted_tile_keys, Control* ctl, uint32_t ntile, uint32_t n_max,
                         uint32_t* tile_offsets, cudaStream_t st);
 constexpr uint32_t kSortTile = 4096;  // items per sort tile

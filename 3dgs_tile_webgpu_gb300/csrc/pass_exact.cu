@@ -106,7 +106,7 @@ template <bool FP64, bool GROUPED>
 __global__ void __launch_bounds__(kBlock, 4) k_project(BatchView b, PassOptions o, float4* __restrict__ mean_out,
                                                     float4* __restrict__ conic_out, float4* __restrict__ color_out,
                                                     uint32_t* __restrict__ count_out, uint32_t* __restrict__ key_out,
-                                                    float4* __restrict__ rec_out) {
+                                                    float4* __restrict__ rec_out, float4* __restrict__ erec_out) {
   __shared__ float s_snorm[256];
   __shared__ uint32_t s_group;
   __shared__ CountShared s_count;
@@ -149,7 +149,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_project(BatchView b, PassOptions 
     float4 mo4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     uint32_t cnt = 0, key = kInvisibleKey, nbox = 0;
     Projected pr = {};
-    float op = 0.0f, rx = 0.0f, ry = 0.0f;
+    float op = 0.0f, rx = 0.0f, ry = 0.0f, thr = 0.0f;
     f3 vdir = {0.0f, 0.0f, 0.0f};
     // Project and cull; a splat that survives gets its tile box.
     do {
@@ -206,7 +206,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_project(BatchView b, PassOptions 
       op = clampf(so.w, 0.0f, 1.0f);
       if (o.antialias == 0u) op = op * sqrtf(clampf(pr.orig_det / pr.det, 0.0f, 1.0f));
       if (op < (float)(1.0 / 255.0) || op != op) break;
-      const float thr = gsdm::logf_(op * 255.0f);
+      thr = gsdm::logf_(op * 255.0f);
       const float ex = sqrtf((thr * 2.0f) * clampf(pr.cov_x, 1e-12f, 1e4f));
       const float ey = sqrtf((thr * 2.0f) * clampf(pr.cov_z, 1e-12f, 1e4f));
       rx = ceilf(ex);
@@ -246,6 +246,10 @@ __global__ void __launch_bounds__(kBlock, 4) k_project(BatchView b, PassOptions 
       const f3 col = eval_sh_any(v.degree, co, vdir, s_snorm);
       mo4 = make_float4(pr.cx, pr.cy, pr.depth, op);
       conic_out[item] = make_float4(pr.conic_x, pr.conic_y, pr.conic_z, rx + ry * 512.0f);
+      // Emission record: what the emission reads per depth rank, in one
+      // 32-byte gather (layout in pass_common.cuh).
+      erec_out[2 * (size_t)item] = make_float4(pr.cx, pr.cy, pr.conic_x, pr.conic_y);
+      erec_out[2 * (size_t)item + 1] = make_float4(pr.conic_z, thr, rx + ry * 512.0f, 0.0f);
       color_out[item] = make_float4(col.x, col.y, col.z, __uint_as_float(slot ^ kActiveTag));
       if (rec_out) {
         // Packed raster record of the fast forms (layout in pass_common.cuh).
@@ -271,19 +275,23 @@ __global__ void __launch_bounds__(kBlock, 4) k_project(BatchView b, PassOptions 
 }
 
 void launch_project(const BatchView& b, const PassOptions& o, float4* mean, float4* conic, float4* color,
-                    uint32_t* counts, uint32_t* keys, float4* rec, cudaStream_t st) {
+                    uint32_t* counts, uint32_t* keys, float4* rec, float4* erec, cudaStream_t st) {
   if (b.total_blocks == 0) return;  // projection blocks over the view groups
   const bool grouped = b.ngroups < b.nviews;
   if (o.proj_fp64) {
     if (grouped)
-      k_project<true, true><<<b.total_blocks, kBlock, 0, st>>>(b, o, mean, conic, color, counts, keys, rec);
+      k_project<true, true><<<b.total_blocks, kBlock, 0, st>>>(b, o, mean, conic, color, counts, keys, rec,
+                                                                      erec);
     else
-      k_project<true, false><<<b.total_blocks, kBlock, 0, st>>>(b, o, mean, conic, color, counts, keys, rec);
+      k_project<true, false><<<b.total_blocks, kBlock, 0, st>>>(b, o, mean, conic, color, counts, keys, rec,
+                                                                      erec);
   } else {
     if (grouped)
-      k_project<false, true><<<b.total_blocks, kBlock, 0, st>>>(b, o, mean, conic, color, counts, keys, rec);
+      k_project<false, true><<<b.total_blocks, kBlock, 0, st>>>(b, o, mean, conic, color, counts, keys, rec,
+                                                                      erec);
     else
-      k_project<false, false><<<b.total_blocks, kBlock, 0, st>>>(b, o, mean, conic, color, counts, keys, rec);
+      k_project<false, false><<<b.total_blocks, kBlock, 0, st>>>(b, o, mean, conic, color, counts, keys, rec,
+                                                                      erec);
   }
 }
 
@@ -566,7 +574,7 @@ struct EmitShared {
 // tile-test inputs for its warp, walk the union of the warp's boxes 32 box
 // tiles per round, place hits after the owner's earlier hits, pad with
 // sentinels. The lane's rank data were loaded by the caller.
-__device__ __forceinline__ void emit_group(EmitShared& sm, bool live, uint32_t g, float4 m, float4 c,
+__device__ __forceinline__ void emit_group(EmitShared& sm, bool live, uint32_t g, float4 e0, float4 e1,
                                            uint32_t reserved, uint32_t base_off, const BatchView& bv,
                                            const PassOptions& o, uint32_t capacity, uint32_t* __restrict__ tile_keys,
                                            uint32_t* __restrict__ tile_vals) {
@@ -576,9 +584,11 @@ __device__ __forceinline__ void emit_group(EmitShared& sm, bool live, uint32_t g
   uint32_t nbox = 0;
   if (live) {
     const ViewDesc& v = bv.views[find_view(bv.item_base, bv.nviews, g)];
-    const uint32_t packed = (uint32_t)c.w;
+    // Emission record: (cx, cy, conic a, b), (conic c, threshold, rx + 512 ry, 0).
+    const float4 m = make_float4(e0.x, e0.y, 0.0f, 0.0f), c = make_float4(e0.z, e0.w, e1.x, 0.0f);
+    const uint32_t packed = (uint32_t)e1.z;
     const float rx = (float)(packed % 512u), ry = (float)(packed / 512u);
-    const float thr = gsdm::logf_(m.w * 255.0f);
+    const float thr = e1.y;  // log(opacity * 255), computed by the projection
     const int tiles_x = (int)v.tiles_x, tiles_y = (int)v.tiles_y;
     const float mtx = (float)(tiles_x - 1), mty = (float)(tiles_y - 1);
     int tminx = (int)clampf(floorf((m.x - rx) / 16.0f), 0.0f, mtx);
@@ -665,8 +675,7 @@ __device__ __forceinline__ void emit_group(EmitShared& sm, bool live, uint32_t g
 constexpr uint32_t kEmitTwoGroupsFrom = 1u << 23;  // ranks per launch
 
 template <int G>
-__global__ void __launch_bounds__(kBlock) k_emit(const uint32_t* __restrict__ ids, const float4* __restrict__ mean,
-                                                 const float4* __restrict__ conic,
+__global__ void __launch_bounds__(kBlock) k_emit(const uint32_t* __restrict__ ids, const float4* __restrict__ erec,
                                                  const uint32_t* __restrict__ ordered,
                                                  const uint32_t* __restrict__ offsets, BatchView bv, PassOptions o,
                                                  Control* __restrict__ ctl, uint32_t capacity,
@@ -678,7 +687,7 @@ __global__ void __launch_bounds__(kBlock) k_emit(const uint32_t* __restrict__ id
   const uint32_t first = blockIdx.x * kBlock * G;
   if (first >= n) return;  // whole block past the visible count
   uint32_t g[G], res[G], off[G];
-  float4 m[G], c[G];
+  float4 e0[G], e1[G];
 #pragma unroll
   for (int h = 0; h < G; ++h) {
     const uint32_t r = first + (uint32_t)h * kBlock + tid;
@@ -692,30 +701,30 @@ __global__ void __launch_bounds__(kBlock) k_emit(const uint32_t* __restrict__ id
 #pragma unroll
   for (int h = 0; h < G; ++h) {
     const uint32_t r = first + (uint32_t)h * kBlock + tid;
-    m[h] = c[h] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    e0[h] = e1[h] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     if (r < n) {
-      m[h] = __ldg(mean + g[h]);
-      c[h] = __ldg(conic + g[h]);
+      e0[h] = __ldg(erec + 2 * (size_t)g[h]);
+      e1[h] = __ldg(erec + 2 * (size_t)g[h] + 1);
     }
   }
 #pragma unroll
   for (int h = 0; h < G; ++h) {
     const uint32_t r = first + (uint32_t)h * kBlock + tid;
-    emit_group(sm, r < n, g[h], m[h], c[h], res[h], off[h], bv, o, capacity, tile_keys, tile_vals);
+    emit_group(sm, r < n, g[h], e0[h], e1[h], res[h], off[h], bv, o, capacity, tile_keys, tile_vals);
   }
 }
 
-void launch_emit(const uint32_t* ids, uint32_t n_max, const float4* mean, const float4* conic,
-                 const uint32_t* ordered, const uint32_t* offsets, const BatchView& b, const PassOptions& o,
-                 Control* ctl, uint32_t capacity, uint32_t* tile_keys, uint32_t* tile_vals, cudaStream_t st) {
+void launch_emit(const uint32_t* ids, uint32_t n_max, const float4* erec, const uint32_t* ordered,
+                 const uint32_t* offsets, const BatchView& b, const PassOptions& o, Control* ctl, uint32_t capacity,
+                 uint32_t* tile_keys, uint32_t* tile_vals, cudaStream_t st) {
   if (n_max == 0) return;
   if (n_max >= kEmitTwoGroupsFrom) {
     const uint32_t grid = (n_max + 2 * kBlock - 1) / (2 * kBlock);
-    k_emit<2><<<grid, kBlock, 0, st>>>(ids, mean, conic, ordered, offsets, b, o, ctl, capacity, tile_keys,
+    k_emit<2><<<grid, kBlock, 0, st>>>(ids, erec, ordered, offsets, b, o, ctl, capacity, tile_keys,
                                        tile_vals);
   } else {
     const uint32_t grid = (n_max + kBlock - 1) / kBlock;
-    k_emit<1><<<grid, kBlock, 0, st>>>(ids, mean, conic, ordered, offsets, b, o, ctl, capacity, tile_keys,
+    k_emit<1><<<grid, kBlock, 0, st>>>(ids, erec, ordered, offsets, b, o, ctl, capacity, tile_keys,
                                        tile_vals);
   }
 }

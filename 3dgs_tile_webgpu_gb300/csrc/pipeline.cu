@@ -81,7 +81,8 @@ struct gs3d_pipeline {
   // Per-slot workspaces (sized by data.count).
   uint32_t slot_cap = 0;
   float4* mean = nullptr;
-  float4* rec = nullptr;  // packed raster records, two float4 per slot
+  float4* rec = nullptr;   // packed raster records, two float4 per slot
+  float4* erec = nullptr;  // emission records, two float4 per slot
   float4* conic = nullptr;
   float4* color = nullptr;
   uint32_t* counts = nullptr;
@@ -259,7 +260,7 @@ gs3d_status ensure_slots(gs3d_pipeline* p, uint32_t count) {
   const uint32_t cap = std::max(count, p->slot_cap * 2u);
   cudaError_t e = cudaSuccess;
   if ((e = dalloc(p->mean, cap)) || (e = dalloc(p->conic, cap)) || (e = dalloc(p->color, cap)) ||
-      (e = dalloc(p->rec, 2 * (size_t)cap)) ||
+      (e = dalloc(p->rec, 2 * (size_t)cap)) || (e = dalloc(p->erec, 2 * (size_t)cap)) ||
       (e = dalloc(p->counts, cap)) || (e = dalloc(p->keys, cap)) || (e = dalloc(p->vis_off, cap)) ||
       (e = dalloc(p->dk[0], cap)) || (e = dalloc(p->dk[1], cap)) || (e = dalloc(p->dv[0], cap)) ||
       (e = dalloc(p->dv[1], cap)) || (e = dalloc(p->ordered, cap)) || (e = dalloc(p->ioff, cap))) {
@@ -367,7 +368,7 @@ void release_all(gs3d_pipeline* p) {
     dfree(p->stage_dev[i]);
     if (p->stage_pinned[i]) cudaFreeHost(p->stage_pinned[i]);
   }
-  dfree(p->mean); dfree(p->rec); dfree(p->conic); dfree(p->color); dfree(p->counts); dfree(p->keys); dfree(p->vis_off);
+  dfree(p->mean); dfree(p->rec); dfree(p->erec); dfree(p->conic); dfree(p->color); dfree(p->counts); dfree(p->keys); dfree(p->vis_off);
   dfree(p->dk[0]); dfree(p->dk[1]); dfree(p->dv[0]); dfree(p->dv[1]); dfree(p->ordered); dfree(p->ioff);
   dfree(p->tk[0]); dfree(p->tk[1]); dfree(p->tv[0]); dfree(p->tv[1]);
   dfree(p->tile_offsets); dfree(p->tile_order); dfree(p->ctl); dfree(p->epoch_dev); dfree(p->output_state); dfree(p->status);
@@ -721,7 +722,7 @@ void record_batch(gs3d_pipeline* p, const Plan& pl, unsigned char* dev, cudaStre
   // K1: projection.
   mark(p, GS3D_STAGE_PROJECT, st);
   const bool exact = p->desc.raster_precision == GS3D_RASTER_EXACT;
-  launch_project(bv, o, p->mean, p->conic, p->color, p->counts, p->keys, exact ? nullptr : p->rec, st);
+  launch_project(bv, o, p->mean, p->conic, p->color, p->counts, p->keys, exact ? nullptr : p->rec, p->erec, st);
   launches += pl.blocks ? 1 : 0;
   // Visibility compaction.
   mark(p, GS3D_STAGE_COMPACT, st);
@@ -755,7 +756,7 @@ void record_batch(gs3d_pipeline* p, const Plan& pl, unsigned char* dev, cudaStre
   const uint32_t max_digit = p->tuning.tile_digit_bits;
   const int tile_passes = (int)std::min<uint32_t>(kMaxSortPasses, (tile_bits + max_digit - 1) / max_digit);
   const int digit_bits = (int)((tile_bits + tile_passes - 1) / tile_passes);
-  launch_emit(p->dv[cur], N, p->mean, p->conic, p->ordered, p->ioff, bv, o, ctl, cap32, p->tk[0], p->tv[0], st);
+  launch_emit(p->dv[cur], N, p->erec, p->ordered, p->ioff, bv, o, ctl, cap32, p->tk[0], p->tv[0], st);
   launches += N ? 1 : 0;
   // Tile sort.
   mark(p, GS3D_STAGE_TILE_SORT, st);

@@ -40,7 +40,8 @@ def parse():
     ap.add_argument("--cameras", type=int, default=16)
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--height", type=int, default=1080)
-    ap.add_argument("--precision", default="fp32", choices=["fp32", "exact", "half2"])
+    ap.add_argument("--precision", default="half2", choices=["fp32", "exact", "half2"],
+                    help="raster form of the batched (headline) measurement: the metric's batched fp16 is half2")
     ap.add_argument("--plain-precision", default="fp32", choices=["fp32", "exact"])
     ap.add_argument("--latency-frames", type=int, default=240)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -372,7 +373,7 @@ def main() -> None:
 
     plain = make_pipe(args.plain_precision)
     colors = [torch.empty((H, W, 4), dtype=torch.float16, device="cuda") for _ in range(ncam)]
-    host = torch.empty((H, W, 4), dtype=torch.float16, pin_memory=True)
+    host = [torch.empty((H, W, 4), dtype=torch.float16, pin_memory=True) for _ in range(ncam)]
     data = ds.data()
 
     # Size the intersection workspace from the demand of every camera
@@ -494,15 +495,45 @@ def main() -> None:
 
     # End to end through the public API (batched form): camera/object tables
     # from host memory in, every rendered rgba16f image back to pinned host
-    # memory, every step.
+    # memory, every step. Two pipelines with their own targets alternate, so
+    # the read-back of step k (on a copy stream) overlaps the render of step
+    # k + 1; a pipeline renders again only after its previous images are back.
+    colors2 = [torch.empty_like(c) for c in colors]
+    batched2 = P.TiledGaussianPipeline(ds.data(), {"raster_precision": args.precision,
+                                                   "intersection_capacity": int(demand * 1.25 * ncam) + 256})
+    batched2.set_tuning(tuning)
+    views2 = [(data, cam, W, H, colors2[i].data_ptr(), 0, "rgba16f") for i, cam in enumerate(cams)]
+    gstream2 = torch.cuda.Stream()
+    batched2.render_batch(views2)
+    torch.cuda.synchronize()
+    batched2.capture_graph(views2, gstream2.cuda_stream)
+    lanes = [(batched, gstream, colors), (batched2, gstream2, colors2)]
+    copy_stream = torch.cuda.Stream()
+    copied = [None, None]  # event: lane's images are back in host memory
+
+    def e2e_step(k):
+        pipe, gs, targets = lanes[k & 1]
+        with torch.cuda.stream(gs):
+            if copied[k & 1] is not None:
+                gs.wait_event(copied[k & 1])
+            pipe.launch_graph(cams, stream=gs.cuda_stream)
+            done = torch.cuda.Event()
+            done.record(gs)
+        with torch.cuda.stream(copy_stream):
+            copy_stream.wait_event(done)
+            for hb, c in zip(host, targets):
+                hb.copy_(c, non_blocking=True)
+            ev = torch.cuda.Event()
+            ev.record(copy_stream)
+            copied[k & 1] = ev
+
+    for k in range(2):
+        e2e_step(k)
     torch.cuda.synchronize()
     barrier()
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        with torch.cuda.stream(gstream):
-            batched.launch_graph(cams, stream=gstream.cuda_stream)
-            for c in colors:
-                host.copy_(c, non_blocking=True)
+    for k in range(args.steps):
+        e2e_step(k)
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     e2e_s = max_over_ranks(e2e_s, world)
@@ -553,6 +584,7 @@ def main() -> None:
 
     plain.dispose()
     batched.dispose()
+    batched2.dispose()
     if rank != 0:
         return
     out = {
