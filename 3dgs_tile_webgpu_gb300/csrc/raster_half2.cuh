@@ -143,6 +143,26 @@ __device__ __forceinline__ void blend_range_h2(uint32_t begin, uint32_t source_c
       }
       const bool use0 = p0 >= th0;
       const bool use1 = p1 >= th1;
+      if (!STATS) {
+        // Branch-free: a pixel below the threshold (or done) blends alpha
+        // 2^-inf = +0, which leaves its colour, depth and transmittance
+        // exactly unchanged (t * 0 = 0, x + c * 0 = x for finite c).
+        const float q0 = use0 ? p0 : -__int_as_float(0x7f800000);
+        const float q1 = use1 ? p1 : -__int_as_float(0x7f800000);
+        float2 al;
+        if (HALF) {
+          const uint32_t lim_bits = __float_as_uint(c.z);
+          al = __half22float2(
+              h2ex2_approx(__hmin2(__floats2half2_rn(q0, q1), *reinterpret_cast<const __half2*>(&lim_bits))));
+        } else {
+          al.x = ex2_approx(fminf(q0, c.z));
+          al.y = ex2_approx(fminf(q1, c.z));
+        }
+        const float4 col = ws.col[j];
+        blend_pixel<DEPTH>(al.x, col, c.w, a0);
+        blend_pixel<DEPTH>(al.y, col, c.w, a1);
+        continue;
+      }
       if (!(use0 || use1)) continue;
       float2 al;
       if (HALF) {

@@ -510,15 +510,21 @@ def main() -> None:
     lanes = [(batched, gstream, colors), (batched2, gstream2, colors2)]
     copy_stream = torch.cuda.Stream()
     copied = [None, None]  # event: lane's images are back in host memory
+    rendered = [None]      # event: the previous step's render finished
 
     def e2e_step(k):
+        # Renders run one after another (each pass expects the whole GPU);
+        # only the read-back overlaps the next render.
         pipe, gs, targets = lanes[k & 1]
         with torch.cuda.stream(gs):
             if copied[k & 1] is not None:
                 gs.wait_event(copied[k & 1])
+            if rendered[0] is not None:
+                gs.wait_event(rendered[0])
             pipe.launch_graph(cams, stream=gs.cuda_stream)
             done = torch.cuda.Event()
             done.record(gs)
+            rendered[0] = done
         with torch.cuda.stream(copy_stream):
             copy_stream.wait_event(done)
             for hb, c in zip(host, targets):
