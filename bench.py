@@ -134,10 +134,26 @@ class Clocks:
 
 
 def stage_bytes(stage: str, n: int, v: int, inter: int, tiles: int, pixels: int, coeffs: int, depth_passes: int,
-                tile_passes: int, color_bytes: int, depth_out: bool) -> int:
-    """Algorithmic DRAM bytes of one launch of each stage (the data it must move)."""
+                tile_passes: int, color_bytes: int, depth_out: bool, groups: int = 1, precision: str = "half2",
+                views: int = 1) -> int:
+    """Algorithmic DRAM bytes of each stage over one batch (the data it must move).
+
+    n, v, inter, tiles, pixels: totals over the batch's `views` views (all of
+    one scene); groups: view groups (the views of one launch share one read of
+    the packed scene); precision: raster form (half2 reads the 32-byte packed record per
+    intersection, fp32 that record plus the FP32 colour, exact the reference's
+    mean, conic and colour)."""
+    fast = precision != "exact"
     if stage == "project":
-        return n * (4 + 16 + 8 + 4) + v * 4 * coeffs + n * (16 + 4 + 4) + v * 32
+        # Read once per group: the tail, mean + id, shape and rotation of every
+        # splat, the SH of every splat visible in some view of the group.
+        n_scene, per_group = n // max(1, views), max(1, views // max(1, groups))
+        sh = min(n_scene, (v // max(1, views)) * per_group) * 4 * coeffs
+        scene = groups * (n_scene * (4 + 16 + 8 + 4) + sh)
+        # Written per view: mean, count, key of every item; conic, colour and
+        # the emission (and, fast forms, raster) record of every visible one.
+        written = n * (16 + 4 + 4) + v * (16 + 16 + 32 + (32 if fast else 0))
+        return scene + written
     if stage == "compact":
         return n * 4 + n * 4 + v * 8
     if stage == "depth_sort":
@@ -145,13 +161,14 @@ def stage_bytes(stage: str, n: int, v: int, inter: int, tiles: int, pixels: int,
     if stage == "scan":
         return v * (4 + 4) + v * 8
     if stage == "emit":
-        return v * (4 + 16 + 16 + 4 + 4) + inter * 8
+        return v * (4 + 32 + 4 + 4) + inter * 8
     if stage == "tile_sort":
         return tile_passes * inter * 16
     if stage == "ranges":
         return inter * 4 + (tiles + 1) * 4
     if stage == "raster":
-        return (tiles + 1) * 4 + inter * (4 + 48) + pixels * (color_bytes + (4 if depth_out else 0))
+        per_record = 32 if precision == "half2" else 48
+        return (tiles + 1) * 4 + inter * (4 + per_record) + pixels * (color_bytes + (4 if depth_out else 0))
     return 0
 
 
@@ -556,12 +573,16 @@ def main() -> None:
     tile_bits = max(1, int(np.ceil(np.log2(tiles + 1))))
     tile_passes = (tile_bits + 7) // 8
     stages = {}
-    # per batch: every stage processes all views of the step
+    # per batch: every stage processes all views of the step, in launches of
+    # views_per_launch views (one view group each: the views share the scene)
     bn, bv_, bi, bt = n * ncam, v * ncam, inter * ncam, tiles * ncam
-    btile_bits = max(1, int(np.ceil(np.log2(bt + 1))))
-    btile_passes = (btile_bits + 7) // 8
+    vpl = int(tuning["views_per_launch"]) or ncam
+    nlaunch = (ncam + vpl - 1) // vpl
+    ltile_bits = max(1, int(np.ceil(np.log2(tiles * min(vpl, ncam) + 1))))
+    btile_passes = min(4, (ltile_bits + int(tuning["tile_digit_bits"]) - 1) // int(tuning["tile_digit_bits"]))
     for name, ms in stage_ms.items():
-        b = stage_bytes(name, bn, bv_, bi, bt, W * H * ncam, 16, 4, btile_passes, 8, False)
+        b = stage_bytes(name, bn, bv_, bi, bt, W * H * ncam, 16, 4, btile_passes, 8, False, groups=nlaunch,
+                        precision=args.precision, views=ncam)
         gbs = b / (ms * 1e-3) / 1e9 if ms > 0 else 0.0
         stages[name] = {"ms": ms, "bytes": b, "GB/s": gbs, "frac": gbs / hbm}
     dom = max(stages, key=lambda k: stages[k]["ms"])
