@@ -48,6 +48,11 @@ __device__ __forceinline__ f3 eval_sh_any(uint32_t degree, const uint32_t* co, f
   }
 }
 
+// Bits [s, e) of a word, 0 <= s < e <= 32.
+__device__ __forceinline__ uint32_t bit_range(uint32_t s, uint32_t e) {
+  return (e >= 32u ? 0xffffffffu : ((1u << e) - 1u)) & ~((1u << s) - 1u);
+}
+
 // Per-warp tables of the projection's cooperative tile count: the splat
 // parameters of the tile test, the box, and the inclusive box-tile counts.
 struct CountShared {
@@ -565,8 +570,9 @@ constexpr int kEmitWarps = kBlock / 32;
 
 struct EmitShared {
   float f[10][kEmitWarps][32];     // cx, cy, conic a, b, c, threshold, rx, ry, view width, height
-  uint32_t u[8][kEmitWarps][32];   // tminx, tminy, box width, tiles_x, tile_base, base, reserved, item
-  uint32_t incl[kEmitWarps][32];   // inclusive box-tile counts
+  uint32_t u[9][kEmitWarps][32];   // tminx, tminy, box width, tiles_x, tile_base, base, reserved, item,
+                                   // first box tile of the warp's walk
+  uint32_t own[kEmitWarps][32];    // lane owning the k-th segment of the round
   uint32_t filled[kEmitWarps][32]; // records placed so far per rank
 };
 
@@ -614,24 +620,35 @@ __device__ __forceinline__ void emit_group(EmitShared& sm, bool live, uint32_t g
     const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
     if (lane >= (uint32_t)d) incl += y;
   }
-  sm.incl[warp][lane] = incl;
+  const uint32_t excl = incl - nbox;
+  const uint32_t le = lt | (1u << lane);
+  sm.u[8][warp][lane] = excl;
   sm.filled[warp][lane] = 0u;
-  __syncwarp();
+  uint32_t filled = 0;
   const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
 
+  // Rounds of 32 box tiles. The boxes lie end to end in lane order, so a
+  // round is a run of segments, one per owning lane: a lane finds its segment
+  // from the OR of the segment starts and the segment's owner from a table
+  // the owners wrote; each owner adds its hits under its own segment mask.
   for (uint32_t j0 = 0; j0 < total; j0 += 32) {
+    const uint32_t lo = max(excl, j0), hi = min(incl, j0 + 32u);
+    const bool seg = lo < hi;
+    const uint32_t starts = __reduce_or_sync(0xffffffffu, seg ? 1u << (lo - j0) : 0u);
+    const uint32_t owners = __ballot_sync(0xffffffffu, seg);
+    if (seg) sm.own[warp][__popc(owners & lt)] = lane;
+    __syncwarp();
     const uint32_t j = j0 + lane;
     const bool valid = j < total;
-    uint32_t owner = 0;
-#pragma unroll
-    for (uint32_t step = 16; step >= 1; step >>= 1)
-      if (sm.incl[warp][owner + step - 1] <= j) owner += step;
+    uint32_t owner = 0, seg_start = 0;
     bool hit = false;
     uint32_t t = 0;
     if (valid) {
+      const uint32_t mine = starts & le;
+      owner = sm.own[warp][__popc(mine) - 1u];
+      seg_start = 31u - (uint32_t)__clz(mine);
       const uint32_t bw = sm.u[2][warp][owner];
-      const uint32_t first = owner ? sm.incl[warp][owner - 1] : 0u;
-      const uint32_t kk = j - first;
+      const uint32_t kk = j - sm.u[8][warp][owner];
       const uint32_t by = kk / bw, bx = kk - by * bw;
       const int tx = (int)(sm.u[0][warp][owner] + bx), ty = (int)(sm.u[1][warp][owner] + by);
       hit = boundary_tile_hit(sm.f[0][warp][owner], sm.f[1][warp][owner], sm.f[2][warp][owner],
@@ -641,24 +658,27 @@ __device__ __forceinline__ void emit_group(EmitShared& sm, bool live, uint32_t g
       t = sm.u[4][warp][owner] + (uint32_t)ty * sm.u[3][warp][owner] + (uint32_t)tx;
     }
     const uint32_t hits = __ballot_sync(0xffffffffu, hit);
-    const uint32_t same = __match_any_sync(0xffffffffu, valid ? owner : 32u + lane);
     if (hit) {
-      const uint32_t local = sm.filled[warp][owner] + __popc(hits & same & lt);
+      // After the owner's earlier hits: those of past rounds, then those of
+      // this round below this lane within the owner's segment.
+      const uint32_t local = sm.filled[warp][owner] + __popc(hits & lt & ~((1u << seg_start) - 1u));
       const uint32_t base = sm.u[5][warp][owner];
       if (local < sm.u[6][warp][owner] && base + local < capacity) {
         tile_keys[base + local] = t;
         tile_vals[base + local] = sm.u[7][warp][owner];
       }
     }
-    __syncwarp();
-    // The highest lane of each owner's group advances the owner's count.
-    if (valid && lane == 31u - (uint32_t)__clz(same)) sm.filled[warp][owner] += __popc(hits & same);
-    __syncwarp();
+    __syncwarp();  // every read of filled and the owner table is done
+    if (seg) {
+      filled += __popc(hits & bit_range(lo - j0, hi - j0));
+      sm.filled[warp][lane] = filled;
+    }
   }
+  __syncwarp();
 
   // Sentinel padding for reserved slots without a hit.
   if (live) {
-    for (uint32_t pad = sm.filled[warp][lane]; pad < reserved; ++pad)
+    for (uint32_t pad = filled; pad < reserved; ++pad)
       if (base_off + pad < capacity) {
         tile_keys[base_off + pad] = sentinel;
         tile_vals[base_off + pad] = g;
