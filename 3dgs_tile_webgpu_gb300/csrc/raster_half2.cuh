@@ -84,16 +84,28 @@ __device__ __forceinline__ void blend_range_h2(uint32_t begin, uint32_t source_c
   uint32_t stop0 = s1, stop1 = s1;
   const float pyc1 = pyc0 + 4.0f;
   const uint32_t lt = (1u << lane) - 1u;
+  auto load_id = [&](uint32_t i) -> uint32_t {
+    if (i >= s1) return 0u;
+    uint32_t src = i;
+    if (capped) src = (uint32_t)floorf((((float)i + 0.5f) * (float)source_count) / (float)raster_count);
+    return __ldg(ids + begin + src);
+  };
+  // The FP32 form loads the next group's record ids one group ahead (the
+  // half2 form, at its register limit for 9 blocks per SM, is faster without).
+  uint32_t next_id = HALF ? 0u : load_id(s0 + lane);
   for (uint32_t b = s0; b < s1; b += 32) {
     if (__all_sync(0xffffffffu, done0 && done1)) break;
     const uint32_t i = b + lane;
     bool reach = false;
     float4 r0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), r1 = r0, col32 = r0;
     float depth = 0.0f;
+    uint32_t cur_id = 0;
+    if (!HALF) {
+      cur_id = next_id;
+      next_id = load_id(b + 32u + lane);
+    }
     if (i < s1) {
-      uint32_t src = i;
-      if (capped) src = (uint32_t)floorf((((float)i + 0.5f) * (float)source_count) / (float)raster_count);
-      const uint32_t g = __ldg(ids + begin + src);
+      const uint32_t g = HALF ? load_id(i) : cur_id;
       r0 = __ldg(rec + 2 * (size_t)g);  // one 32-byte record
       r1 = __ldg(rec + 2 * (size_t)g + 1);
       if (!HALF) col32 = __ldg(color + g);
