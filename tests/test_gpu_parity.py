@@ -365,3 +365,20 @@ def test_graph_replay_matches_direct_batches():
         assert list(dev.to_numpy(rg.output_state, (4,))) == list(dev.to_numpy(rd.output_state, (4,)))
     graph.dispose()
     direct.dispose()
+
+
+def test_benchmark_frame_bit_exact():
+    # The benchmark's 3M clustered scene at 1920x1080 (camera 0): ~2.2M visible
+    # splats and ~5.3M intersections, so every sort pass walks chunks of
+    # several 4096-item tiles and the chunked scans run their full grid. Every
+    # buffer the reference exposes is identical to the oracle's; the image is
+    # the EXACT raster's.
+    scene = sc.config2_scene()
+    frame = sc.config2_frames(1)[0]
+    o = oracle.render(scene, frame, 0, output_depth=False)
+    assert int(o["visible_state"][0]) > 2_000_000 and int(o["state"][1]) > 4_000_000
+    run = GpuRun(scene, frame, "exact", capacity=int(o["state"][1]) + 4096)
+    g = run.render(frame)
+    run.close()
+    assert_bit_exact(g, o, image=False)
+    assert np.array_equal(g["rgba"].view(np.uint32), o["rgba"].view(np.uint32))

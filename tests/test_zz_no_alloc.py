@@ -58,3 +58,44 @@ def test_static_compaction_rejects_oversize_and_null():
     too_many = pkg().abi.STATIC_COMPACT_MAX_ITEMS + 1
     assert lib.gs3d_compact_visible_static(None, too_many, None, None, None, None, None) == 2
     assert lib.gs3d_compact_visible_static(None, 16, None, None, None, None, None) == 1
+
+
+@pytest.mark.parametrize("pattern", ["random", "all", "none", "every7"])
+def test_static_compaction_sizes(pattern):
+    # The chunked compaction at sizes around its row (32), unit (256) and
+    # chunk boundaries (a persistent grid of 4 blocks per SM: 608 chunks on a
+    # GB300), from empty to multi-million inputs, against numpy.
+    import torch
+    lib = pkg().load()
+    rng = np.random.Generator(np.random.PCG64(77))
+    sizes = [0, 1, 2, 31, 32, 33, 255, 256, 257, 2047, 2048, 2049, 65535, 65537, 155647, 155648, 155649,
+             1_000_003, 4_999_999]
+    result = torch.full((2,), -1, dtype=torch.int32, device="cuda")
+    for n in sizes:
+        if pattern == "random":
+            vis = rng.random(n) < 0.5
+        elif pattern == "all":
+            vis = np.ones(n, bool)
+        elif pattern == "none":
+            vis = np.zeros(n, bool)
+        else:
+            vis = (np.arange(n) % 7) == 3
+        keys_host = np.where(vis, rng.integers(0, 0xFFFFFFFE, n, dtype=np.uint32), np.uint32(0xFFFFFFFF))
+        keys = torch.from_numpy(keys_host.astype(np.uint32).view(np.int32)).cuda() if n else None
+        m = max(n, 1)
+        offs = torch.full((m,), -1, dtype=torch.int32, device="cuda")
+        kout = torch.full((m,), -1, dtype=torch.int32, device="cuda")
+        iout = torch.full((m,), -1, dtype=torch.int32, device="cuda")
+        st = lib.gs3d_compact_visible_static(keys.data_ptr() if n else None, n, offs.data_ptr(), kout.data_ptr(),
+                                             iout.data_ptr(), result.data_ptr(), None)
+        assert st == 0, n
+        torch.cuda.synchronize()
+        count, err = (int(v) for v in result.cpu().numpy().view(np.uint32))
+        assert err == 0 and count == int(vis.sum()), n
+        if n == 0:
+            continue
+        expect_off = (np.cumsum(vis) - vis).astype(np.uint32)
+        assert np.array_equal(offs.cpu().numpy().view(np.uint32)[:n], expect_off), n
+        idx = np.nonzero(vis)[0].astype(np.uint32)
+        assert np.array_equal(iout.cpu().numpy().view(np.uint32)[:count], idx), n
+        assert np.array_equal(kout.cpu().numpy().view(np.uint32)[:count], keys_host[idx]), n
