@@ -53,10 +53,6 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
   const uint32_t s = (uint32_t)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
 }
-__device__ __forceinline__ void cp_async_commit_wait() {
-  asm volatile("cp.async.commit_group;" ::: "memory");
-  asm volatile("cp.async.wait_all;" ::: "memory");
-}
 
 // Tiles [t0, t1) of chunk c when n items split over `chunks` chunks.
 __device__ __forceinline__ void chunk_tiles(uint32_t n, uint32_t chunks, uint32_t c, uint32_t* t0, uint32_t* t1) {
@@ -82,7 +78,6 @@ __global__ void __launch_bounds__(kBlock) k_chunk_count(const uint32_t* __restri
   chunk_tiles(n, chunks, blockIdx.x, &t0, &t1);
   const uint32_t begin = (uint32_t)min((uint64_t)t0 * kSortTile, (uint64_t)n);
   const uint32_t end = (uint32_t)min((uint64_t)t1 * kSortTile, (uint64_t)n);
-  const uint32_t lt = (1u << lane) - 1u;
   // Each warp takes 512-key runs: four 16-byte loads per lane in flight
   // before any counting (begin is a multiple of 4096, so they are aligned).
   constexpr uint32_t kRun = 512u;
@@ -170,10 +165,9 @@ __device__ __forceinline__ void cp_async_wait_group() {
   asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
-// Tile buffers of the scatter (keys and values each): with two, tile t+1
-// streams in while tile t is ranked and scattered.
-constexpr int kScatterBuffers = 2;
-constexpr size_t kChunkDynSmem = 2 * kScatterBuffers * kSortTile * sizeof(uint32_t);
+// Two tile buffers (keys and values each): tile t+1 streams in while tile t
+// is ranked and scattered.
+constexpr size_t kChunkDynSmem = 2 * 2 * kSortTile * sizeof(uint32_t);
 
 template <int BITS>
 struct ScatterShared {
@@ -280,23 +274,18 @@ __global__ void __launch_bounds__(kBlock, kChunkBlocksPerSm)
   uint32_t t0, t1;
   chunk_tiles(n, chunks, blockIdx.x, &t0, &t1);
   if (t0 >= t1) return;
-  if (kScatterBuffers == 2) load_tile_async(keys_in, vals_in, t0 * kSortTile, n, s_buf, s_buf + kSortTile);
+  load_tile_async(keys_in, vals_in, t0 * kSortTile, n, s_buf, s_buf + kSortTile);
   if (tid < RADIX) sm.run[tid] = offsets[(size_t)blockIdx.x * RADIX + tid];
   for (uint32_t i = tid; i < kSortWarps * RADIX; i += kBlock) (&sm.warp_hist[0][0])[i] = 0u;
 
   for (uint32_t t = t0; t < t1; ++t) {
-    uint32_t* kb = s_buf + (kScatterBuffers == 2 ? ((t - t0) & 1u) : 0u) * 2u * kSortTile;
+    uint32_t* kb = s_buf + ((t - t0) & 1u) * 2u * kSortTile;
     uint32_t* vb = kb + kSortTile;
-    if (kScatterBuffers == 2) {
-      if (t + 1u < t1) {
-        uint32_t* nb = s_buf + (((t - t0) & 1u) ^ 1u) * 2u * kSortTile;
-        load_tile_async(keys_in, vals_in, (t + 1u) * kSortTile, n, nb, nb + kSortTile);
-        cp_async_wait_group<1>();
-      } else {
-        cp_async_wait_group<0>();
-      }
+    if (t + 1u < t1) {
+      uint32_t* nb = s_buf + (((t - t0) & 1u) ^ 1u) * 2u * kSortTile;
+      load_tile_async(keys_in, vals_in, (t + 1u) * kSortTile, n, nb, nb + kSortTile);
+      cp_async_wait_group<1>();
     } else {
-      load_tile_async(keys_in, vals_in, t * kSortTile, n, kb, vb);
       cp_async_wait_group<0>();
     }
     __syncthreads();
