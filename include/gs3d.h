@@ -259,12 +259,17 @@ gs3d_status gs3d_pipeline_autotune(gs3d_pipeline* pipeline, const gs3d_view* vie
  * global tile ids [tile_base[v], tile_base[v+1]); each view's tiles hold
  * exactly the records, order and image a single-view render of that view
  * produces. The batch shares one intersection workspace: on overflow no view
- * is published and the output state reports the batch's demand. */
+ * is published and the output state reports the batch's demand. Consecutive
+ * views whose gs3d_gaussian_data names the same buffers (means, shape,
+ * rotations, SH) with the same counts and SH degree form a view group: the
+ * projection decodes each splat once for the whole group, so order views by
+ * scene. */
 gs3d_status gs3d_pipeline_render_batch(gs3d_pipeline* pipeline, const gs3d_view* views, uint32_t count,
                                        uint32_t attempt, int reset_valid, void* stream);
 /* Capture the batched pass for these views (scenes, sizes, targets and object
  * counts fixed) into CUDA graphs; gs3d_pipeline_launch_graph then replays it
- * with new cameras: one graph launch per frame instead of ~20 launches.
+ * with new cameras: one graph launch per frame instead of ~28 kernel launches
+ * per launch sequence.
  * `stream` must be a non-default stream; profiling must be off. Any
  * update_data/resize_intersections drops the graphs. Two graph instances
  * alternate over two staging buffers, so the host prepares frame N+1 while
