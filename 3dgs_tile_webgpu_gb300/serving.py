@@ -164,6 +164,10 @@ class RenderServer:
                     nxt.dispatched = now
                     batch.append(nxt)
                     total += b
+                # Requests of one scene side by side: consecutive views of a
+                # scene share the projection's decode (a view group); every
+                # request's image is unchanged by its place in the batch.
+                batch.sort(key=lambda r: r.scene)
                 self._render_batch(lane, batch)
             busy += lane.event is not None
         return busy
