@@ -471,14 +471,13 @@ def main() -> None:
         return launches
 
     def timed(step, pipe_for_stages, stream_for_timing=None):
-        """Device time of exactly `steps` steps, per-stage events on."""
+        """Device time of exactly `steps` steps (no instrumentation), then the
+        per-stage breakdown from a second, profiled run of as many steps."""
         stream_for_timing = stream_for_timing or torch.cuda.current_stream()
         for _ in range(max(args.warmup, 3)):
             step()
         torch.cuda.synchronize()
         clocks = Clocks(local)
-        pipe_for_stages.set_profiling(True)
-        pipe_for_stages.stage_times()
         barrier()
         torch.cuda.synchronize()
         clocks.start()
@@ -492,6 +491,11 @@ def main() -> None:
         ck = clocks.stop()
         barrier()
         ms = e0.elapsed_time(e1)
+        pipe_for_stages.set_profiling(True)
+        pipe_for_stages.stage_times()
+        for _ in range(args.steps):
+            step()
+        torch.cuda.synchronize()
         sm, prof = pipe_for_stages.stage_times()
         pipe_for_stages.set_profiling(False)
         ms = max_over_ranks(ms, world)
