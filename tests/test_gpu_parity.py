@@ -326,9 +326,11 @@ def test_raster_stats_match_reference_counters(name):
     assert_bit_exact(g, o)
 
 
-def test_graph_replay_matches_direct_batches():
+@pytest.mark.parametrize("order", ["ABA", "AAB"])
+def test_graph_replay_matches_direct_batches(order):
     # Captured pass replayed with new cameras (two alternating graph
-    # instances) equals render_batch bit for bit, frame after frame.
+    # instances) equals render_batch bit for bit, frame after frame; "AAB"
+    # puts two views of one scene side by side (a view group).
     import importlib
     import torch
     P = importlib.import_module("3dgs_tile_webgpu_gb300")
@@ -342,7 +344,7 @@ def test_graph_replay_matches_direct_batches():
 
     colors = [torch.zeros((h, w, 4), dtype=torch.float16, device="cuda") for (w, h) in sizes]
     ref_colors = [torch.zeros_like(c) for c in colors]
-    data = [ds[0].data(), ds[1].data(), ds[0].data()]
+    data = [ds[0 if k == "A" else 1].data() for k in order]
     graph = P.TiledGaussianPipeline(data[0], {"raster_precision": "half2", "intersection_capacity": 1 << 20})
     direct = P.TiledGaussianPipeline(data[0], {"raster_precision": "half2", "intersection_capacity": 1 << 20})
     stream = torch.cuda.Stream()
