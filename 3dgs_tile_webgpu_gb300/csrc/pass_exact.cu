@@ -153,6 +153,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_project(BatchView b, PassOptions 
     const float vw = v.vw, vh = v.vh;
     float4 mo4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     uint32_t cnt = 0, key = kInvisibleKey, nbox = 0;
+    bool single = false;
     Projected pr = {};
     float op = 0.0f, rx = 0.0f, ry = 0.0f, thr = 0.0f;
     f3 vdir = {0.0f, 0.0f, 0.0f};
@@ -228,14 +229,22 @@ __global__ void __launch_bounds__(kBlock, 4) k_project(BatchView b, PassOptions 
       }
       const int tiles_x = (int)v.tiles_x, tiles_y = (int)v.tiles_y;
       const float mtx = (float)(tiles_x - 1), mty = (float)(tiles_y - 1);
-      int tminx = (int)clampf(floorf(bminx / 16.0f), 0.0f, mtx);
-      int tminy = (int)clampf(floorf(bminy / 16.0f), 0.0f, mty);
-      int tmaxx = (int)clampf(floorf(bmaxx / 16.0f), 0.0f, mtx);
-      int tmaxy = (int)clampf(floorf(bmaxy / 16.0f), 0.0f, mty);
+      const float fx0 = floorf(bminx / 16.0f), fy0 = floorf(bminy / 16.0f);
+      const float fx1 = floorf(bmaxx / 16.0f), fy1 = floorf(bmaxy / 16.0f);
+      int tminx = (int)clampf(fx0, 0.0f, mtx);
+      int tminy = (int)clampf(fy0, 0.0f, mty);
+      int tmaxx = (int)clampf(fx1, 0.0f, mtx);
+      int tmaxy = (int)clampf(fy1, 0.0f, mty);
       if (o.axis == 1u) { tminx = 0; tmaxx = tiles_x - 1; }
       if (o.axis == 2u) { tminy = 0; tmaxy = tiles_y - 1; }
       const uint32_t bw = (uint32_t)(tmaxx - tminx + 1);
       nbox = bw * (uint32_t)(tmaxy - tminy + 1);
+      // A box of one on-screen tile that no clamp touched holds the centre
+      // strictly inside that tile (rx, ry >= 1 and the floors of c - r and
+      // c + r agree), so the reference's tile test takes its centre-inside
+      // path and passes: the count is 1 without the walk.
+      single = o.axis == 0u && fx0 == fx1 && fy0 == fy1 && fx0 >= 0.0f && fx0 <= mtx && fy0 >= 0.0f &&
+               fy0 <= mty;
       s_count.f[0][warp][lane] = pr.cx; s_count.f[1][warp][lane] = pr.cy;
       s_count.f[2][warp][lane] = pr.conic_x; s_count.f[3][warp][lane] = pr.conic_y;
       s_count.f[4][warp][lane] = pr.conic_z; s_count.f[5][warp][lane] = thr;
@@ -244,7 +253,8 @@ __global__ void __launch_bounds__(kBlock, 4) k_project(BatchView b, PassOptions 
       s_count.u[2][warp][lane] = bw;
     } while (false);
     // Tiles passing the tile test (projectionHelpers.ts:223-236), counted by the whole warp.
-    cnt = count_tiles_warp(s_count, nbox, vw, vh, o.axis);
+    cnt = count_tiles_warp(s_count, single ? 0u : nbox, vw, vh, o.axis);
+    if (single) cnt = 1u;
     if (cnt > 0) {
       uint32_t co[16];
       load_sh(v.sh + (size_t)slot * v.C, v.degree, co);
@@ -614,67 +624,77 @@ __device__ __forceinline__ void emit_group(EmitShared& sm, bool live, uint32_t g
     sm.u[3][warp][lane] = (uint32_t)tiles_x; sm.u[4][warp][lane] = v.tile_base;
     sm.u[5][warp][lane] = base_off; sm.u[6][warp][lane] = reserved; sm.u[7][warp][lane] = g;
   }
-  uint32_t incl = nbox;
-#pragma unroll
-  for (int d = 1; d < 32; d <<= 1) {
-    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
-    if (lane >= (uint32_t)d) incl += y;
-  }
-  const uint32_t excl = incl - nbox;
   const uint32_t le = lt | (1u << lane);
-  sm.u[8][warp][lane] = excl;
   sm.filled[warp][lane] = 0u;
   uint32_t filled = 0;
-  const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-
-  // Rounds of 32 box tiles. The boxes lie end to end in lane order, so a
-  // round is a run of segments, one per owning lane: a lane finds its segment
-  // from the OR of the segment starts and the segment's owner from a table
-  // the owners wrote; each owner adds its hits under its own segment mask.
-  for (uint32_t j0 = 0; j0 < total; j0 += 32) {
-    const uint32_t lo = max(excl, j0), hi = min(incl, j0 + 32u);
-    const bool seg = lo < hi;
-    const uint32_t starts = __reduce_or_sync(0xffffffffu, seg ? 1u << (lo - j0) : 0u);
-    const uint32_t owners = __ballot_sync(0xffffffffu, seg);
-    if (seg) sm.own[warp][__popc(owners & lt)] = lane;
-    __syncwarp();
-    const uint32_t j = j0 + lane;
-    const bool valid = j < total;
-    uint32_t owner = 0, seg_start = 0;
-    bool hit = false;
-    uint32_t t = 0;
-    if (valid) {
-      const uint32_t mine = starts & le;
-      owner = sm.own[warp][__popc(mine) - 1u];
-      seg_start = 31u - (uint32_t)__clz(mine);
-      const uint32_t bw = sm.u[2][warp][owner];
-      const uint32_t kk = j - sm.u[8][warp][owner];
-      const uint32_t by = kk / bw, bx = kk - by * bw;
-      const int tx = (int)(sm.u[0][warp][owner] + bx), ty = (int)(sm.u[1][warp][owner] + by);
-      hit = boundary_tile_hit(sm.f[0][warp][owner], sm.f[1][warp][owner], sm.f[2][warp][owner],
-                              sm.f[3][warp][owner], sm.f[4][warp][owner], sm.f[5][warp][owner],
-                              sm.f[6][warp][owner], sm.f[7][warp][owner], tx, ty, sm.f[8][warp][owner],
-                              sm.f[9][warp][owner], o.axis);
-      t = sm.u[4][warp][owner] + (uint32_t)ty * sm.u[3][warp][owner] + (uint32_t)tx;
+  // A splat whose every box tile passed the projection's count (reserved ==
+  // nbox) emits its whole box: those boxes are walked first without the tile
+  // test, the others after it with the test. Each splat is walked once, so
+  // its records keep row-major box order.
+  const bool full = reserved == nbox;
+#pragma unroll 1
+  for (int pass = 0; pass < 2; ++pass) {
+    const uint32_t nb = (pass == 0) == full ? nbox : 0u;
+    uint32_t incl = nb;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
+      if (lane >= (uint32_t)d) incl += y;
     }
-    const uint32_t hits = __ballot_sync(0xffffffffu, hit);
-    if (hit) {
-      // After the owner's earlier hits: those of past rounds, then those of
-      // this round below this lane within the owner's segment.
-      const uint32_t local = sm.filled[warp][owner] + __popc(hits & lt & ~((1u << seg_start) - 1u));
-      const uint32_t base = sm.u[5][warp][owner];
-      if (local < sm.u[6][warp][owner] && base + local < capacity) {
-        tile_keys[base + local] = t;
-        tile_vals[base + local] = sm.u[7][warp][owner];
+    const uint32_t excl = incl - nb;
+    sm.u[8][warp][lane] = excl;
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+
+    // Rounds of 32 box tiles. The boxes lie end to end in lane order, so a
+    // round is a run of segments, one per owning lane: a lane finds its
+    // segment from the OR of the segment starts and the segment's owner from
+    // a table the owners wrote; each owner adds its hits under its own mask.
+    for (uint32_t j0 = 0; j0 < total; j0 += 32) {
+      const uint32_t lo = max(excl, j0), hi = min(incl, j0 + 32u);
+      const bool seg = lo < hi;
+      const uint32_t starts = __reduce_or_sync(0xffffffffu, seg ? 1u << (lo - j0) : 0u);
+      const uint32_t owners = __ballot_sync(0xffffffffu, seg);
+      if (seg) sm.own[warp][__popc(owners & lt)] = lane;
+      __syncwarp();
+      const uint32_t j = j0 + lane;
+      const bool valid = j < total;
+      uint32_t owner = 0, seg_start = 0;
+      bool hit = false;
+      uint32_t t = 0;
+      if (valid) {
+        const uint32_t mine = starts & le;
+        owner = sm.own[warp][__popc(mine) - 1u];
+        seg_start = 31u - (uint32_t)__clz(mine);
+        const uint32_t bw = sm.u[2][warp][owner];
+        const uint32_t kk = j - sm.u[8][warp][owner];
+        const uint32_t by = kk / bw, bx = kk - by * bw;
+        const int tx = (int)(sm.u[0][warp][owner] + bx), ty = (int)(sm.u[1][warp][owner] + by);
+        hit = pass == 0 ||
+              boundary_tile_hit(sm.f[0][warp][owner], sm.f[1][warp][owner], sm.f[2][warp][owner],
+                                sm.f[3][warp][owner], sm.f[4][warp][owner], sm.f[5][warp][owner],
+                                sm.f[6][warp][owner], sm.f[7][warp][owner], tx, ty, sm.f[8][warp][owner],
+                                sm.f[9][warp][owner], o.axis);
+        t = sm.u[4][warp][owner] + (uint32_t)ty * sm.u[3][warp][owner] + (uint32_t)tx;
+      }
+      const uint32_t hits = __ballot_sync(0xffffffffu, hit);
+      if (hit) {
+        // After the owner's earlier hits: those of past rounds, then those of
+        // this round below this lane within the owner's segment.
+        const uint32_t local = sm.filled[warp][owner] + __popc(hits & lt & ~((1u << seg_start) - 1u));
+        const uint32_t base = sm.u[5][warp][owner];
+        if (local < sm.u[6][warp][owner] && base + local < capacity) {
+          tile_keys[base + local] = t;
+          tile_vals[base + local] = sm.u[7][warp][owner];
+        }
+      }
+      __syncwarp();  // every read of filled, the owner table and the walk bases is done
+      if (seg) {
+        filled += __popc(hits & bit_range(lo - j0, hi - j0));
+        sm.filled[warp][lane] = filled;
       }
     }
-    __syncwarp();  // every read of filled and the owner table is done
-    if (seg) {
-      filled += __popc(hits & bit_range(lo - j0, hi - j0));
-      sm.filled[warp][lane] = filled;
-    }
+    __syncwarp();
   }
-  __syncwarp();
 
   // Sentinel padding for reserved slots without a hit.
   if (live) {
