@@ -260,17 +260,47 @@ class TiledGaussianPipeline:
                self._p)
         return list(items), list(tiles)
 
+    @staticmethod
+    def _stats_dict(s: Stats) -> dict:
+        return {"visibleGaussianCount": s.visible_gaussian_count, "intersectionCount": s.intersection_count,
+                "requestedIntersections": s.requested_intersections,
+                "intersectionCapacity": int(s.intersection_capacity), "overflow": bool(s.overflow),
+                "deviceError": int(s.device_error),
+                "rasterWork": {"checked": int(s.raster_checked), "blended": int(s.raster_blended),
+                               "pixels": int(s.raster_pixels), "alphaStopped": int(s.raster_alpha_stopped)}}
+
     def read_stats(self) -> dict:
         s = Stats()
         st = self._lib.gs3d_pipeline_read_stats(self._p, C.byref(s))
-        out = {"visibleGaussianCount": s.visible_gaussian_count, "intersectionCount": s.intersection_count,
-               "requestedIntersections": s.requested_intersections,
-               "intersectionCapacity": int(s.intersection_capacity), "overflow": bool(s.overflow),
-               "deviceError": int(s.device_error),
-               "rasterWork": {"checked": int(s.raster_checked), "blended": int(s.raster_blended),
-                              "pixels": int(s.raster_pixels), "alphaStopped": int(s.raster_alpha_stopped)}}
+        out = self._stats_dict(s)
         _raise(self._lib, st, self._p)
         return out
+
+    def request_stats(self, stream: int = 0) -> None:
+        """Enqueue the asynchronous read-back of the last render's counters
+        (one in flight per pipeline); ``poll_stats`` collects it."""
+        _raise(self._lib, self._lib.gs3d_pipeline_request_stats(self._p, C.c_void_p(int(stream))), self._p)
+
+    def poll_stats(self, wait: bool = False):
+        """The requested counters as read_stats returns them, or None while the
+        copy is still in flight (``wait`` blocks until it lands)."""
+        s = Stats()
+        st = self._lib.gs3d_pipeline_poll_stats(self._p, C.byref(s), 1 if wait else 0)
+        if st == abi.GS3D_NOT_READY:
+            return None
+        out = self._stats_dict(s)
+        _raise(self._lib, st, self._p)
+        return out
+
+    def set_wait_limit(self, polls: int) -> None:
+        """Polls a look-back wait may spend on one status word before the
+        frame reports a device timeout (0: the default, about one second)."""
+        _raise(self._lib, self._lib.gs3d_pipeline_set_wait_limit(self._p, int(polls)), self._p)
+
+    def debug_withhold_chunk(self) -> None:
+        """Test hook: the next render's compaction never scans its first
+        chunk, so the next chunk's look-back wait runs out."""
+        _raise(self._lib, self._lib.gs3d_pipeline_debug_withhold_chunk(self._p), self._p)
 
     def read_profile(self) -> dict:
         """GaussianPassProfileStats of the last render (types.ts:105-148):
@@ -323,6 +353,12 @@ class TiledGaussianPipeline:
             self.dispose()
         except Exception:
             pass
+
+
+def debug_fail_allocation(nth: int) -> None:
+    """Test hook: the nth device allocation the library makes from now on
+    (1 = the next one) fails as out of memory; 0 disarms."""
+    load().gs3d_debug_fail_allocation(int(nth))
 
 
 def pack_splats(centers, scales, opacity, quaternions, rgb, sh_rest, first_slot: int, means, scales_opacity,

@@ -12,10 +12,11 @@ GS3D_ERROR_OUT_OF_MEMORY = 4
 GS3D_ERROR_CUDA = 5
 GS3D_ERROR_DEVICE_TIMEOUT = 6
 GS3D_ERROR_UNSUPPORTED = 7
+GS3D_NOT_READY = 8
 STATIC_COMPACT_MAX_ITEMS = 16777216
 STAGES = ("project", "compact", "depth_sort", "scan", "emit", "tile_sort", "ranges", "raster")
 STATUS_NAMES = {0: "ok", 1: "invalid-argument", 2: "range", 3: "not-prepared", 4: "allocation-failed",
-                5: "cuda-error", 6: "device-timeout", 7: "unsupported"}
+                5: "cuda-error", 6: "device-timeout", 7: "unsupported", 8: "not-ready"}
 
 
 class GaussianData(C.Structure):
@@ -118,6 +119,11 @@ SIGNATURES = {
     "gs3d_pipeline_batch_layout": (C.c_int, [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.c_uint32,
                                              C.POINTER(C.c_uint32)]),
     "gs3d_pipeline_read_stats": (C.c_int, [_P, C.POINTER(Stats)]),
+    "gs3d_pipeline_request_stats": (C.c_int, [_P, _P]),
+    "gs3d_pipeline_poll_stats": (C.c_int, [_P, C.POINTER(Stats), C.c_int]),
+    "gs3d_pipeline_set_wait_limit": (C.c_int, [_P, C.c_uint32]),
+    "gs3d_pipeline_debug_withhold_chunk": (C.c_int, [_P]),
+    "gs3d_debug_fail_allocation": (None, [C.c_uint32]),
     "gs3d_pipeline_get_resources": (C.c_int, [_P, C.POINTER(Resources)]),
     "gs3d_pipeline_read_profile": (C.c_int, [_P, C.POINTER(ProfileStats)]),
     "gs3d_pipeline_last_error": (C.c_char_p, [_P]),

@@ -110,15 +110,19 @@ enum Ticket { kTicketCompact = 0, kTicketScan = 1 };
 // so a replayed CUDA graph never reuses an epoch.
 constexpr uint32_t kEpochsPerFrame = 16;
 
-// The epoch of look-back launch `index` of the current frame.
+constexpr uint32_t kSpinLimit = 1u << 22;  // default polls before a wait is declared expired (about 1 s)
+
+// The epoch of look-back launch `add` of the current frame, and how many
+// polls a wait of that launch may spend on one status word.
 struct Epoch {
-  const uint32_t* base;  // device counter, or null for a host-chosen epoch
+  const uint32_t* base;  // device counter
   uint32_t add;
-  __device__ __forceinline__ uint32_t get() const { return (base ? *base : 0u) + add; }
+  uint32_t spin_limit;   // 0: kSpinLimit
+  __device__ __forceinline__ uint32_t get() const { return *base + add; }
+  __device__ __forceinline__ uint32_t limit() const { return spin_limit ? spin_limit : kSpinLimit; }
 };
 constexpr unsigned long long kFlagAggregate = 1ull;
 constexpr unsigned long long kFlagInclusive = 2ull;
-constexpr uint32_t kSpinLimit = 1u << 22;  // polls before a wait is declared expired
 
 __device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long* p) {
   unsigned long long v;
@@ -137,10 +141,11 @@ __device__ __forceinline__ uint32_t sat_add(uint32_t a, uint32_t b) { return a +
 // word gets bit 0 and the caller treats the word as an inclusive zero, so the
 // kernel always finishes and the host sees the error.
 __device__ __forceinline__ unsigned long long wait_status(const unsigned long long* p, unsigned long long v,
-                                                          uint32_t epoch, uint32_t* err, bool* expired) {
+                                                          uint32_t epoch, uint32_t limit, uint32_t* err,
+                                                          bool* expired) {
   uint32_t polls = 0, backoff = 8;
   while ((uint32_t)(v >> 34) != epoch) {
-    if (++polls >= kSpinLimit) {
+    if (++polls >= limit) {
       atomicOr(err, 1u);
       *expired = true;
       return 0;
@@ -160,7 +165,7 @@ __device__ __forceinline__ unsigned long long wait_status(const unsigned long lo
 // warp must call it.
 template <bool SATURATE, int K = 4>
 __device__ __forceinline__ uint32_t warp_lookback(const unsigned long long* status, uint32_t tile, uint32_t epoch,
-                                                  uint32_t* err) {
+                                                  uint32_t limit, uint32_t* err) {
   const uint32_t lane = threadIdx.x & 31u;
   uint32_t excl = 0;
   int64_t end = (int64_t)tile - 1;
@@ -178,7 +183,7 @@ __device__ __forceinline__ uint32_t warp_lookback(const unsigned long long* stat
       bool incl = true, expired = false;
       uint32_t val = 0;
       if (idx >= 0) {
-        const unsigned long long w = wait_status(status + idx, v[k], epoch, err, &expired);
+        const unsigned long long w = wait_status(status + idx, v[k], epoch, limit, err, &expired);
         incl = expired || ((w >> 32) & 3ull) == kFlagInclusive;
         val = expired ? 0u : (uint32_t)w;
       }
@@ -244,6 +249,10 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* s
 void launch_project(const BatchView& b, const PassOptions& o, float4* mean, float4* conic, float4* color,
                     uint32_t* counts, uint32_t* keys, float4* rec, float4* erec, cudaStream_t st);
 void launch_epoch_begin(uint32_t* epoch_base, cudaStream_t st);
+// Advance ticket counter `ticket` of the control block by one (a test hook:
+// the chunk of ticket 0 is then never scanned, so its successor's look-back
+// wait runs out).
+void launch_skip_ticket(Control* ctl, uint32_t ticket, cudaStream_t st);
 void launch_compact(const uint32_t* keys, uint32_t n, uint32_t* vis_off, uint32_t* keys_out, uint32_t* vals_out,
                     Control* ctl, unsigned long long* status, Epoch epoch, uint32_t chunks, cudaStream_t st);
 void launch_scan_counts(const uint32_t* sorted_ids, const uint32_t* tile_counts, uint32_t* ordered,

@@ -341,7 +341,7 @@ __device__ __forceinline__ void warp_units(uint32_t u0, uint32_t u1, uint32_t wa
 // Every lane gets the chunk's exclusive prefix and its total.
 template <bool SAT>
 __device__ __forceinline__ void chunk_publish(uint32_t* s_warp, unsigned long long* status, uint32_t c,
-                                              uint32_t epoch, uint32_t* err, uint32_t* prefix_out,
+                                              uint32_t epoch, uint32_t limit, uint32_t* err, uint32_t* prefix_out,
                                               uint32_t* total_out) {
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t wc = lane < kScanWarps ? s_warp[lane] : 0u;
@@ -360,7 +360,7 @@ __device__ __forceinline__ void chunk_publish(uint32_t* s_warp, unsigned long lo
     if (lane == 0) st_release(mine, pack_status(epoch, kFlagInclusive, total));
   } else {
     if (lane == 0) st_release(mine, pack_status(epoch, kFlagAggregate, total));
-    prefix = warp_lookback<SAT>(status, c, epoch, err);
+    prefix = warp_lookback<SAT>(status, c, epoch, limit, err);
     if (lane == 0) st_release(mine, pack_status(epoch, kFlagInclusive, SAT ? sat_add(prefix, total) : prefix + total));
   }
   if (lane < kScanWarps) s_warp[lane] = SAT ? sat_add(prefix, excl) : prefix + excl;
@@ -405,7 +405,7 @@ __global__ void __launch_bounds__(kBlock) k_compact(const uint32_t* __restrict__
   __syncthreads();
   if (warp == 0) {
     uint32_t prefix, total;
-    chunk_publish<false>(s_warp, status, c, ep.get(), &ctl->error, &prefix, &total);
+    chunk_publish<false>(s_warp, status, c, ep.get(), ep.limit(), &ctl->error, &prefix, &total);
     if (lane == 0 && last) {
       const uint32_t v = prefix + total;
       ctl->visible_state[0] = v;
@@ -449,6 +449,10 @@ __global__ void k_epoch_begin(uint32_t* base) {
 }
 
 void launch_epoch_begin(uint32_t* epoch_base, cudaStream_t st) { k_epoch_begin<<<1, 1, 0, st>>>(epoch_base); }
+
+__global__ void k_skip_ticket(Control* ctl, uint32_t ticket) { ctl->tickets[ticket] += 1u; }
+
+void launch_skip_ticket(Control* ctl, uint32_t ticket, cudaStream_t st) { k_skip_ticket<<<1, 1, 0, st>>>(ctl, ticket); }
 
 uint32_t scan_chunks(uint32_t n_max, int sms) {
   const uint64_t units = ((uint64_t)n_max + kUnit - 1) / kUnit;
@@ -510,7 +514,7 @@ __global__ void __launch_bounds__(kBlock) k_scan_counts(const uint32_t* __restri
   __syncthreads();
   if (warp == 0) {
     uint32_t prefix, total;
-    chunk_publish<true>(s_warp, status, c, ep.get(), &ctl->error, &prefix, &total);
+    chunk_publish<true>(s_warp, status, c, ep.get(), ep.limit(), &ctl->error, &prefix, &total);
     if (lane == 0 && last) {
       const uint32_t all = sat_add(prefix, total);
       const bool overflow = all > capacity;

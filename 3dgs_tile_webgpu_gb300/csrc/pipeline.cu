@@ -3,10 +3,12 @@
 // TiledGaussianPipeline.render (src/renderer/pipeline/TiledGaussianPipeline.ts:324-341).
 #include <cuda_runtime.h>
 #include <math.h>
+#include <stddef.h>
 #include <stdint.h>
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <new>
 #include <string>
 #include <vector>
@@ -157,6 +159,17 @@ struct gs3d_pipeline {
   // Final buffers of the two sorts (after ping-pong).
   int depth_final = 0;
   int tile_final = 0;
+  // Asynchronous stats read-back (gs3d_pipeline_request_stats / poll_stats):
+  // pinned copy of the counters, its completion event, and the layout of the
+  // render it describes.
+  unsigned char* rb_pinned = nullptr;
+  cudaEvent_t rb_event = nullptr;
+  bool rb_pending = false;
+  uint32_t rb_chunks = 1;
+  // Polls a look-back wait may spend on one status word (0: the default),
+  // and the test hook that withholds the compaction's first chunk.
+  uint32_t wait_limit = 0;
+  bool withhold_first_chunk = false;
   // Kernel timing: one set of GS3D_STAGE_COUNT + 1 events per profiled render.
   bool profiling = false;
   std::vector<cudaEvent_t> events;  // pool, in sets of kStageEvents
@@ -182,11 +195,23 @@ void dfree(T*& ptr) {
   ptr = nullptr;
 }
 
+// Allocation-failure injection (gs3d_debug_fail_allocation): the countdown
+// reaches zero on the device allocation that is made to fail.
+std::atomic<int64_t> g_fail_countdown{0};
+
+cudaError_t device_malloc(void** ptr, size_t bytes) {
+  if (g_fail_countdown.load() > 0 && g_fail_countdown.fetch_sub(1) == 1) {
+    *ptr = nullptr;
+    return cudaErrorMemoryAllocation;
+  }
+  return cudaMalloc(ptr, bytes);
+}
+
 template <typename T>
 cudaError_t dalloc(T*& ptr, size_t count) {
   dfree(ptr);
   if (count == 0) count = 1;
-  return cudaMalloc((void**)&ptr, count * sizeof(T));
+  return device_malloc((void**)&ptr, count * sizeof(T));
 }
 
 uint32_t tiles_for(uint32_t px) { return (px + 15u) / 16u; }
@@ -245,41 +270,67 @@ size_t status_words_needed(uint32_t slots, uint64_t capacity) {
 gs3d_status ensure_status(gs3d_pipeline* p) {
   const size_t need = status_words_needed(p->slot_cap, p->capacity);
   if (need <= p->status_words) return GS3D_OK;
-  cudaError_t e = dalloc(p->status, need);
-  if (e != cudaSuccess) return cuda_fail(p, e, "allocating look-back status");
-  e = cudaMemset(p->status, 0, need * sizeof(unsigned long long));
-  if (e != cudaSuccess) return cuda_fail(p, e, "clearing look-back status");
+  unsigned long long* fresh = nullptr;
+  cudaError_t e = dalloc(fresh, need);
+  if (e == cudaSuccess) e = cudaMemset(fresh, 0, need * sizeof(unsigned long long));
+  if (e != cudaSuccess) {
+    dfree(fresh);
+    return cuda_fail(p, e, "allocating look-back status");
+  }
+  dfree(p->status);
+  p->status = fresh;
   p->status_words = need;
   p->epoch = 0;
   return GS3D_OK;
+}
+
+// Grows every buffer of `bufs` to its new element count, or none of them: on
+// a failed allocation the new buffers are released and the old ones kept, so
+// the pipeline stays usable at its previous size ("allocation-failed" leaves
+// the previous resources in place, GaussianPass.ts:808-826).
+struct Grow {
+  void** slot;
+  size_t bytes;
+};
+cudaError_t grow_all(Grow* bufs, size_t n) {
+  std::vector<void*> fresh(n, nullptr);
+  cudaError_t e = cudaSuccess;
+  for (size_t i = 0; i < n && e == cudaSuccess; ++i) e = device_malloc(&fresh[i], std::max<size_t>(bufs[i].bytes, 1));
+  if (e != cudaSuccess) {
+    for (void* q : fresh)
+      if (q) cudaFree(q);
+    return e;
+  }
+  for (size_t i = 0; i < n; ++i) {
+    if (*bufs[i].slot) cudaFree(*bufs[i].slot);
+    *bufs[i].slot = fresh[i];
+  }
+  return cudaSuccess;
 }
 
 gs3d_status ensure_slots(gs3d_pipeline* p, uint32_t count) {
   if (count <= p->slot_cap) return GS3D_OK;
   // AttributePool.grow semantics: at least double.
   const uint32_t cap = std::max(count, p->slot_cap * 2u);
-  cudaError_t e = cudaSuccess;
-  if ((e = dalloc(p->mean, cap)) || (e = dalloc(p->conic, cap)) || (e = dalloc(p->color, cap)) ||
-      (e = dalloc(p->rec, 2 * (size_t)cap)) || (e = dalloc(p->erec, 2 * (size_t)cap)) ||
-      (e = dalloc(p->counts, cap)) || (e = dalloc(p->keys, cap)) || (e = dalloc(p->vis_off, cap)) ||
-      (e = dalloc(p->dk[0], cap)) || (e = dalloc(p->dk[1], cap)) || (e = dalloc(p->dv[0], cap)) ||
-      (e = dalloc(p->dv[1], cap)) || (e = dalloc(p->ordered, cap)) || (e = dalloc(p->ioff, cap))) {
-    p->slot_cap = 0;
-    return cuda_fail(p, e, "allocating per-Gaussian workspaces");
-  }
-  cudaMemset(p->conic, 0, (size_t)cap * sizeof(float4));
-  cudaMemset(p->color, 0, (size_t)cap * sizeof(float4));
+  const size_t f4 = (size_t)cap * sizeof(float4), u = (size_t)cap * sizeof(uint32_t);
+  Grow bufs[] = {{(void**)&p->mean, f4},    {(void**)&p->conic, f4},   {(void**)&p->color, f4},
+                 {(void**)&p->rec, 2 * f4}, {(void**)&p->erec, 2 * f4}, {(void**)&p->counts, u},
+                 {(void**)&p->keys, u},     {(void**)&p->vis_off, u}, {(void**)&p->dk[0], u},
+                 {(void**)&p->dk[1], u},    {(void**)&p->dv[0], u},   {(void**)&p->dv[1], u},
+                 {(void**)&p->ordered, u},  {(void**)&p->ioff, u}};
+  cudaError_t e = grow_all(bufs, sizeof(bufs) / sizeof(bufs[0]));
+  if (e != cudaSuccess) return cuda_fail(p, e, "allocating per-Gaussian workspaces");
+  cudaMemset(p->conic, 0, f4);
+  cudaMemset(p->color, 0, f4);
   p->slot_cap = cap;
   return ensure_status(p);
 }
 
 gs3d_status ensure_capacity(gs3d_pipeline* p, uint64_t capacity) {
-  cudaError_t e = cudaSuccess;
-  if ((e = dalloc(p->tk[0], capacity)) || (e = dalloc(p->tk[1], capacity)) || (e = dalloc(p->tv[0], capacity)) ||
-      (e = dalloc(p->tv[1], capacity))) {
-    p->capacity = 0;
-    return cuda_fail(p, e, "allocating intersection workspaces");
-  }
+  const size_t u = (size_t)capacity * sizeof(uint32_t);
+  Grow bufs[] = {{(void**)&p->tk[0], u}, {(void**)&p->tk[1], u}, {(void**)&p->tv[0], u}, {(void**)&p->tv[1], u}};
+  cudaError_t e = grow_all(bufs, 4);
+  if (e != cudaSuccess) return cuda_fail(p, e, "allocating intersection workspaces");
   p->capacity = capacity;
   return ensure_status(p);
 }
@@ -287,6 +338,7 @@ gs3d_status ensure_capacity(gs3d_pipeline* p, uint64_t capacity) {
 gs3d_status ensure_stage(gs3d_pipeline* p, size_t bytes) {
   if (bytes <= p->stage_cap) return GS3D_OK;
   const size_t cap = std::max(bytes, std::max<size_t>(16384, p->stage_cap * 2));
+  p->stage_cap = 0;  // until every slot is regrown
   for (uint32_t i = 0; i < kObjectRing; ++i) {
     if (p->stage_ev_used[i]) cudaEventSynchronize(p->stage_ev[i]);
     dfree(p->stage_dev[i]);
@@ -360,6 +412,13 @@ void release_graphs(gs3d_pipeline* p) {
 
 void release_all(gs3d_pipeline* p) {
   release_graphs(p);
+  if (p->rb_event) {
+    cudaEventSynchronize(p->rb_event);
+    cudaEventDestroy(p->rb_event);
+  }
+  if (p->rb_pinned) cudaFreeHost(p->rb_pinned);
+  p->rb_event = nullptr;
+  p->rb_pinned = nullptr;
   for (cudaEvent_t e : p->events) cudaEventDestroy(e);
   p->events.clear();
   for (uint32_t i = 0; i < kObjectRing; ++i) {
@@ -392,6 +451,7 @@ const char* gs3d_status_string(gs3d_status s) {
     case GS3D_ERROR_CUDA: return "CUDA error";
     case GS3D_ERROR_DEVICE_TIMEOUT: return "device wait expired";
     case GS3D_ERROR_UNSUPPORTED: return "unsupported option";
+    case GS3D_NOT_READY: return "not ready";
   }
   return "unknown status";
 }
@@ -714,10 +774,18 @@ void record_batch(gs3d_pipeline* p, const Plan& pl, unsigned char* dev, cudaStre
   uint32_t launches = 0;
   Control* ctl = p->ctl;
   uint32_t ep = 0;  // look-back launch index within the frame
-  auto epoch = [&]() { return Epoch{p->epoch_dev, ++ep}; };
+  auto epoch = [&]() { return Epoch{p->epoch_dev, ++ep, p->wait_limit}; };
   launch_epoch_begin(p->epoch_dev, st);
   cudaMemsetAsync(ctl, 0, sizeof(Control), st);
   launches += 1;
+  if (p->withhold_first_chunk) {
+    // Test hook (gs3d_pipeline_debug_withhold_chunk): the compaction's ticket
+    // counter starts at 1, so no block scans chunk 0 and the look-back of
+    // chunk 1 waits on a status word that is never published.
+    launch_skip_ticket(ctl, kTicketCompact, st);
+    p->withhold_first_chunk = false;
+    ++launches;
+  }
 
   // K1: projection.
   mark(p, GS3D_STAGE_PROJECT, st);
@@ -1075,19 +1143,24 @@ gs3d_status gs3d_pipeline_batch_layout(gs3d_pipeline* p, uint32_t* item_base, ui
   return GS3D_OK;
 }
 
-gs3d_status gs3d_pipeline_read_stats(gs3d_pipeline* p, gs3d_stats* out) {
-  if (!p || !out) return GS3D_ERROR_INVALID_ARGUMENT;
-  cudaSetDevice(p->device);
-  cudaError_t e = cudaStreamSynchronize(p->last_stream);
-  if (e != cudaSuccess) return cuda_fail(p, e, "synchronising the render stream");
+}  // extern "C"
+
+namespace {
+
+// The counters of a finished render: the part of the control block from
+// visible_state to raster_stats, and the batch summary (used when the batch
+// ran as several launch sequences).
+constexpr size_t kCountersOffset = offsetof(Control, visible_state);
+constexpr size_t kCountersBytes = offsetof(Control, order_hist) - offsetof(Control, visible_state);
+constexpr size_t kReadbackBytes = kCountersBytes + sizeof(BatchSummary);
+
+gs3d_status fill_stats(gs3d_pipeline* p, const unsigned char* counters, const BatchSummary* summary, uint32_t chunks,
+                       gs3d_stats* out) {
   Control c;
-  e = cudaMemcpy(&c, p->ctl, sizeof(Control), cudaMemcpyDeviceToHost);
-  if (e != cudaSuccess) return cuda_fail(p, e, "reading the pass state");
-  if (p->last_chunks > 1) {
+  memcpy((unsigned char*)&c + kCountersOffset, counters, kCountersBytes);
+  if (chunks > 1) {
     // A batch of several launch sequences: the totals of all of them.
-    BatchSummary b;
-    e = cudaMemcpy(&b, p->summary, sizeof(b), cudaMemcpyDeviceToHost);
-    if (e != cudaSuccess) return cuda_fail(p, e, "reading the batch summary");
+    const BatchSummary& b = *summary;
     c.visible_state[0] = b.visible;
     c.state[0] = b.intersections;
     c.state[1] = b.requested;
@@ -1109,6 +1182,84 @@ gs3d_status gs3d_pipeline_read_stats(gs3d_pipeline* p, gs3d_stats* out) {
   if (c.error) return fail(p, GS3D_ERROR_DEVICE_TIMEOUT, "a device-side look-back wait expired");
   return GS3D_OK;
 }
+
+}  // namespace
+
+extern "C" {
+
+gs3d_status gs3d_pipeline_read_stats(gs3d_pipeline* p, gs3d_stats* out) {
+  if (!p || !out) return GS3D_ERROR_INVALID_ARGUMENT;
+  cudaSetDevice(p->device);
+  cudaError_t e = cudaStreamSynchronize(p->last_stream);
+  if (e != cudaSuccess) return cuda_fail(p, e, "synchronising the render stream");
+  unsigned char counters[kCountersBytes];
+  BatchSummary b{};
+  e = cudaMemcpy(counters, (const unsigned char*)p->ctl + kCountersOffset, kCountersBytes, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(p, e, "reading the pass state");
+  if (p->last_chunks > 1) {
+    e = cudaMemcpy(&b, p->summary, sizeof(b), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(p, e, "reading the batch summary");
+  }
+  return fill_stats(p, counters, &b, p->last_chunks, out);
+}
+
+gs3d_status gs3d_pipeline_request_stats(gs3d_pipeline* p, void* stream) {
+  if (!p) return GS3D_ERROR_INVALID_ARGUMENT;
+  if (p->rb_pending) return fail(p, GS3D_ERROR_UNSUPPORTED, "a stats read-back is already in flight");
+  cudaSetDevice(p->device);
+  cudaError_t e = cudaSuccess;
+  if (!p->rb_pinned && (e = cudaMallocHost((void**)&p->rb_pinned, kReadbackBytes)) != cudaSuccess) {
+    p->rb_pinned = nullptr;
+    return cuda_fail(p, e, "allocating the pinned read-back buffer");
+  }
+  if (!p->rb_event && (e = cudaEventCreateWithFlags(&p->rb_event, cudaEventDisableTiming)) != cudaSuccess) {
+    p->rb_event = nullptr;
+    return cuda_fail(p, e, "creating the read-back event");
+  }
+  cudaStream_t st = stream ? (cudaStream_t)stream : p->last_stream;
+  if (st != p->last_stream && p->last_stream) {
+    // Order the copies after the last render's stream.
+    if ((e = cudaEventRecord(p->rb_event, p->last_stream)) != cudaSuccess ||
+        (e = cudaStreamWaitEvent(st, p->rb_event, 0)) != cudaSuccess)
+      return cuda_fail(p, e, "ordering the read-back after the render");
+  }
+  p->rb_chunks = p->last_chunks;
+  if ((e = cudaMemcpyAsync(p->rb_pinned, (const unsigned char*)p->ctl + kCountersOffset, kCountersBytes,
+                           cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+      (p->rb_chunks > 1 && (e = cudaMemcpyAsync(p->rb_pinned + kCountersBytes, p->summary, sizeof(BatchSummary),
+                                                cudaMemcpyDeviceToHost, st)) != cudaSuccess) ||
+      (e = cudaEventRecord(p->rb_event, st)) != cudaSuccess)
+    return cuda_fail(p, e, "enqueueing the stats read-back");
+  p->rb_pending = true;
+  return GS3D_OK;
+}
+
+gs3d_status gs3d_pipeline_poll_stats(gs3d_pipeline* p, gs3d_stats* out, int wait) {
+  if (!p || !out) return GS3D_ERROR_INVALID_ARGUMENT;
+  if (!p->rb_pending) return fail(p, GS3D_ERROR_NOT_PREPARED, "no stats read-back was requested");
+  cudaSetDevice(p->device);
+  cudaError_t e = wait ? cudaEventSynchronize(p->rb_event) : cudaEventQuery(p->rb_event);
+  if (e == cudaErrorNotReady) return GS3D_NOT_READY;
+  p->rb_pending = false;
+  if (e != cudaSuccess) return cuda_fail(p, e, "waiting for the stats read-back");
+  return fill_stats(p, p->rb_pinned, (const BatchSummary*)(p->rb_pinned + kCountersBytes), p->rb_chunks, out);
+}
+
+gs3d_status gs3d_pipeline_set_wait_limit(gs3d_pipeline* p, uint32_t polls) {
+  if (!p) return GS3D_ERROR_INVALID_ARGUMENT;
+  if (p->last_stream) cudaStreamSynchronize(p->last_stream);
+  release_graphs(p);  // captured graphs hold the limit they were captured with
+  p->wait_limit = polls;
+  return GS3D_OK;
+}
+
+gs3d_status gs3d_pipeline_debug_withhold_chunk(gs3d_pipeline* p) {
+  if (!p) return GS3D_ERROR_INVALID_ARGUMENT;
+  p->withhold_first_chunk = true;
+  return GS3D_OK;
+}
+
+void gs3d_debug_fail_allocation(uint32_t nth) { g_fail_countdown.store((int64_t)nth); }
 
 gs3d_status gs3d_pipeline_get_resources(gs3d_pipeline* p, gs3d_resources* r) {
   if (!p || !r) return GS3D_ERROR_INVALID_ARGUMENT;

@@ -46,7 +46,9 @@ typedef enum gs3d_status {
   /* A bounded device-side wait (scan/sort look-back) gave up; the frame is invalid. */
   GS3D_ERROR_DEVICE_TIMEOUT = 6,
   /* The build does not support the requested option. */
-  GS3D_ERROR_UNSUPPORTED = 7
+  GS3D_ERROR_UNSUPPORTED = 7,
+  /* Not an error: an asynchronous read-back has not landed yet. */
+  GS3D_NOT_READY = 8
 } gs3d_status;
 
 /* DepthSortMode (types.ts:11). */
@@ -285,6 +287,37 @@ gs3d_status gs3d_pipeline_batch_layout(gs3d_pipeline* pipeline, uint32_t* item_b
 /* readStats() (TiledGaussianPipeline.ts:353-366): synchronises the stream of
  * the last render. */
 gs3d_status gs3d_pipeline_read_stats(gs3d_pipeline* pipeline, gs3d_stats* stats);
+/* readStats() without blocking, the way GaussianPass reads its output state
+ * (GaussianPass.ts:1019-1079: one read-back in flight, resolved when the GPU
+ * has passed it). request_stats enqueues a copy of the last render's counters
+ * into pinned memory owned by the pipeline, on `stream` (NULL: the last
+ * render's stream) after the last render, and returns at once;
+ * GS3D_ERROR_UNSUPPORTED if a read-back is already in flight. poll_stats
+ * returns GS3D_NOT_READY while the copy is in flight (wait = 0), or waits
+ * for it (wait != 0), then fills *stats exactly as read_stats does (including
+ * GS3D_ERROR_DEVICE_TIMEOUT) and ends the read-back. */
+gs3d_status gs3d_pipeline_request_stats(gs3d_pipeline* pipeline, void* stream);
+gs3d_status gs3d_pipeline_poll_stats(gs3d_pipeline* pipeline, gs3d_stats* stats, int wait);
+
+/* Failure detection (no counterpart in the reference, whose GPU waits cannot
+ * hang: WebGPU has no inter-workgroup spin). The compaction and scan kernels
+ * wait on their predecessors' look-back status words; a wait that spends
+ * `polls` polls (with nanosleep back-off) on one word gives up, the frame
+ * reports GS3D_ERROR_DEVICE_TIMEOUT through read_stats / poll_stats, nothing
+ * is left running and the pipeline stays usable. 0 restores the default of
+ * 4,194,304 polls (about one second). Releases captured graphs. */
+gs3d_status gs3d_pipeline_set_wait_limit(gs3d_pipeline* pipeline, uint32_t polls);
+/* Test hook for that path: the next render's visibility compaction never
+ * scans its first chunk, so the look-back of the chunk after it waits on a
+ * status word that nothing publishes until the wait limit runs out. The
+ * render needs at least two compaction chunks (more than 256 active splats). */
+gs3d_status gs3d_pipeline_debug_withhold_chunk(gs3d_pipeline* pipeline);
+/* Test hook for the "allocation-failed" status (types.ts:209-233): the nth
+ * device allocation the library makes from now on (1 = the next one) fails
+ * as if the device were out of memory; 0 disarms. A failed workspace growth
+ * returns GS3D_ERROR_OUT_OF_MEMORY and keeps the previous workspaces, so the
+ * pipeline keeps rendering at its previous size. Process-wide. */
+void gs3d_debug_fail_allocation(uint32_t nth);
 /* getResources() (TiledGaussianPipeline.ts:391-406). */
 gs3d_status gs3d_pipeline_get_resources(gs3d_pipeline* pipeline, gs3d_resources* resources);
 /* Message of the last failed call on this pipeline ("" if none). */
@@ -384,20 +417,21 @@ gs3d_status gs3d_pack_splats(const gs3d_splat_source* source, uint32_t first_slo
 
 /* Visibility compaction with no device allocation. This entry point has no
  * counterpart in the reference. It serves callers that cannot call cudaMalloc
- * where they enqueue work: code running during CUDA graph capture, hosts that
- * route all device memory through their own arena, real-time loops that must
- * not stall on the allocator. The caller passes every input and output; the
- * kernel's scratch is a static device array of about 40 KB per GPU, held
- * until the process exits.
+ * where they enqueue work: hosts that route all device memory through their
+ * own arena or allocator (and must not see allocations they did not make),
+ * and real-time loops that must not stall on the driver's allocator. The
+ * caller passes every input and output; the kernel's scratch is a static
+ * device array of about 41 KB per GPU, held until the process exits.
  *   keys[n]            per-ordinal depth key, 0xffffffff = not visible
  *   visible_offsets[n] exclusive count of visible ordinals before each one
  *   keys_out/ids_out   (key, ordinal) of the visible ordinals, in ordinal order
  *   result[2]          device words: visible count, error flags (nonzero: a
  *                      bounded device wait expired)
  * n must not exceed GS3D_STATIC_COMPACT_MAX_ITEMS (else GS3D_ERROR_RANGE);
- * keys must be 16-byte aligned. The first call on a device sets up the static
- * array's address and must come before any stream capture. All calls share
- * the array: calls that overlap on the GPU race, so order them on one stream. */
+ * keys must be 4-byte aligned. The first call on a device looks up the static
+ * array's device address and the SM count. All calls share the array, which
+ * keeps the previous call's contents (each call clears what must start at
+ * zero): calls that overlap on the GPU race, so order them on one stream. */
 #define GS3D_STATIC_COMPACT_MAX_ITEMS 16777216u
 gs3d_status gs3d_compact_visible_static(const uint32_t* keys, uint32_t n, uint32_t* visible_offsets,
                                         uint32_t* keys_out, uint32_t* ids_out, uint32_t* result, void* stream);
