@@ -53,13 +53,34 @@ __device__ uint32_t encode_oct101012(float qx, float qy, float qz, float qw) {
   return (r << 20) | (v << 10) | u;
 }
 
+// The shared exponent of engine.rs:1945, `max.log2().ceil()` on an f32: the
+// ceiling of log2 rounded to f32. It equals the exact ceiling except just
+// above a power of two 2^e (e != 0), where log2 rounds down to e itself and
+// the exponent stays e instead of e + 1. Decided exactly: the f32 neighbour
+// of e towards e + 1 lies ulp(e) above a positive e, and below |e| by
+// ulp(|e|) (half that when |e| is a power of two) for a negative e; log2
+// rounds to e when log2(m) is under half that gap. log2(m) is evaluated in
+// double, far more precisely than the decision needs.
+__device__ int rounded_log2_ceil(float mx) {
+  if (isnan(mx)) return 0;       // Rust's saturating cast of NaN
+  if (isinf(mx)) return 127;     // clamped below
+  int ex = 0;
+  const float f = frexpf(mx, &ex);  // mx = f 2^ex, f in [0.5, 1)
+  if (f == 0.5f) return ex - 1;      // a power of two
+  const int e = ex - 1;              // floor(log2 mx); mantissa m = 2 f in (1, 2)
+  if (e == 0) return 1;              // log2 m itself is representable: above 0
+  const int a = e > 0 ? e : -e;
+  int gap_exp = (31 - __clz(a)) - 23;
+  if (e < 0 && (a & (a - 1)) == 0) gap_exp -= 1;
+  const double log2_m = log1p((double)(2.0f * f) - 1.0) * 1.4426950408889634074;
+  return log2_m < ldexp(1.0, gap_exp - 1) ? e : e + 1;
+}
+
 // engine.rs:1940-1949 pack_sh.
 __device__ uint32_t pack_sh(float r, float g, float b) {
   const float mx = fmaxf(fmaxf(fabsf(r), fabsf(g)), fabsf(b));
   if (mx == 0.0f) return 0u;
-  int ex = 0;
-  const float m = frexpf(mx, &ex);  // mx = m 2^ex, m in [0.5, 1)
-  int e = m == 0.5f ? ex - 1 : ex;   // ceil(log2 mx)
+  int e = rounded_log2_ceil(mx);
   e = e < -126 ? -126 : (e > 127 ? 127 : e);
   const float mult = 127.0f / ldexpf(1.0f, e);
   const float c[3] = {r, g, b};

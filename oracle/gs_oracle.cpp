@@ -21,7 +21,7 @@
 // golden, so image-level parity is pinned only through these function-level
 // tests.
 //
-// Build: oracle/build_oracle.sh (g++ -O2 -ffp-contract=off -fopenmp).
+// Build: oracle/__init__.py build() (g++ -O2 -std=c++17 -ffp-contract=off -fno-fast-math -fopenmp).
 
 #include <math.h>
 #include <stdint.h>
@@ -577,7 +577,7 @@ uint32_t gso_pack_sh(const float* rgb) {
   if (mx == 0.0f) return 0u;
   float e = ceilf(log2f(mx));
   e = e < -126.0f ? -126.0f : (e > 127.0f ? 127.0f : e);
-  int exponent = (int)e;
+  int exponent = isnan(e) ? 0 : (int)e;  // Rust's `as i32` maps NaN to 0
   float mult = 127.0f / ldexpf(1.0f, exponent);
   uint32_t b[3];
   for (int i = 0; i < 3; ++i) {
