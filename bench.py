@@ -650,11 +650,43 @@ def main() -> None:
         gbs = b / (ms * 1e-3) / 1e9 if ms > 0 else 0.0
         stages[name] = {"ms": ms, "bytes": b, "GB/s": gbs, "frac": gbs / hbm}
     dom = max(stages, key=lambda k: stages[k]["ms"])
+
+    # The raster's own bound is FP32 arithmetic, not HBM: FLOPs = 12 checked
+    # + 10 blended samples (the reference's rasterStats counters,
+    # TileRasterizer.ts:545-546,617,702), counted in an untimed pass of the
+    # same batch with the counters on, over the raster's CUDA-event time,
+    # against SMs x 128 FP32 lanes x 2 x the median SM clock sampled during
+    # the timed steps (MEASURED_PEAKS.json carries no FP32 figure).
+    counting = P.TiledGaussianPipeline(ds.data(), {"raster_precision": args.precision, "raster_stats": True,
+                                                   "intersection_capacity": int(demand * 1.25 * ncam) + 256})
+    counting.set_tuning(tuning)
+    counting.render_batch(views)
+    work = counting.read_stats()["rasterWork"]
+    counting.dispose()
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    clock_mhz = clock_info.get("sm_mhz") or 2070.0
+    fp32_peak = sms * 128 * 2 * clock_mhz * 1e6 / 1e12  # TFLOP/s
+    raster_flops = 12 * work["checked"] + 10 * work["blended"]
+    raster_s = stage_ms["raster"] * 1e-3
+    raster_tflops = raster_flops / raster_s / 1e12 if raster_s > 0 else 0.0
+    raster_fp32 = {"kernel": "raster", "bound": "fp32", "achieved": raster_tflops, "peak": fp32_peak,
+                   "unit": "TFLOP/s", "frac": raster_tflops / fp32_peak,
+                   "flops_per_batch": raster_flops, "checked": work["checked"], "blended": work["blended"],
+                   "exp_per_s": work["blended"] / raster_s if raster_s > 0 else 0.0,
+                   "peak_source": f"{sms} SMs x 128 FP32 lanes x 2 x {clock_mhz:.0f} MHz (median sampled SM clock)"}
+    launches_per_batch = nlaunch
     traffic = measured_traffic(dom, args, int(tuning["views_per_launch"]))
-    roofline = {"kernel": dom, "bound": "hbm", "achieved": stages[dom]["GB/s"], "peak": hbm, "unit": "GB/s",
-                "frac": stages[dom]["frac"], "traffic": traffic, "peak_source": peak_kind,
-                "note": "reported against HBM; the projection and raster are instruction-issue bound "
-                        "(73-85% issue active in the ncu captures under profiles/), not bandwidth bound"}
+    traffic_per_launch = traffic / launches_per_batch if traffic else None
+    if dom == "raster":
+        roofline = dict(raster_fp32, traffic=traffic_per_launch,
+                        traffic_unit="DRAM bytes per launch (ncu)",
+                        hbm={"achieved": stages[dom]["GB/s"], "peak": hbm, "unit": "GB/s",
+                             "frac": stages[dom]["frac"], "bytes_per_batch": stages[dom]["bytes"],
+                             "peak_source": peak_kind})
+    else:
+        roofline = {"kernel": dom, "bound": "hbm", "achieved": stages[dom]["GB/s"], "peak": hbm, "unit": "GB/s",
+                    "frac": stages[dom]["frac"], "traffic": traffic_per_launch,
+                    "traffic_unit": "DRAM bytes per launch (ncu)", "peak_source": peak_kind}
 
     # Image quality of camera 0 against the FP64 oracle, and the CPU baseline.
     cpu = None
@@ -702,6 +734,7 @@ def main() -> None:
         "e2e": {"value": e2e_fps, "unit": "frames/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "roofline": roofline,
+        "raster_fp32": raster_fp32,
         "stages": stages,
         "profiled_renders": profiled,
         "clocks": clock_info,
