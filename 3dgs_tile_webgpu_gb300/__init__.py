@@ -267,7 +267,8 @@ class TiledGaussianPipeline:
                 "intersectionCapacity": int(s.intersection_capacity), "overflow": bool(s.overflow),
                 "deviceError": int(s.device_error),
                 "rasterWork": {"checked": int(s.raster_checked), "blended": int(s.raster_blended),
-                               "pixels": int(s.raster_pixels), "alphaStopped": int(s.raster_alpha_stopped)}}
+                               "pixels": int(s.raster_pixels), "alphaStopped": int(s.raster_alpha_stopped)},
+                "outputState": [int(v) for v in s.output_state]}
 
     def read_stats(self) -> dict:
         s = Stats()

@@ -3,7 +3,7 @@ from __future__ import annotations
 
 import ctypes as C
 
-GS3D_ABI_VERSION = 2
+GS3D_ABI_VERSION = 3
 GS3D_OK = 0
 GS3D_ERROR_INVALID_ARGUMENT = 1
 GS3D_ERROR_RANGE = 2
@@ -85,7 +85,7 @@ class Stats(C.Structure):
                 ("requested_intersections", C.c_uint32), ("overflow", C.c_uint32),
                 ("intersection_capacity", C.c_uint64), ("device_error", C.c_uint32), ("reserved", C.c_uint32),
                 ("raster_checked", C.c_uint64), ("raster_blended", C.c_uint64), ("raster_pixels", C.c_uint64),
-                ("raster_alpha_stopped", C.c_uint64)]
+                ("raster_alpha_stopped", C.c_uint64), ("output_state", C.c_uint32 * 4)]
 
 
 class Resources(C.Structure):

@@ -1152,10 +1152,10 @@ namespace {
 // ran as several launch sequences).
 constexpr size_t kCountersOffset = offsetof(Control, visible_state);
 constexpr size_t kCountersBytes = offsetof(Control, order_hist) - offsetof(Control, visible_state);
-constexpr size_t kReadbackBytes = kCountersBytes + sizeof(BatchSummary);
+constexpr size_t kReadbackBytes = kCountersBytes + sizeof(BatchSummary) + 4 * sizeof(uint32_t);
 
 gs3d_status fill_stats(gs3d_pipeline* p, const unsigned char* counters, const BatchSummary* summary, uint32_t chunks,
-                       gs3d_stats* out) {
+                       const uint32_t* output_state, gs3d_stats* out) {
   Control c;
   memcpy((unsigned char*)&c + kCountersOffset, counters, kCountersBytes);
   if (chunks > 1) {
@@ -1179,6 +1179,7 @@ gs3d_status fill_stats(gs3d_pipeline* p, const unsigned char* counters, const Ba
   out->raster_blended = c.raster_stats[1];
   out->raster_pixels = c.raster_stats[2];
   out->raster_alpha_stopped = c.raster_stats[3];
+  for (int i = 0; i < 4; ++i) out->output_state[i] = output_state[i];
   if (c.error) return fail(p, GS3D_ERROR_DEVICE_TIMEOUT, "a device-side look-back wait expired");
   return GS3D_OK;
 }
@@ -1200,7 +1201,10 @@ gs3d_status gs3d_pipeline_read_stats(gs3d_pipeline* p, gs3d_stats* out) {
     e = cudaMemcpy(&b, p->summary, sizeof(b), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_fail(p, e, "reading the batch summary");
   }
-  return fill_stats(p, counters, &b, p->last_chunks, out);
+  uint32_t output_state[4];
+  e = cudaMemcpy(output_state, p->output_state, sizeof(output_state), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(p, e, "reading the output state");
+  return fill_stats(p, counters, &b, p->last_chunks, output_state, out);
 }
 
 gs3d_status gs3d_pipeline_request_stats(gs3d_pipeline* p, void* stream) {
@@ -1228,6 +1232,8 @@ gs3d_status gs3d_pipeline_request_stats(gs3d_pipeline* p, void* stream) {
                            cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
       (p->rb_chunks > 1 && (e = cudaMemcpyAsync(p->rb_pinned + kCountersBytes, p->summary, sizeof(BatchSummary),
                                                 cudaMemcpyDeviceToHost, st)) != cudaSuccess) ||
+      (e = cudaMemcpyAsync(p->rb_pinned + kCountersBytes + sizeof(BatchSummary), p->output_state,
+                           4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
       (e = cudaEventRecord(p->rb_event, st)) != cudaSuccess)
     return cuda_fail(p, e, "enqueueing the stats read-back");
   p->rb_pending = true;
@@ -1242,7 +1248,8 @@ gs3d_status gs3d_pipeline_poll_stats(gs3d_pipeline* p, gs3d_stats* out, int wait
   if (e == cudaErrorNotReady) return GS3D_NOT_READY;
   p->rb_pending = false;
   if (e != cudaSuccess) return cuda_fail(p, e, "waiting for the stats read-back");
-  return fill_stats(p, p->rb_pinned, (const BatchSummary*)(p->rb_pinned + kCountersBytes), p->rb_chunks, out);
+  return fill_stats(p, p->rb_pinned, (const BatchSummary*)(p->rb_pinned + kCountersBytes), p->rb_chunks,
+                    (const uint32_t*)(p->rb_pinned + kCountersBytes + sizeof(BatchSummary)), out);
 }
 
 gs3d_status gs3d_pipeline_set_wait_limit(gs3d_pipeline* p, uint32_t polls) {

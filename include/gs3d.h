@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define GS3D_ABI_VERSION 2u
+#define GS3D_ABI_VERSION 3u
 
 typedef enum gs3d_status {
   GS3D_OK = 0,
@@ -161,6 +161,10 @@ typedef struct gs3d_stats {
   uint64_t raster_blended;
   uint64_t raster_pixels;
   uint64_t raster_alpha_stopped;
+  /* The 16-byte output state after the render (intersections.ts:114-133,
+   * read back by GaussianPass.ts:1019-1079): attempt, version (the attempt
+   * of the last complete image, 0 if none), demand, overflow. */
+  uint32_t output_state[4];
 } gs3d_stats;
 
 /* getResources() (TiledGaussianPipeline.ts:391-406, types.ts:174-193).
