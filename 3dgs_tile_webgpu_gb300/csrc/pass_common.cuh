@@ -92,7 +92,7 @@ struct Control {
   uint32_t tile_hist[kMaxSortPasses][256];   // digit histograms of the tile sort (its count kernels)
   uint32_t visible_state[4];     // visible, visible, radix blocks, 0
   uint32_t state[4];             // count, total, radix blocks, overflow
-  uint32_t error;                // bit 0: look-back wait expired
+  uint32_t error;                // bit 0: look-back wait expired; bit 2: a sort tile copy never landed
   uint32_t pad[3];
   unsigned long long raster_stats[4];  // checked, blended, pixels, alpha-stopped
   uint32_t order_hist[34];       // raster work-list buckets (tile load classes)
@@ -271,9 +271,11 @@ constexpr uint32_t kSortTile = 4096;  // items per sort tile
 // pass's digit histogram. n is read from *n_ptr on the device.
 constexpr uint32_t kChunkBlocksPerSm = 3;
 uint32_t chunk_pass_chunks(uint32_t n_max, int sms);
+// err: the control block's error word (bit 2: a tile copy of the scatter
+// never landed).
 void launch_chunk_pass(int bits, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
                        uint32_t* vals_out, const uint32_t* n_ptr, int shift, uint32_t* hist, uint32_t chunks,
-                       uint32_t* counts, cudaStream_t st);
+                       uint32_t* counts, uint32_t* err, cudaStream_t st);
 // Opt every sort-scatter instantiation into its shared-memory size (once per
 // device; call before any stream capture).
 void prepare_sort_kernels();

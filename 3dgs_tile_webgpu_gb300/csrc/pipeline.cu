@@ -804,7 +804,7 @@ void record_batch(gs3d_pipeline* p, const Plan& pl, unsigned char* dev, cudaStre
   const uint32_t depth_chunks = chunk_pass_chunks(N, p->sms);
   for (int pass = 0; pass < depth_passes; ++pass) {
     launch_chunk_pass(8, p->dk[cur], p->dv[cur], p->dk[cur ^ 1], p->dv[cur ^ 1], &ctl->visible_state[0], 8 * pass,
-                      ctl->depth_hist[pass], depth_chunks, p->chunk_counts, st);
+                      ctl->depth_hist[pass], depth_chunks, p->chunk_counts, &ctl->error, st);
     cur ^= 1;
     launches += 3;
   }
@@ -832,7 +832,7 @@ void record_batch(gs3d_pipeline* p, const Plan& pl, unsigned char* dev, cudaStre
   const uint32_t tile_chunks = chunk_pass_chunks(cap32, p->sms);
   for (int pass = 0; pass < tile_passes; ++pass) {
     launch_chunk_pass(digit_bits, p->tk[tcur], p->tv[tcur], p->tk[tcur ^ 1], p->tv[tcur ^ 1], &ctl->state[0],
-                      digit_bits * pass, ctl->tile_hist[pass], tile_chunks, p->chunk_counts, st);
+                      digit_bits * pass, ctl->tile_hist[pass], tile_chunks, p->chunk_counts, &ctl->error, st);
     tcur ^= 1;
     launches += 3;
   }

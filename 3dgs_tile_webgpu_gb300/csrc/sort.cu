@@ -17,10 +17,12 @@
 //                   digit's global base from that histogram;
 //   k_chunk_scatter one block per chunk walks its tiles in order with running
 //                   per-digit offsets: tile t+1 streams into shared memory by
-//                   cp.async while tile t is ranked per digit within each warp
-//                   by ballot bit-splitting (warp-striped layout: item
-//                   j*32+lane of each warp's 512-item segment, so ranks follow
-//                   index order), staged in place in block-sorted order, and
+//                   two bulk copies (cp.async.bulk, 16 KB of keys and 16 KB
+//                   of values, completion counted on an mbarrier) while tile
+//                   t is ranked per digit within each warp by ballot
+//                   bit-splitting (warp-striped layout: item j*32+lane of
+//                   each warp's 512-item segment, so ranks follow index
+//                   order), staged in place in block-sorted order, and
 //                   written out with each digit's run contiguous.
 // Stable: tiles in index order within a chunk, chunks in index order, ranks in
 // index order within a tile.
@@ -47,11 +49,6 @@ __device__ __forceinline__ uint32_t match_digit(uint32_t d, uint32_t valid_mask)
     peers &= bit ? bal : ~bal;
   }
   return peers;
-}
-
-__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
-  const uint32_t s = (uint32_t)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
 }
 
 // Tiles [t0, t1) of chunk c when n items split over `chunks` chunks.
@@ -139,32 +136,6 @@ __global__ void __launch_bounds__(kBlock) k_chunk_offsets(const uint32_t* __rest
   }
 }
 
-// Issues the cp.async copies of one tile's keys and values into shared
-// memory (the ragged end with plain loads) and commits them as one group.
-__device__ __forceinline__ void load_tile_async(const uint32_t* __restrict__ keys_in,
-                                                const uint32_t* __restrict__ vals_in, uint32_t base, uint32_t n,
-                                                uint32_t* kb, uint32_t* vb) {
-  for (uint32_t c = threadIdx.x; c < kSortTile / 4u; c += kBlock) {
-    const uint32_t first = base + 4u * c;
-    if (first + 4u <= n) {
-      cp_async16(kb + 4u * c, keys_in + first);
-      cp_async16(vb + 4u * c, vals_in + first);
-    } else {
-      for (uint32_t e = 0; e < 4u; ++e)
-        if (first + e < n) {
-          kb[4u * c + e] = keys_in[first + e];
-          vb[4u * c + e] = vals_in[first + e];
-        }
-    }
-  }
-  asm volatile("cp.async.commit_group;" ::: "memory");
-}
-
-template <int N>
-__device__ __forceinline__ void cp_async_wait_group() {
-  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
-}
-
 // Two tile buffers (keys and values each): tile t+1 streams in while tile t
 // is ranked and scattered.
 constexpr size_t kChunkDynSmem = 2 * 2 * kSortTile * sizeof(uint32_t);
@@ -175,7 +146,57 @@ struct ScatterShared {
   uint32_t block_excl[1u << BITS];
   uint32_t run[1u << BITS];  // global position of the next key of each digit
   uint32_t scan[kBlock / 32];
+  unsigned long long bar[2];  // bulk-copy completion of each tile buffer
 };
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Bulk copies of one tile's keys and values (items base .. min(base + 4096,
+// n)) into kb/vb, issued by thread 0 and counted on the buffer's mbarrier;
+// the last n % 4 items of a ragged tile (a bulk copy moves whole 16-byte
+// units) come by plain loads, visible after the next block barrier.
+__device__ __forceinline__ void load_tile_bulk(const uint32_t* __restrict__ keys_in,
+                                               const uint32_t* __restrict__ vals_in, uint32_t base, uint32_t n,
+                                               uint32_t* kb, uint32_t* vb, uint32_t bar) {
+  const uint32_t items = min(kSortTile, n - base);
+  const uint32_t whole = items & ~3u;  // items moved by the bulk copies
+  if (threadIdx.x == 0) {
+    const uint32_t bytes = whole * 4u;
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(2u * bytes) : "memory");
+    if (bytes) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // the buffer's previous reads come first
+      asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                       smem_addr(kb)),
+                   "l"(keys_in + base), "r"(bytes), "r"(bar)
+                   : "memory");
+      asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                       smem_addr(vb)),
+                   "l"(vals_in + base), "r"(bytes), "r"(bar)
+                   : "memory");
+    }
+  }
+  for (uint32_t e = whole + threadIdx.x; e < items; e += kBlock) {
+    kb[e] = keys_in[base + e];
+    vb[e] = vals_in[base + e];
+  }
+}
+
+// Bounded wait for phase `parity` of the mbarrier (about a second of polls).
+__device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity) {
+  uint32_t backoff = 16;
+  for (uint32_t polls = 0; polls < kSpinLimit; ++polls) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    __nanosleep(backoff);
+    backoff = backoff < 256 ? backoff * 2 : 256;
+  }
+  return false;
+}
 
 // Ranks the tile held in kb/vb (items base .. base + 4096, those below n),
 // stages it in place in block-sorted order and writes each digit's run to its
@@ -263,7 +284,7 @@ __global__ void __launch_bounds__(kBlock, kChunkBlocksPerSm)
     k_chunk_scatter(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
                     uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
                     const uint32_t* __restrict__ n_ptr, int shift, uint32_t chunks,
-                    const uint32_t* __restrict__ offsets) {
+                    const uint32_t* __restrict__ offsets, uint32_t* __restrict__ err) {
   constexpr uint32_t RADIX = 1u << BITS;
   __shared__ ScatterShared<BITS> sm;
   extern __shared__ uint4 s_dyn[];
@@ -274,21 +295,31 @@ __global__ void __launch_bounds__(kBlock, kChunkBlocksPerSm)
   uint32_t t0, t1;
   chunk_tiles(n, chunks, blockIdx.x, &t0, &t1);
   if (t0 >= t1) return;
-  load_tile_async(keys_in, vals_in, t0 * kSortTile, n, s_buf, s_buf + kSortTile);
+  if (tid < 2u) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&sm.bar[tid])) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  __syncthreads();
+  uint32_t phases = 0;  // parity of the next phase of each buffer's barrier
+  load_tile_bulk(keys_in, vals_in, t0 * kSortTile, n, s_buf, s_buf + kSortTile, smem_addr(&sm.bar[0]));
   if (tid < RADIX) sm.run[tid] = offsets[(size_t)blockIdx.x * RADIX + tid];
   for (uint32_t i = tid; i < kSortWarps * RADIX; i += kBlock) (&sm.warp_hist[0][0])[i] = 0u;
 
   for (uint32_t t = t0; t < t1; ++t) {
-    uint32_t* kb = s_buf + ((t - t0) & 1u) * 2u * kSortTile;
+    const uint32_t k = (t - t0) & 1u;
+    uint32_t* kb = s_buf + k * 2u * kSortTile;
     uint32_t* vb = kb + kSortTile;
     if (t + 1u < t1) {
-      uint32_t* nb = s_buf + (((t - t0) & 1u) ^ 1u) * 2u * kSortTile;
-      load_tile_async(keys_in, vals_in, (t + 1u) * kSortTile, n, nb, nb + kSortTile);
-      cp_async_wait_group<1>();
-    } else {
-      cp_async_wait_group<0>();
+      uint32_t* nb = s_buf + (k ^ 1u) * 2u * kSortTile;
+      load_tile_bulk(keys_in, vals_in, (t + 1u) * kSortTile, n, nb, nb + kSortTile, smem_addr(&sm.bar[k ^ 1u]));
     }
-    __syncthreads();
+    const bool landed = bar_wait(smem_addr(&sm.bar[k]), (phases >> k) & 1u);
+    phases ^= 1u << k;
+    if (!__syncthreads_and(landed)) {
+      // A copy never landed: flag the frame and leave, after the other
+      // buffer's copy (if one was issued) had its own bounded wait.
+      if (tid == 0) atomicOr(err, 4u);
+      if (t + 1u < t1) bar_wait(smem_addr(&sm.bar[k ^ 1u]), (phases >> (k ^ 1u)) & 1u);
+      return;
+    }
     const uint32_t base = t * kSortTile;
     if ((uint64_t)base + kSortTile <= n)
       scatter_tile<BITS, true>(sm, kb, vb, base, n, shift, keys_out, vals_out);
@@ -300,11 +331,11 @@ __global__ void __launch_bounds__(kBlock, kChunkBlocksPerSm)
 template <int B>
 void launch_chunk_bits(uint32_t chunks, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
                        uint32_t* vals_out, const uint32_t* n_ptr, int shift, uint32_t* hist, uint32_t* counts,
-                       cudaStream_t st) {
+                       uint32_t* err, cudaStream_t st) {
   k_chunk_count<B><<<chunks, kBlock, 0, st>>>(keys_in, n_ptr, shift, chunks, counts, hist);
   k_chunk_offsets<B><<<1u << B, kBlock, 0, st>>>(hist, chunks, counts);
   k_chunk_scatter<B><<<chunks, kBlock, kChunkDynSmem, st>>>(keys_in, vals_in, keys_out, vals_out, n_ptr, shift,
-                                                           chunks, counts);
+                                                           chunks, counts, err);
 }
 
 template <int B>
@@ -324,10 +355,10 @@ uint32_t chunk_pass_chunks(uint32_t n_max, int sms) {
 
 void launch_chunk_pass(int bits, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
                        uint32_t* vals_out, const uint32_t* n_ptr, int shift, uint32_t* hist, uint32_t chunks,
-                       uint32_t* counts, cudaStream_t st) {
+                       uint32_t* counts, uint32_t* err, cudaStream_t st) {
 #define GS_CHUNK(B)                                                                                             \
   case B:                                                                                                       \
-    launch_chunk_bits<B>(chunks, keys_in, vals_in, keys_out, vals_out, n_ptr, shift, hist, counts, st);         \
+    launch_chunk_bits<B>(chunks, keys_in, vals_in, keys_out, vals_out, n_ptr, shift, hist, counts, err, st);    \
     break;
   switch (bits) {
     GS_CHUNK(1)
