@@ -172,6 +172,67 @@ class RenderServer:
             busy += lane.event is not None
         return busy
 
+    def _wait_oldest(self) -> None:
+        """Block until the batch dispatched first among the busy lanes is done
+        (instead of spinning on event queries while nothing can be
+        dispatched)."""
+        busy = [l for l in self.lanes if l.event is not None]
+        if busy:
+            min(busy, key=lambda l: min(r.dispatched for r in l.batch) if l.batch else 0.0).event.synchronize()
+
+    def run_closed(self, make_request, concurrency: int, total: int, warmup: int = 0) -> dict:
+        """Closed loop: keep `concurrency` requests outstanding (each completed
+        request is replaced at once by a new one from make_request(i)) until
+        `total` have completed after `warmup` unrecorded ones. By Little's law
+        the mean latency is concurrency / throughput."""
+        self.completed = []
+        self.batches = self.retries = 0
+        issued = 0
+        done = 0
+
+        def submit_one():
+            nonlocal issued
+            r = make_request(issued)
+            r.arrival = time.perf_counter()
+            self.submit(r)
+            issued += 1
+
+        for _ in range(concurrency):
+            submit_one()
+        t0 = None
+        recorded = []
+        while done < warmup + total:
+            now = time.perf_counter()
+            before = len(self.completed)
+            self.poll(now)
+            finished = self.completed[before:]
+            for r in finished:
+                done += 1
+                if done == warmup:
+                    t0 = time.perf_counter()
+                if done > warmup:
+                    recorded.append(r)
+                if issued < warmup + total:
+                    submit_one()
+            if not finished:
+                # poll() has dispatched whatever a free lane could take, so
+                # nothing can start before a batch completes: wait for one.
+                self._wait_oldest()
+        t1 = time.perf_counter()
+        t0 = t0 if t0 is not None else t1
+        lat = sorted(r.latency_ms for r in recorded)
+        while any(l.event is not None for l in self.lanes):
+            self.poll(time.perf_counter())
+        fps = len(recorded) / (t1 - t0) if t1 > t0 else 0.0
+        return {
+            "concurrency": concurrency, "requests": len(recorded), "seconds": t1 - t0, "frames_per_s": fps,
+            "p50_ms": lat[len(lat) // 2] if lat else None,
+            "p99_ms": lat[min(len(lat) - 1, int(0.99 * len(lat)))] if lat else None,
+            "max_ms": lat[-1] if lat else None, "mean_ms": sum(lat) / len(lat) if lat else None,
+            "little_bound_ms": 1000.0 * concurrency / fps if fps else None,
+            "batches": self.batches, "retries": self.retries,
+        }
+
     def run(self, requests: list, realtime: bool = True) -> dict:
         """Feed requests at their arrival times (seconds from start) and run
         until all complete. Returns latency and throughput statistics."""
