@@ -74,23 +74,28 @@ def peaks():
         return 6800.0, "fallback"
 
 
-TRAFFIC_FILE = os.path.join(ROOT, "profiles", "dram_traffic_config2_3M_1080p.md")
+PROFILES = os.path.join(ROOT, "profiles")
 
 
-def measured_traffic(stage: str, args, views_per_launch: int) -> int | None:
-    """DRAM bytes (read + write) of `stage`'s kernel per batch of the step,
-    from the committed ncu summary, when that capture was taken on this
-    workload and launch shape."""
+def measured_traffic_per_view(stage: str, args) -> int | None:
+    """DRAM bytes (read + write) per view of `stage`'s kernel, from a
+    committed ncu summary taken on a smaller batch of this scene and
+    resolution (the traffic grows in proportion to the views)."""
     try:
-        with open(TRAFFIC_FILE) as f:
+        names = sorted(f for f in os.listdir(PROFILES) if f.endswith(".md"))
+    except OSError:
+        return None
+    for name in names:
+        with open(os.path.join(PROFILES, name)) as f:
             for line in f:
                 parts = line.split()
-                if len(parts) == 9 and parts[0] == "traffic" and parts[1] == stage:
-                    cfg = (int(parts[2]), int(parts[3]), int(parts[4]), int(parts[5]), parts[6], int(parts[7]))
-                    if cfg == (args.splats, args.width, args.height, args.cameras, args.precision, views_per_launch):
-                        return int(parts[8])
-    except (OSError, ValueError):
-        pass
+                if len(parts) == 7 and parts[0] == "traffic_per_view" and parts[1] == stage:
+                    try:
+                        cfg = (int(parts[2]), int(parts[3]), int(parts[4]), parts[5])
+                        if cfg == (args.splats, args.width, args.height, args.precision):
+                            return int(parts[6])
+                    except ValueError:
+                        continue
     return None
 
 
@@ -694,12 +699,12 @@ def main() -> None:
                    "flops_per_batch": raster_flops, "checked": work["checked"], "blended": work["blended"],
                    "exp_per_s": work["blended"] / raster_s if raster_s > 0 else 0.0,
                    "peak_source": f"{sms} SMs x 128 FP32 lanes x 2 x {clock_mhz:.0f} MHz (median sampled SM clock)"}
-    launches_per_batch = nlaunch
-    traffic = measured_traffic(dom, args, int(tuning["views_per_launch"]))
-    traffic_per_launch = traffic / launches_per_batch if traffic else None
+    per_view = measured_traffic_per_view(dom, args)
+    traffic_per_launch = per_view * min(vpl, ncam) if per_view else None
     if dom == "raster":
         roofline = dict(raster_fp32, traffic=traffic_per_launch,
-                        traffic_unit="DRAM bytes per launch (ncu)",
+                        algorithmic_bytes_per_launch=stages[dom]["bytes"] / nlaunch,
+                        traffic_unit="DRAM bytes per launch (ncu, scaled from a 4-view capture)",
                         hbm={"achieved": stages[dom]["GB/s"], "peak": hbm, "unit": "GB/s",
                              "frac": stages[dom]["frac"], "bytes_per_batch": stages[dom]["bytes"],
                              "peak_source": peak_kind})
