@@ -209,9 +209,11 @@ class TiledGaussianPipeline:
         return arr, keep
 
     def set_tuning(self, tuning: dict) -> None:
-        """Launch shape (outputs do not depend on it): ``views_per_launch``
-        (0 = a whole batch at once), ``tile_digit_bits`` (4..8),
-        ``work_order`` (1 = heaviest tiles first)."""
+        """Launch shape: ``views_per_launch`` (0 = a whole batch at once),
+        ``tile_digit_bits`` (4..8), ``work_order`` (1 = heaviest tiles first)
+        change nothing the batch produces; ``tile_size`` (8, 16 or 32; 0 =
+        16) sets the tiles of batched renders, which leaves the EXACT image
+        unchanged but not the per-tile buffers."""
         t = Tuning()
         self._lib.gs3d_pipeline_get_tuning(self._p, C.byref(t))
         for k, v in tuning.items():
@@ -222,7 +224,7 @@ class TiledGaussianPipeline:
         t = Tuning()
         _raise(self._lib, self._lib.gs3d_pipeline_get_tuning(self._p, C.byref(t)), self._p)
         return {"views_per_launch": t.views_per_launch, "tile_digit_bits": t.tile_digit_bits,
-                "work_order": t.work_order}
+                "work_order": t.work_order, "tile_size": t.tile_size or 16}
 
     def autotune(self, views: list, trials: int = 3, stream: int = 0) -> tuple[dict, float]:
         """Time candidate tunings on this batch (same tuple layout as

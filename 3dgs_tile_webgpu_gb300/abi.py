@@ -55,7 +55,7 @@ class View(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("views_per_launch", C.c_uint32), ("tile_digit_bits", C.c_uint32), ("work_order", C.c_uint32),
-                ("reserved", C.c_uint32)]
+                ("tile_size", C.c_uint32)]
 
 
 class SplatSource(C.Structure):

@@ -9,7 +9,7 @@
 namespace gs {
 
 constexpr int kBlock = 256;  // threads per block for the linear kernels
-constexpr uint32_t kTileSize = 16;  // pixels per tile side (src/renderer/pipeline/constants.ts:1)
+constexpr uint32_t kTileSize = 16;  // the reference's pixels per tile side (src/renderer/pipeline/constants.ts:1)
 
 // One view of a batch: a scene (packed GaussianData buffers), a camera
 // (FrameUniforms.ts:18-58 + the object table), a viewport and its targets.
@@ -48,6 +48,9 @@ struct PassOptions {
   float invalid_depth;
   uint32_t proj_fp64;      // 1: FP64 far-origin mean transform and near-singular conic
   uint32_t any_depth;      // some view of the launch has a depth target
+  uint32_t tile;           // pixels per tile side: 16 (the reference's), or 8 / 32 in tuned batches
+  float tile_px;           // the same as a float
+  float tile_inv;          // its reciprocal (exact: a power of two)
 };
 
 // The batch table in device memory: the per-frame parameters (attempt,

@@ -67,7 +67,7 @@ struct CountShared {
 // per round) instead of each lane walking its own box. Must be called by all
 // 32 lanes; a lane with nbox == 0 contributes nothing. Returns the lane's count.
 __device__ __forceinline__ uint32_t count_tiles_warp(CountShared& sm, uint32_t nbox, float vw, float vh,
-                                                     uint32_t axis) {
+                                                     uint32_t axis, float ts) {
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   uint32_t incl = nbox;
 #pragma unroll
@@ -94,7 +94,7 @@ __device__ __forceinline__ uint32_t count_tiles_warp(CountShared& sm, uint32_t n
       hit = boundary_tile_hit(sm.f[0][warp][owner], sm.f[1][warp][owner], sm.f[2][warp][owner],
                               sm.f[3][warp][owner], sm.f[4][warp][owner], sm.f[5][warp][owner],
                               sm.f[6][warp][owner], sm.f[7][warp][owner], (int)(sm.u[0][warp][owner] + bx),
-                              (int)(sm.u[1][warp][owner] + by), vw, vh, axis);
+                              (int)(sm.u[1][warp][owner] + by), vw, vh, axis, ts);
     }
     const uint32_t hits = __ballot_sync(0xffffffffu, hit);
     const uint32_t same = __match_any_sync(0xffffffffu, valid ? owner : 32u + lane);
@@ -229,8 +229,10 @@ __global__ void __launch_bounds__(kBlock, 4) k_project(BatchView b, PassOptions 
       }
       const int tiles_x = (int)v.tiles_x, tiles_y = (int)v.tiles_y;
       const float mtx = (float)(tiles_x - 1), mty = (float)(tiles_y - 1);
-      const float fx0 = floorf(bminx / 16.0f), fy0 = floorf(bminy / 16.0f);
-      const float fx1 = floorf(bmaxx / 16.0f), fy1 = floorf(bmaxy / 16.0f);
+      // Division by the tile side, a power of two: the product with its
+      // reciprocal is the same correctly rounded value.
+      const float fx0 = floorf(bminx * o.tile_inv), fy0 = floorf(bminy * o.tile_inv);
+      const float fx1 = floorf(bmaxx * o.tile_inv), fy1 = floorf(bmaxy * o.tile_inv);
       int tminx = (int)clampf(fx0, 0.0f, mtx);
       int tminy = (int)clampf(fy0, 0.0f, mty);
       int tmaxx = (int)clampf(fx1, 0.0f, mtx);
@@ -253,7 +255,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_project(BatchView b, PassOptions 
       s_count.u[2][warp][lane] = bw;
     } while (false);
     // Tiles passing the tile test (projectionHelpers.ts:223-236), counted by the whole warp.
-    cnt = count_tiles_warp(s_count, single ? 0u : nbox, vw, vh, o.axis);
+    cnt = count_tiles_warp(s_count, single ? 0u : nbox, vw, vh, o.axis, o.tile_px);
     if (single) cnt = 1u;
     if (cnt > 0) {
       uint32_t co[16];
@@ -611,10 +613,10 @@ __device__ __forceinline__ void emit_group(EmitShared& sm, bool live, uint32_t g
     const float thr = e1.y;  // log(opacity * 255), computed by the projection
     const int tiles_x = (int)v.tiles_x, tiles_y = (int)v.tiles_y;
     const float mtx = (float)(tiles_x - 1), mty = (float)(tiles_y - 1);
-    int tminx = (int)clampf(floorf((m.x - rx) / 16.0f), 0.0f, mtx);
-    int tminy = (int)clampf(floorf((m.y - ry) / 16.0f), 0.0f, mty);
-    int tmaxx = (int)clampf(floorf((m.x + rx) / 16.0f), 0.0f, mtx);
-    int tmaxy = (int)clampf(floorf((m.y + ry) / 16.0f), 0.0f, mty);
+    int tminx = (int)clampf(floorf((m.x - rx) * o.tile_inv), 0.0f, mtx);
+    int tminy = (int)clampf(floorf((m.y - ry) * o.tile_inv), 0.0f, mty);
+    int tmaxx = (int)clampf(floorf((m.x + rx) * o.tile_inv), 0.0f, mtx);
+    int tmaxy = (int)clampf(floorf((m.y + ry) * o.tile_inv), 0.0f, mty);
     if (o.axis == 1u) { tminx = 0; tmaxx = tiles_x - 1; }
     if (o.axis == 2u) { tminy = 0; tmaxy = tiles_y - 1; }
     const uint32_t bw = (uint32_t)(tmaxx - tminx + 1);
@@ -677,7 +679,7 @@ __device__ __forceinline__ void emit_group(EmitShared& sm, bool live, uint32_t g
               boundary_tile_hit(sm.f[0][warp][owner], sm.f[1][warp][owner], sm.f[2][warp][owner],
                                 sm.f[3][warp][owner], sm.f[4][warp][owner], sm.f[5][warp][owner],
                                 sm.f[6][warp][owner], sm.f[7][warp][owner], tx, ty, sm.f[8][warp][owner],
-                                sm.f[9][warp][owner], o.axis);
+                                sm.f[9][warp][owner], o.axis, o.tile_px);
         t = sm.u[4][warp][owner] + (uint32_t)ty * sm.u[3][warp][owner] + (uint32_t)tx;
       }
       const uint32_t hits = __ballot_sync(0xffffffffu, hit);

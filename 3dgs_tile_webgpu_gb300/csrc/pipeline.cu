@@ -136,9 +136,10 @@ struct gs3d_pipeline {
   std::vector<gs3d_camera> graph_cameras;
   uint32_t graph_launches = 0;
   uint32_t graph_next = 0;
+  uint32_t graph_tile = kTileSize;
   // Tuning (gs3d_pipeline_set_tuning / autotune) and the device summary of a
   // batch rendered as several launch sequences.
-  gs3d_tuning tuning{0u, 8u, 1u, 0u};
+  gs3d_tuning tuning{0u, 8u, 1u, 0u};  // tile_size 0: the reference's 16
   BatchSummary* summary = nullptr;
   uint32_t last_chunks = 1;
   BatchView last_bv{};  // batch table of the last launch sequence (device pointers)
@@ -214,7 +215,11 @@ cudaError_t dalloc(T*& ptr, size_t count) {
   return device_malloc((void**)&ptr, count * sizeof(T));
 }
 
-uint32_t tiles_for(uint32_t px) { return (px + 15u) / 16u; }
+// Tiles covering `px` pixels with tiles of `tile` pixels per side.
+uint32_t tiles_for(uint32_t px, uint32_t tile = kTileSize) { return (px + tile - 1u) / tile; }
+
+// Pixels per tile side of a batched render: the tuning's, or the reference's 16.
+uint32_t batch_tile(const gs3d_pipeline* p) { return p->tuning.tile_size ? p->tuning.tile_size : kTileSize; }
 
 uint32_t ceil_log2(uint64_t v) {
   uint32_t b = 0;
@@ -577,6 +582,7 @@ size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
 
 struct Plan {
   uint32_t n = 0, ngroups = 0;
+  uint32_t tile = kTileSize;  // pixels per tile side
   bool any_depth = false;
   uint32_t items = 0, tiles = 0, blocks = 0;
   size_t objects = 0;
@@ -606,7 +612,7 @@ bool same_scene(const gs3d_view& a, const gs3d_view& b) {
 
 // Validate a batch, grow every workspace it needs and lay out its batch
 // table. Not capturable (it may allocate).
-gs3d_status plan_batch(gs3d_pipeline* p, const gs3d_view* views, uint32_t n, Plan* out) {
+gs3d_status plan_batch(gs3d_pipeline* p, const gs3d_view* views, uint32_t n, Plan* out, uint32_t tile) {
   if (n == 0 || n > kMaxViews) return fail(p, GS3D_ERROR_RANGE, "a batch holds 1 to 4096 views");
   uint64_t items = 0, tiles = 0, blocks = 0;
   uint32_t ngroups = 0;
@@ -624,7 +630,7 @@ gs3d_status plan_batch(gs3d_pipeline* p, const gs3d_view* views, uint32_t n, Pla
       return fail(p, GS3D_ERROR_RANGE, "depth range must satisfy 0 <= near < far");
     if (v.width == 0 || v.height == 0) return fail(p, GS3D_ERROR_RANGE, "render size must be positive");
     any_depth = any_depth || v.targets.depth != nullptr;
-    const uint32_t tx = tiles_for(v.width), ty = tiles_for(v.height);
+    const uint32_t tx = tiles_for(v.width, tile), ty = tiles_for(v.height, tile);
     // TiledGaussianPipeline.ts:294-296
     if (tx > 65535u || ty > 65535u) return fail(p, GS3D_ERROR_RANGE, "Render size exceeds WebGPU's tile dispatch limit");
     const uint64_t b = ((uint64_t)v.data->active_count + kBlock - 1) / kBlock;
@@ -647,6 +653,7 @@ gs3d_status plan_batch(gs3d_pipeline* p, const gs3d_view* views, uint32_t n, Pla
   if ((s = ensure_status(p)) != GS3D_OK) return s;
   if ((s = ensure_tiles(p, tiles)) != GS3D_OK) return s;
   out->n = n;
+  out->tile = tile;
   out->ngroups = ngroups;
   out->any_depth = any_depth;
   out->items = (uint32_t)items;
@@ -696,8 +703,8 @@ void stage_batch(gs3d_pipeline* p, const gs3d_view* views, const Plan& pl, uint3
     w.C = (d.sh_degree + 1) * (d.sh_degree + 1);
     w.object_count = v.camera->object_count;
     w.color_half = v.targets.color_format == GS3D_COLOR_RGBA16F ? 1u : 0u;
-    w.tiles_x = tiles_for(v.width);
-    w.tiles_y = tiles_for(v.height);
+    w.tiles_x = tiles_for(v.width, pl.tile);
+    w.tiles_y = tiles_for(v.height, pl.tile);
     w.item_base = item;
     w.tile_base = tile;
     memcpy(w.P, v.camera->projection, sizeof(w.P));
@@ -764,6 +771,9 @@ void record_batch(gs3d_pipeline* p, const Plan& pl, unsigned char* dev, cudaStre
   o.depth_encoding = p->desc.depth_encoding;
   o.proj_fp64 = p->desc.projection_precision == GS3D_PROJECTION_FP64 ? 1u : 0u;
   o.any_depth = pl.any_depth ? 1u : 0u;
+  o.tile = pl.tile;
+  o.tile_px = (float)pl.tile;
+  o.tile_inv = 1.0f / (float)pl.tile;
   memcpy(o.background, p->desc.background, sizeof(o.background));
   o.t_threshold = p->desc.raster_transmittance_threshold;
   o.depth_alpha_threshold = p->desc.depth_alpha_threshold;
@@ -860,9 +870,9 @@ void record_batch(gs3d_pipeline* p, const Plan& pl, unsigned char* dev, cudaStre
 // The whole pass of TiledGaussianPipeline.render (TiledGaussianPipeline.ts:324-341)
 // for every view of a batch in one launch sequence.
 gs3d_status enqueue(gs3d_pipeline* p, const gs3d_view* views, uint32_t n, uint32_t attempt, int reset_valid,
-                    cudaStream_t st, const uint32_t** frame_params = nullptr) {
+                    cudaStream_t st, uint32_t tile, const uint32_t** frame_params = nullptr) {
   Plan pl;
-  gs3d_status s = plan_batch(p, views, n, &pl);
+  gs3d_status s = plan_batch(p, views, n, &pl, tile);
   if (s != GS3D_OK) return s;
   if ((s = ensure_stage(p, pl.stage_bytes)) != GS3D_OK) return s;
   const uint32_t slot = p->frame_index++ % kObjectRing;
@@ -893,13 +903,13 @@ gs3d_status enqueue_batch(gs3d_pipeline* p, const gs3d_view* views, uint32_t n, 
   const uint32_t per = views_per_launch(p, n);
   if (per >= n) {
     p->last_chunks = 1;
-    return enqueue(p, views, n, attempt, reset_valid, st);
+    return enqueue(p, views, n, attempt, reset_valid, st, batch_tile(p));
   }
   // Grow every workspace for the largest launch first, so no launch
   // sequence is queued on buffers that a later one reallocates.
   for (uint32_t k = 0; k < n; k += per) {
     Plan pl;
-    gs3d_status s = plan_batch(p, views + k, std::min(per, n - k), &pl);
+    gs3d_status s = plan_batch(p, views + k, std::min(per, n - k), &pl, batch_tile(p));
     if (s != GS3D_OK) return s;
     if ((s = ensure_stage(p, pl.stage_bytes)) != GS3D_OK) return s;
   }
@@ -908,7 +918,7 @@ gs3d_status enqueue_batch(gs3d_pipeline* p, const gs3d_view* views, uint32_t n, 
   for (uint32_t k = 0; k < n; k += per) {
     const uint32_t m = std::min(per, n - k);
     const uint32_t* params = nullptr;
-    gs3d_status s = enqueue(p, views + k, m, attempt, reset_valid, st, &params);
+    gs3d_status s = enqueue(p, views + k, m, attempt, reset_valid, st, batch_tile(p), &params);
     if (s != GS3D_OK) return s;
     launches += p->last_launches + 1;
     k_summary_add<<<1, 1, 0, st>>>(p->summary, p->ctl, params, p->output_state, k + m >= n ? 1 : 0);
@@ -938,7 +948,9 @@ gs3d_status gs3d_pipeline_render(gs3d_pipeline* p, const gs3d_camera* cam, uint3
   v.height = p->height;
   v.targets = *targets;
   p->last_chunks = 1;
-  return enqueue(p, &v, 1, attempt, reset_valid, (cudaStream_t)stream);
+  // A single-view render keeps the reference's 16-pixel tiles, so every
+  // buffer getResources() exposes is the reference's.
+  return enqueue(p, &v, 1, attempt, reset_valid, (cudaStream_t)stream, kTileSize);
 }
 
 gs3d_status gs3d_pipeline_render_batch(gs3d_pipeline* p, const gs3d_view* views, uint32_t count, uint32_t attempt,
@@ -965,7 +977,7 @@ gs3d_status gs3d_pipeline_capture_graph(gs3d_pipeline* p, const gs3d_view* views
   size_t total = 0;
   for (uint32_t k = 0; k < count; k += per) {
     Plan pl;
-    gs3d_status s = plan_batch(p, views + k, std::min(per, count - k), &pl);
+    gs3d_status s = plan_batch(p, views + k, std::min(per, count - k), &pl, batch_tile(p));
     if (s != GS3D_OK) return s;
     plans.push_back(pl);
     p->graph_chunks.push_back({k, pl.n, total});
@@ -1005,6 +1017,7 @@ gs3d_status gs3d_pipeline_capture_graph(gs3d_pipeline* p, const gs3d_view* views
     }
   }
   p->graph_stage_bytes = total;
+  p->graph_tile = batch_tile(p);
   p->prepared = true;
   p->graph_views.assign(views, views + count);
   p->graph_cameras.resize(count);
@@ -1031,6 +1044,7 @@ gs3d_status gs3d_pipeline_launch_graph(gs3d_pipeline* p, const gs3d_camera* came
   for (const auto& ch : p->graph_chunks) {
     Plan pl;
     pl.n = ch.count;
+    pl.tile = p->graph_tile;
     size_t objects = 0;
     for (uint32_t i = 0; i < ch.count; ++i) objects += cameras[ch.first + i].object_count;
     layout_plan(&pl, ch.count, objects);
@@ -1054,10 +1068,11 @@ gs3d_status gs3d_pipeline_set_tuning(gs3d_pipeline* p, const gs3d_tuning* t) {
   if (t->tile_digit_bits < 4 || t->tile_digit_bits > 8)
     return fail(p, GS3D_ERROR_RANGE, "tile_digit_bits must be in [4, 8]");
   if (t->work_order > 1) return fail(p, GS3D_ERROR_INVALID_ARGUMENT, "work_order must be 0 or 1");
+  if (t->tile_size != 0 && t->tile_size != 8 && t->tile_size != 16 && t->tile_size != 32)
+    return fail(p, GS3D_ERROR_RANGE, "tile_size must be 8, 16 or 32 (0: 16)");
   if (p->last_stream) cudaStreamSynchronize(p->last_stream);
   release_graphs(p);  // captured graphs follow the tuning they were captured with
   p->tuning = *t;
-  p->tuning.reserved = 0;
   return GS3D_OK;
 }
 
@@ -1079,14 +1094,20 @@ gs3d_status gs3d_pipeline_autotune(gs3d_pipeline* p, const gs3d_view* views, uin
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   // Milliseconds per batch with tuning t (one untimed render first, which
-  // also grows the workspaces); an overflowing batch is an error.
+  // also grows the workspaces); an overflowing batch is an error, except for
+  // a tile-size candidate (smaller tiles make more intersections), which is
+  // then skipped (*ms stays infinite).
   auto measure = [&](const gs3d_tuning& t, double* ms) -> gs3d_status {
     p->tuning = t;
+    *ms = HUGE_VAL;
     gs3d_status s = enqueue_batch(p, views, count, 1, 0, st);
     if (s != GS3D_OK) return s;
     gs3d_stats stats;
     if ((s = gs3d_pipeline_read_stats(p, &stats)) != GS3D_OK) return s;
-    if (stats.overflow) return fail(p, GS3D_ERROR_RANGE, "intersection capacity too small for the batch");
+    if (stats.overflow) {
+      if (t.tile_size != 0 && t.tile_size != kTileSize) return GS3D_OK;
+      return fail(p, GS3D_ERROR_RANGE, "intersection capacity too small for the batch");
+    }
     cudaEventRecord(e0, st);
     for (uint32_t i = 0; i < trials; ++i)
       if ((s = enqueue_batch(p, views, count, 1, 0, st)) != GS3D_OK) return s;
@@ -1100,8 +1121,16 @@ gs3d_status gs3d_pipeline_autotune(gs3d_pipeline* p, const gs3d_view* views, uin
   gs3d_tuning cur{0u, 8u, 1u, 0u};
   double cur_ms = 0.0;
   gs3d_status s = measure(cur, &cur_ms);
-  // Coordinate descent: views per launch (halving), widest tile-sort digit,
-  // then the raster work order.
+  // Coordinate descent: tile size (8 and 32 against the reference's 16; the
+  // raster block follows the tile, one warp per 8x8 patch), views per launch
+  // (halving), widest tile-sort digit, then the raster work order.
+  for (uint32_t ts : {8u, 32u}) {
+    if (s != GS3D_OK) break;
+    gs3d_tuning t = cur;
+    t.tile_size = ts;
+    double ms = 0.0;
+    if ((s = measure(t, &ms)) == GS3D_OK && ms < cur_ms) { cur = t; cur_ms = ms; }
+  }
   for (uint32_t v = count / 2; s == GS3D_OK && v >= 1; v /= 2) {
     gs3d_tuning t = cur;
     t.views_per_launch = v;

@@ -3,12 +3,14 @@
 // boundary, background and depth semantics as raster_impl.cuh): FP32 and
 // packed half2, one kernel template (HALF) over the same pixel-pair layout.
 //
-// 128 threads per 16x16 tile; each thread owns two pixels of one column,
-// (x, y) and (x, y + 4), so warp w owns the 8x8 patch at (8 (w & 1), 8 (w >> 1)).
-// The two pixels share dx and the x-only terms of the quadratic, the record
-// loads, the culling test and the loop.
+// One warp per 8x8 patch of the tile: 128 threads per 16x16 tile (32 per 8x8,
+// 512 per 32x32 tile in batches tuned to those tile sizes); each thread owns
+// two pixels of one column, (x, y) and (x, y + 4), so warp w owns the 8x8
+// patch at (8 (w mod P), 8 (w div P)), P = tile / 8. The two pixels share dx
+// and the x-only terms of the quadratic, the record loads, the culling test
+// and the loop.
 //
-// The four warps of a tile work independently (no block barrier while
+// The warps of a tile work independently (no block barrier while
 // blending): each warp walks the tile's sorted records 32 at a time, every
 // lane gathers one packed 32-byte record (pass_common.cuh), tests whether the
 // splat's support can reach the warp's 8x8 patch (the exact minimum of the
@@ -38,8 +40,6 @@
 
 namespace gs {
 
-constexpr int kHalfThreads = 128;
-constexpr int kHalfWarps = kHalfThreads / 32;
 
 __device__ __forceinline__ __half2 h2ex2_approx(__half2 x) {
   uint32_t in = *reinterpret_cast<uint32_t*>(&x), out;
@@ -231,8 +231,22 @@ __device__ __forceinline__ void store_pixel(const ViewDesc& v, const PassOptions
   if (v.depth) v.depth[off] = finalize_depth(a.d, a.t, o, v.vnear, v.vfar);
 }
 
-template <bool HALF, bool PERIODIC, bool STATS, bool DEPTH>
-__global__ void __launch_bounds__(kHalfThreads, HALF ? 9 : 8) k_raster_h2(const uint32_t* __restrict__ tile_offsets,
+// Threads of the block for a TILE x TILE tile: one warp per 8x8 patch.
+template <int TILE>
+constexpr int h2_threads() {
+  return 32 * (TILE / 8) * (TILE / 8);
+}
+// Resident blocks per SM the register budget is set for: 9 blocks of 128
+// threads (half2) / 8 (FP32) at the reference's 16-pixel tiles, the same
+// threads per SM at other tile sizes (at most 32 blocks).
+template <bool HALF, int TILE>
+constexpr int h2_min_blocks() {
+  return (HALF ? 1152 : 1024) / h2_threads<TILE>() > 32 ? 32 : (HALF ? 1152 : 1024) / h2_threads<TILE>();
+}
+
+template <bool HALF, bool PERIODIC, bool STATS, bool DEPTH, int TILE>
+__global__ void __launch_bounds__(h2_threads<TILE>(), h2_min_blocks<HALF, TILE>())
+    k_raster_h2(const uint32_t* __restrict__ tile_offsets,
                                                            const uint32_t* __restrict__ order,
                                                            const uint32_t* __restrict__ ids,
                                                            const float4* __restrict__ mean,
@@ -240,7 +254,8 @@ __global__ void __launch_bounds__(kHalfThreads, HALF ? 9 : 8) k_raster_h2(const 
                                                            const float4* __restrict__ rec, BatchView bv,
                                                            PassOptions o, Control* __restrict__ ctl) {
   if (ctl->state[3] != 0u) return;  // overflow: nothing is published
-  __shared__ WarpStage s_stage[kHalfWarps];
+  constexpr uint32_t PW = TILE / 8;  // patches per tile row
+  __shared__ WarpStage s_stage[PW * PW];
   __shared__ uint32_t s_view;
   __shared__ unsigned long long s_stats[4];
   const uint32_t tile = order ? order[blockIdx.x] : blockIdx.x;
@@ -253,7 +268,7 @@ __global__ void __launch_bounds__(kHalfThreads, HALF ? 9 : 8) k_raster_h2(const 
   const uint32_t tx = local % v.tiles_x, ty = local / v.tiles_x;
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
   WarpStage& ws = s_stage[warp];
-  const uint32_t patch_x = tx * kTileSize + 8u * (warp & 1u), patch_y = ty * kTileSize + 8u * (warp >> 1);
+  const uint32_t patch_x = tx * TILE + 8u * (warp % PW), patch_y = ty * TILE + 8u * (warp / PW);
   const uint32_t px = patch_x + morton_compact(lane);
   const uint32_t py0 = patch_y + morton_compact(lane >> 1);
   const uint32_t py1 = py0 + 4u;
@@ -318,13 +333,13 @@ __global__ void __launch_bounds__(kHalfThreads, HALF ? 9 : 8) k_raster_h2(const 
 
 // half = true: packed half2 form; false: FP32 form. o.any_depth: some view
 // of the launch has a depth target.
-template <bool HALF, bool PERIODIC>
-inline void launch_raster_pairs_t(const uint32_t* tile_offsets, const uint32_t* order, const uint32_t* ids,
-                                  const float4* mean, const float4* color, const float4* rec, const BatchView& b,
-                                  const PassOptions& o, Control* ctl, bool stats, cudaStream_t st) {
-#define GS_RASTER_H2(S, D)                                                                                       \
-  k_raster_h2<HALF, PERIODIC, S, D><<<b.total_tiles, kHalfThreads, 0, st>>>(tile_offsets, order, ids, mean, color, \
-                                                                           rec, b, o, ctl)
+template <bool HALF, bool PERIODIC, int TILE>
+inline void launch_raster_pairs_tile(const uint32_t* tile_offsets, const uint32_t* order, const uint32_t* ids,
+                                     const float4* mean, const float4* color, const float4* rec, const BatchView& b,
+                                     const PassOptions& o, Control* ctl, bool stats, cudaStream_t st) {
+#define GS_RASTER_H2(S, D)                                                                          \
+  k_raster_h2<HALF, PERIODIC, S, D, TILE><<<b.total_tiles, h2_threads<TILE>(), 0, st>>>(            \
+      tile_offsets, order, ids, mean, color, rec, b, o, ctl)
   const bool depth = o.any_depth != 0u;
   if (stats) {
     if (depth) GS_RASTER_H2(true, true); else GS_RASTER_H2(true, false);
@@ -332,6 +347,18 @@ inline void launch_raster_pairs_t(const uint32_t* tile_offsets, const uint32_t* 
     if (depth) GS_RASTER_H2(false, true); else GS_RASTER_H2(false, false);
   }
 #undef GS_RASTER_H2
+}
+
+template <bool HALF, bool PERIODIC>
+inline void launch_raster_pairs_t(const uint32_t* tile_offsets, const uint32_t* order, const uint32_t* ids,
+                                  const float4* mean, const float4* color, const float4* rec, const BatchView& b,
+                                  const PassOptions& o, Control* ctl, bool stats, cudaStream_t st) {
+  if (o.tile == 8u)
+    launch_raster_pairs_tile<HALF, PERIODIC, 8>(tile_offsets, order, ids, mean, color, rec, b, o, ctl, stats, st);
+  else if (o.tile == 32u)
+    launch_raster_pairs_tile<HALF, PERIODIC, 32>(tile_offsets, order, ids, mean, color, rec, b, o, ctl, stats, st);
+  else
+    launch_raster_pairs_tile<HALF, PERIODIC, 16>(tile_offsets, order, ids, mean, color, rec, b, o, ctl, stats, st);
 }
 
 inline void launch_raster_pairs(bool half, const uint32_t* tile_offsets, const uint32_t* order, const uint32_t* ids,

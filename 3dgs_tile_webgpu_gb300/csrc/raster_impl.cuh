@@ -99,39 +99,47 @@ struct PixelAcc {
   float r, g, b, t, d;
 };
 
-// Shared batch of the exact form: geo = (cx, cy, opacity, threshold),
-// con = (a, b, c, depth), colour, and the 8-bit warp-patch masks.
+// Shared batch of the exact form (NB records: one per thread of the tile's
+// block, at most 256): geo = (cx, cy, opacity, threshold), con = (a, b, c,
+// depth), colour, and the warp-patch masks (bit w: warp w's 8x4 patch can be
+// reached).
+template <int NT>
 struct Batch {
-  float4 geo[kBlock];
-  float4 con[kBlock];
-  float4 col[kBlock];
-  uint8_t mask[kBlock];
+  static constexpr int NB = NT < 256 ? NT : 256;
+  float4 geo[NB];
+  float4 con[NB];
+  float4 col[NB];
+  uint32_t mask[NB];
 };
 
 constexpr float kLog2MinAlpha = -7.99435329f;  // log2(1/255)
 constexpr float kLog2MaxAlpha = -0.01449957f;  // log2(0.99)
 
-// Which of the tile's eight 8x4 warp patches can hold a pixel centre inside
-// the splat's support {q(d) <= 2 threshold}. Conservative: the support's
+// Which of the tile's NW 8x4 warp patches can hold a pixel centre inside
+// the splat's support {q(d) <= 2 threshold}. Warp w's lanes are the Morton
+// indices 32 w .. 32 w + 31, so its patch starts at the Morton decode of
+// 32 w. Conservative: the support's
 // bounding box is widened by 5 % + 0.25 px, far beyond the rounding of the
 // per-pixel evaluation for conics whose condition number is below 4e4 (the
 // 0.3 px^2 filter bounds it near 3.3e4); worse-conditioned splats, periodic
 // boundaries and non-finite values keep every bit set.
+template <int NW>
 __device__ __forceinline__ uint32_t patch_mask(float cx, float cy, float ca, float cb, float cc, float thr,
                                                float tile_x0, float tile_y0, uint32_t axis) {
-  if (axis != 0u) return 0xffu;
+  constexpr uint32_t kAll = NW >= 32 ? 0xffffffffu : (1u << NW) - 1u;
+  if (axis != 0u) return kAll;
   const float det = ca * cc - cb * cb;
   const float tr = ca + cc;
-  if (!(det > 0.0f) || !(tr * tr <= 4e4f * det) || !(thr >= 0.0f)) return 0xffu;
+  if (!(det > 0.0f) || !(tr * tr <= 4e4f * det) || !(thr >= 0.0f)) return kAll;
   const float q = 2.0f * thr;
   const float hx = sqrtf(q * cc / det) * 1.05f + 0.25f;
   const float hy = sqrtf(q * ca / det) * 1.05f + 0.25f;
-  if (!(hx < 1e30f) || !(hy < 1e30f)) return 0xffu;
+  if (!(hx < 1e30f) || !(hy < 1e30f)) return kAll;
   uint32_t m = 0;
 #pragma unroll
-  for (uint32_t w = 0; w < 8; ++w) {
-    const float x0 = tile_x0 + (float)(8u * ((w >> 1) & 1u)) + 0.5f;
-    const float y0 = tile_y0 + (float)(4u * ((w & 1u) | (((w >> 2) & 1u) << 1))) + 0.5f;
+  for (uint32_t w = 0; w < (uint32_t)NW; ++w) {
+    const float x0 = tile_x0 + (float)morton_compact(32u * w) + 0.5f;
+    const float y0 = tile_y0 + (float)morton_compact(16u * w) + 0.5f;
     const bool hit = cx + hx >= x0 && cx - hx <= x0 + 7.0f && cy + hy >= y0 && cy - hy <= y0 + 3.0f;
     m |= hit ? (1u << w) : 0u;
   }
@@ -140,8 +148,8 @@ __device__ __forceinline__ uint32_t patch_mask(float cx, float cy, float ca, flo
 
 // One (pixel, splat) step of the front-to-back blend (TileRasterizer.ts:616-707).
 // Returns true when the pixel is done (transmittance below the threshold).
-template <class M, bool PERIODIC>
-__device__ __forceinline__ bool blend_one(const Batch& sb, uint32_t j, float pxc, float pyc, const RasterFrame& f,
+template <class M, bool PERIODIC, int NT>
+__device__ __forceinline__ bool blend_one(const Batch<NT>& sb, uint32_t j, float pxc, float pyc, const RasterFrame& f,
                                           PixelAcc& a, uint32_t* blended) {
   const float4 g = sb.geo[j];
   const float4 c = sb.con[j];
@@ -171,20 +179,21 @@ struct RasterCounters {
 // of the block must call it). `done` marks pixels that take no more samples.
 // With STATS, `cnt` receives the reference's per-pixel counters: samples
 // examined until done (TileRasterizer.ts:617) and samples blended (:702).
-template <class M, bool PERIODIC, bool STATS>
+template <class M, bool PERIODIC, bool STATS, int NT>
 __device__ __forceinline__ void blend_range(uint32_t begin, uint32_t source_count, uint32_t raster_count,
                                             uint32_t s0, uint32_t s1, bool capped, const uint32_t* __restrict__ ids,
                                             const float4* __restrict__ mean, const float4* __restrict__ conic,
                                             const float4* __restrict__ color, const RasterFrame& f, float tile_x0,
-                                            float tile_y0, float pxc, float pyc, bool done, PixelAcc& a, Batch& sb,
-                                            RasterCounters& cnt) {
+                                            float tile_y0, float pxc, float pyc, bool done, PixelAcc& a,
+                                            Batch<NT>& sb, RasterCounters& cnt) {
   const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
   const bool counting = STATS && !done;
   uint32_t stop = s1;  // sample index after which this pixel stopped
-  for (uint32_t b = s0; b < s1; b += kBlock) {
+  constexpr uint32_t NB = (uint32_t)Batch<NT>::NB;
+  for (uint32_t b = s0; b < s1; b += NB) {
     if (!__syncthreads_or(!done)) break;
     const uint32_t i = b + t;
-    if (i < s1) {
+    if (t < NB && i < s1) {
       uint32_t src = i;
       if (capped) src = (uint32_t)floorf((((float)i + 0.5f) * (float)source_count) / (float)raster_count);
       const uint32_t g = __ldg(ids + begin + src);
@@ -194,10 +203,10 @@ __device__ __forceinline__ void blend_range(uint32_t begin, uint32_t source_coun
       sb.geo[t] = make_float4(m.x, m.y, m.w, thr);
       sb.con[t] = make_float4(c.x, c.y, c.z, m.z);
       sb.col[t] = __ldg(color + g);
-      sb.mask[t] = (uint8_t)patch_mask(m.x, m.y, c.x, c.y, c.z, thr, tile_x0, tile_y0, f.axis);
+      sb.mask[t] = patch_mask<NT / 32>(m.x, m.y, c.x, c.y, c.z, thr, tile_x0, tile_y0, f.axis);
     }
     __syncthreads();
-    const uint32_t n = min((uint32_t)kBlock, s1 - b);
+    const uint32_t n = min(NB, s1 - b);
     for (uint32_t c0 = 0; c0 < n; c0 += 32) {
       if (__all_sync(0xffffffffu, done)) break;
       const uint32_t k = c0 + lane;
@@ -206,7 +215,7 @@ __device__ __forceinline__ void blend_range(uint32_t begin, uint32_t source_coun
         const uint32_t j = c0 + (uint32_t)(__ffs(bits) - 1);
         bits &= bits - 1u;
         if (!done) {
-          done = blend_one<M, PERIODIC>(sb, j, pxc, pyc, f, a, STATS ? &cnt.blended : nullptr);
+          done = blend_one<M, PERIODIC, NT>(sb, j, pxc, pyc, f, a, STATS ? &cnt.blended : nullptr);
           if (STATS && done) stop = b + j + 1;
         }
       }
@@ -278,10 +287,12 @@ __device__ __forceinline__ float finalize_depth(float wd, float trans, const Pas
   return dev;
 }
 
-// One block per tile of the batch (in work-list order); the tile's view
+// One block of TILE x TILE threads per tile of the batch (in work-list order),
+// lanes on pixels in the Morton order (warp w: an 8x4 patch); the tile's view
 // supplies its viewport and targets.
-template <class M, bool PERIODIC, bool STATS>
-__global__ void __launch_bounds__(kBlock, 3) k_raster(const uint32_t* __restrict__ tile_offsets,
+template <class M, bool PERIODIC, bool STATS, int TILE>
+__global__ void __launch_bounds__(TILE * TILE, TILE == 32 ? 1 : 768 / (TILE * TILE))
+    k_raster(const uint32_t* __restrict__ tile_offsets,
                                                    const uint32_t* __restrict__ order,
                                                    const uint32_t* __restrict__ ids,
                                                    const float4* __restrict__ mean,
@@ -290,7 +301,8 @@ __global__ void __launch_bounds__(kBlock, 3) k_raster(const uint32_t* __restrict
                                                    Control* __restrict__ ctl) {
   // Overflow: the reference zeroes the raster dispatch, so nothing is written.
   if (ctl->state[3] != 0u) return;
-  __shared__ Batch sb;
+  constexpr int NT = TILE * TILE;
+  __shared__ Batch<NT> sb;
   __shared__ uint32_t s_view;
   __shared__ unsigned long long s_stats[4];
   const uint32_t tile = order ? order[blockIdx.x] : blockIdx.x;
@@ -302,7 +314,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_raster(const uint32_t* __restrict
   const uint32_t local = tile - v.tile_base;
   const uint32_t tx = local % v.tiles_x, ty = local / v.tiles_x;
   const uint32_t lx = morton_compact(threadIdx.x), ly = morton_compact(threadIdx.x >> 1);
-  const uint32_t px = tx * kTileSize + lx, py = ty * kTileSize + ly;
+  const uint32_t px = tx * TILE + lx, py = ty * TILE + ly;
   const uint32_t W = (uint32_t)v.vw, H = (uint32_t)v.vh;
   const bool active = px < W && py < H;
   const uint32_t begin = tile_offsets[tile], end = tile_offsets[tile + 1];
@@ -312,12 +324,12 @@ __global__ void __launch_bounds__(kBlock, 3) k_raster(const uint32_t* __restrict
   const uint32_t chunk = o.chunk;
   const bool chunked = chunk != 0u && raster_count > chunk;
   const float pxc = (float)px + 0.5f, pyc = (float)py + 0.5f;
-  const float tile_x0 = (float)(tx * kTileSize), tile_y0 = (float)(ty * kTileSize);
+  const float tile_x0 = (float)(tx * TILE), tile_y0 = (float)(ty * TILE);
   PixelAcc a = {0.0f, 0.0f, 0.0f, 1.0f, 0.0f};
   RasterCounters cnt = {0u, 0u};
   if (!chunked) {
-    blend_range<M, PERIODIC, STATS>(begin, source_count, raster_count, 0, raster_count, capped, ids, mean, conic,
-                                    color, f, tile_x0, tile_y0, pxc, pyc, !active, a, sb, cnt);
+    blend_range<M, PERIODIC, STATS, NT>(begin, source_count, raster_count, 0, raster_count, capped, ids, mean,
+                                        conic, color, f, tile_x0, tile_y0, pxc, pyc, !active, a, sb, cnt);
   } else {
     const uint32_t nchunk = (raster_count + chunk - 1) / chunk;
     bool finished = !active;
@@ -326,8 +338,8 @@ __global__ void __launch_bounds__(kBlock, 3) k_raster(const uint32_t* __restrict
       const uint32_t s0 = ch * chunk;
       const uint32_t s1 = min(s0 + chunk, raster_count);
       PixelAcc p = {0.0f, 0.0f, 0.0f, 1.0f, 0.0f};
-      blend_range<M, PERIODIC, STATS>(begin, source_count, raster_count, s0, s1, capped, ids, mean, conic, color, f,
-                                      tile_x0, tile_y0, pxc, pyc, finished, p, sb, cnt);
+      blend_range<M, PERIODIC, STATS, NT>(begin, source_count, raster_count, s0, s1, capped, ids, mean, conic,
+                                          color, f, tile_x0, tile_y0, pxc, pyc, finished, p, sb, cnt);
       if (!finished) {
         a.r = a.r + p.r * a.t;
         a.g = a.g + p.g * a.t;
@@ -371,20 +383,33 @@ __global__ void __launch_bounds__(kBlock, 3) k_raster(const uint32_t* __restrict
   if (v.depth) v.depth[off] = finalize_depth(a.d, a.t, o, v.vnear, v.vfar);
 }
 
-template <class M>
-void launch_raster_policy(const uint32_t* tile_offsets, const uint32_t* order, const uint32_t* ids,
-                          const float4* mean, const float4* conic, const float4* color, const BatchView& b,
-                          const PassOptions& o, Control* ctl, bool stats, cudaStream_t st) {
-  if (b.total_tiles == 0) return;
+template <class M, int TILE>
+void launch_raster_tile(const uint32_t* tile_offsets, const uint32_t* order, const uint32_t* ids,
+                        const float4* mean, const float4* conic, const float4* color, const BatchView& b,
+                        const PassOptions& o, Control* ctl, bool stats, cudaStream_t st) {
   const bool periodic = o.axis != 0u;
-#define GS_RASTER(P, S) \
-  k_raster<M, P, S><<<b.total_tiles, kBlock, 0, st>>>(tile_offsets, order, ids, mean, conic, color, b, o, ctl)
+#define GS_RASTER(P, S)                                                                                          \
+  k_raster<M, P, S, TILE><<<b.total_tiles, TILE * TILE, 0, st>>>(tile_offsets, order, ids, mean, conic, color, b, \
+                                                                  o, ctl)
   if (periodic) {
     if (stats) GS_RASTER(true, true); else GS_RASTER(true, false);
   } else {
     if (stats) GS_RASTER(false, true); else GS_RASTER(false, false);
   }
 #undef GS_RASTER
+}
+
+template <class M>
+void launch_raster_policy(const uint32_t* tile_offsets, const uint32_t* order, const uint32_t* ids,
+                          const float4* mean, const float4* conic, const float4* color, const BatchView& b,
+                          const PassOptions& o, Control* ctl, bool stats, cudaStream_t st) {
+  if (b.total_tiles == 0) return;
+  if (o.tile == 8u)
+    launch_raster_tile<M, 8>(tile_offsets, order, ids, mean, conic, color, b, o, ctl, stats, st);
+  else if (o.tile == 32u)
+    launch_raster_tile<M, 32>(tile_offsets, order, ids, mean, conic, color, b, o, ctl, stats, st);
+  else
+    launch_raster_tile<M, 16>(tile_offsets, order, ids, mean, conic, color, b, o, ctl, stats, st);
 }
 
 }  // namespace gs

@@ -24,7 +24,6 @@
 
 namespace gs {
 
-constexpr int kTile = 16;                 // src/renderer/pipeline/constants.ts:1
 constexpr uint32_t kActiveTag = 0x3f800000u;  // src/renderer/pipeline/activeSlots.ts:4
 constexpr uint32_t kInvisibleKey = 0xffffffffu;
 
@@ -366,10 +365,11 @@ __device__ __forceinline__ bool subpixel_has_sample(float cx, float cy, float k0
   return false;
 }
 
-// tileContribution.ts:16-59 for one image centre.
+// tileContribution.ts:16-59 for one image centre; ts = pixels per tile side
+// (the reference's TILE_SIZE, 16, constants.ts:1; 8 and 32 in batched renders
+// tuned to them).
 __device__ __forceinline__ bool tile_rect_test(float cx, float cy, float k0, float k1, float k2, float thr, int tx,
-                                               int ty) {
-  const float ts = (float)kTile;
+                                               int ty, float ts) {
   float rminx = (float)tx * ts, rminy = (float)ty * ts;
   float rmaxx = rminx + ts, rmaxy = rminy + ts;
   bool x_left = cx < rminx, x_right = cx > rmaxx;
@@ -395,21 +395,21 @@ __device__ __forceinline__ bool tile_rect_test(float cx, float cy, float k0, flo
 // tileContribution.ts:84-114
 __device__ __forceinline__ bool boundary_tile_hit(float cx, float cy, float k0, float k1, float k2, float thr,
                                                   float rx, float ry, int tx, int ty, float vw, float vh,
-                                                  uint32_t axis) {
-  if (axis == 0u) return tile_rect_test(cx, cy, k0, k1, k2, thr, tx, ty);
+                                                  uint32_t axis, float ts) {
+  if (axis == 0u) return tile_rect_test(cx, cy, k0, k1, k2, thr, tx, ty, ts);
   bool ax = axis == 1u;
   float period = ax ? vw : vh;
   float cen = ax ? cx : cy;
   float canon = cen - floorf(cen / period) * period;
   float ccx = ax ? canon : cx, ccy = ax ? cy : canon;
-  float tstart = (float)(ax ? tx : ty) * (float)kTile;
+  float tstart = (float)(ax ? tx : ty) * ts;
   float r = ax ? rx : ry;
   int first = (int)ceilf(((tstart - r) - canon) / period);
-  int last = (int)floorf((((tstart + (float)kTile) + r) - canon) / period);
+  int last = (int)floorf((((tstart + ts) + r) - canon) / period);
   for (int img = first; img <= last; ++img) {
     float icx = ccx, icy = ccy;
     if (ax) icx = icx + (float)img * vw; else icy = icy + (float)img * vh;
-    if (tile_rect_test(icx, icy, k0, k1, k2, thr, tx, ty)) return true;
+    if (tile_rect_test(icx, icy, k0, k1, k2, thr, tx, ty, ts)) return true;
   }
   return false;
 }

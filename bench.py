@@ -658,13 +658,14 @@ def main() -> None:
     hbm, peak_kind = peaks()
     mean_stats = {k: statistics.mean(s[k] for s in stats) for k in ("visibleGaussianCount", "requestedIntersections")}
     n, v, inter = scene["active_count"], int(mean_stats["visibleGaussianCount"]), int(mean_stats["requestedIntersections"])
-    tiles = ((W + 15) // 16) * ((H + 15) // 16)
-    tile_bits = max(1, int(np.ceil(np.log2(tiles + 1))))
-    tile_passes = (tile_bits + 7) // 8
+    tile_px = int(tuning.get("tile_size", 16))
+    tiles = ((W + tile_px - 1) // tile_px) * ((H + tile_px - 1) // tile_px)
     stages = {}
     # per batch: every stage processes all views of the step, in launches of
-    # views_per_launch views (one view group each: the views share the scene)
-    bn, bv_, bi, bt = n * ncam, v * ncam, inter * ncam, tiles * ncam
+    # views_per_launch views (one view group each: the views share the scene);
+    # visible and intersection totals are the batched pass's own (its tile
+    # size sets the intersections)
+    bn, bv_, bi, bt = n * ncam, int(bstats["visibleGaussianCount"]), int(bstats["intersectionCount"]), tiles * ncam
     vpl = int(tuning["views_per_launch"]) or ncam
     nlaunch = (ncam + vpl - 1) // vpl
     ltile_bits = max(1, int(np.ceil(np.log2(tiles * min(vpl, ncam) + 1))))
@@ -699,7 +700,7 @@ def main() -> None:
                    "flops_per_batch": raster_flops, "checked": work["checked"], "blended": work["blended"],
                    "exp_per_s": work["blended"] / raster_s if raster_s > 0 else 0.0,
                    "peak_source": f"{sms} SMs x 128 FP32 lanes x 2 x {clock_mhz:.0f} MHz (median sampled SM clock)"}
-    per_view = measured_traffic_per_view(dom, args)
+    per_view = measured_traffic_per_view(dom, args) if tile_px == 16 else None
     traffic_per_launch = per_view * min(vpl, ncam) if per_view else None
     if dom == "raster":
         roofline = dict(raster_fp32, traffic=traffic_per_launch,
@@ -746,7 +747,8 @@ def main() -> None:
                    "frames_per_step": len(cams), "parallelism": f"replicas x{world}",
                    "launch_shape": tuning,
                    "l2": "inputs larger than L2 (288 MB packed scene read every frame)",
-                   "visible_mean": v, "intersections_mean": inter},
+                   "visible_mean": v, "intersections_mean": inter,
+                   "batched_intersections_per_view": int(bstats["intersectionCount"]) // ncam},
         "p50_ms": p50, "p99_ms": p99, "psnr_db_vs_fp64": psnr_db,
         "forms": {"batched": {"precision": args.precision, "frames_per_s": fps, "views_per_batch": ncam,
                               "tuning": tuning, "autotune_ms_per_batch": tune_ms,

@@ -230,31 +230,43 @@ typedef struct gs3d_view {
 } gs3d_view;
 
 /* Launch-shape tuning (no counterpart in the reference, whose dispatch shape
- * is fixed; outputs do not depend on it). views_per_launch: a batch of more
+ * is fixed). views_per_launch: a batch of more
  * views runs as consecutive launch sequences of at most that many views on the
  * same stream (0 = the whole batch at once); read_stats then reports their
  * totals (visible and intersection counts summed, requested = the largest
  * sequence's demand, overflow if any sequence overflowed), the output state
  * covers the whole batch, and get_resources and batch_layout describe the
  * last sequence. tile_digit_bits: the widest digit of the tile sort, 4..8.
- * work_order: 1 = rasterize tiles heaviest first, 0 = in tile order.
+ * work_order: 1 = rasterize tiles heaviest first, 0 = in tile order. None of
+ * these three changes what a batch produces.
+ * tile_size: pixels per tile side of batched renders (render_batch, captured
+ * graphs, autotune): 8, 16 or 32, 0 = the reference's 16 (constants.ts:1).
+ * The rasterizer's block follows the tile (one warp per 8x8 patch in the
+ * FP32 and half2 forms, one thread per pixel in EXACT). The EXACT image does
+ * not depend on it (the tile test is conservative for every pixel of the
+ * tile); the tile ids, counts, intersection records and tile offsets do, and
+ * so do the raster chunk split and maxRasterizedSplatsPerTile, which act per
+ * tile, and the visible set, by splats that reach a tile only where it
+ * extends past the image edge (they cover no pixel). Single-view
+ * gs3d_pipeline_render always uses 16.
  * Setting a tuning releases captured graphs. */
 typedef struct gs3d_tuning {
   uint32_t views_per_launch; /* default 0 */
   uint32_t tile_digit_bits;  /* default 8 */
   uint32_t work_order;       /* default 1 */
-  uint32_t reserved;
+  uint32_t tile_size;        /* default 0 (16) */
 } gs3d_tuning;
 
 gs3d_status gs3d_pipeline_set_tuning(gs3d_pipeline* pipeline, const gs3d_tuning* tuning);
 gs3d_status gs3d_pipeline_get_tuning(gs3d_pipeline* pipeline, gs3d_tuning* tuning);
 
-/* Times the batch under candidate tunings (coordinate descent: views per
- * launch halving from the batch size, tile digit width 7..4, then the work
- * order; `trials` timed batches each after one untimed one), keeps the
- * fastest and returns it with its milliseconds per batch. The views' targets
- * receive the renders. GS3D_ERROR_RANGE if the intersection capacity cannot
- * hold the batch. */
+/* Times the batch under candidate tunings (coordinate descent: tile size 8
+ * and 32 against 16, views per launch halving from the batch size, tile
+ * digit width 7..4, then the work order; `trials` timed batches each after
+ * one untimed one), keeps the fastest and returns it with its milliseconds
+ * per batch. The views' targets receive the renders. GS3D_ERROR_RANGE if the
+ * intersection capacity cannot hold the batch at 16-pixel tiles; a tile size
+ * whose batch overflows the capacity is skipped. */
 gs3d_status gs3d_pipeline_autotune(gs3d_pipeline* pipeline, const gs3d_view* views, uint32_t count, uint32_t trials,
                                    gs3d_tuning* best, double* best_ms, void* stream);
 

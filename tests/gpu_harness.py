@@ -107,11 +107,12 @@ def psnr(a: np.ndarray, b: np.ndarray) -> float:
 
 
 def render_batch(scenes_frames: list, precision: str = "exact", capacity: int = 1 << 22,
-                 color_format: str = "rgba32f", share_scenes: bool = False) -> list:
+                 color_format: str = "rgba32f", share_scenes: bool = False, tuning: dict | None = None) -> list:
     """Render (scene, frame) pairs in one batch and split every buffer per view.
 
     Each view's result uses the view's own ordinals and local tile ids, so it
-    compares directly with a single-view oracle render of that view. With
+    compares directly with a single-view oracle render of that view (at the
+    tuning's tile size: the reference's 16 unless `tuning` sets another). With
     share_scenes, pairs holding the same scene object render from one resident
     copy (one set of device buffers), so consecutive ones form a view group."""
     import torch
@@ -122,6 +123,8 @@ def render_batch(scenes_frames: list, precision: str = "exact", capacity: int = 
     else:
         dss = [dev.DeviceScene(s) for s, _ in scenes_frames]
     pipe = P.TiledGaussianPipeline(dss[0].data(), pipeline_options(scenes_frames[0][1], precision, capacity))
+    if tuning:
+        pipe.set_tuning(tuning)
     targets, views = [], []
     for ds, (scene, frame) in zip(dss, scenes_frames):
         W, H = int(frame["width"]), int(frame["height"])
