@@ -39,7 +39,18 @@ __device__ __forceinline__ void load_sh(const uint32_t* __restrict__ p, uint32_t
   }
 }
 
+// FAST: the colour feeds only a fast raster form (eval_sh_fast); otherwise
+// the reference's expression order (eval_sh, bit-exact with the oracle).
+template <bool FAST>
 __device__ __forceinline__ f3 eval_sh_any(uint32_t degree, const uint32_t* co, f3 d, const float* snorm) {
+  if (FAST) {
+    switch (degree) {
+      case 0: return eval_sh_fast<0>(co, d, snorm);
+      case 1: return eval_sh_fast<1>(co, d, snorm);
+      case 2: return eval_sh_fast<2>(co, d, snorm);
+      default: return eval_sh_fast<3>(co, d, snorm);
+    }
+  }
   switch (degree) {
     case 0: return eval_sh<0>(co, d, snorm);
     case 1: return eval_sh<1>(co, d, snorm);
@@ -107,7 +118,7 @@ __device__ __forceinline__ uint32_t count_tiles_warp(CountShared& sm, uint32_t n
 // GROUPED: some group holds several views (decode once, before the view
 // loop); otherwise every group is one view and the decode stays inside the
 // per-view chain, after the object tests, where it costs fewest registers.
-template <bool FP64, bool GROUPED>
+template <bool FP64, bool GROUPED, bool FAST_SH>
 __global__ void __launch_bounds__(kBlock, 4) k_project(BatchView b, PassOptions o, float4* __restrict__ mean_out,
                                                     float4* __restrict__ conic_out, float4* __restrict__ color_out,
                                                     uint32_t* __restrict__ count_out, uint32_t* __restrict__ key_out,
@@ -260,7 +271,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_project(BatchView b, PassOptions 
     if (cnt > 0) {
       uint32_t co[16];
       load_sh(v.sh + (size_t)slot * v.C, v.degree, co);
-      const f3 col = eval_sh_any(v.degree, co, vdir, s_snorm);
+      const f3 col = eval_sh_any<FAST_SH>(v.degree, co, vdir, s_snorm);
       mo4 = make_float4(pr.cx, pr.cy, pr.depth, op);
       conic_out[item] = make_float4(pr.conic_x, pr.conic_y, pr.conic_z, rx + ry * 512.0f);
       // Emission record: what the emission reads per depth rank, in one
@@ -291,25 +302,27 @@ __global__ void __launch_bounds__(kBlock, 4) k_project(BatchView b, PassOptions 
   }
 }
 
+template <bool FAST_SH>
+void launch_project_t(const BatchView& b, const PassOptions& o, float4* mean, float4* conic, float4* color,
+                      uint32_t* counts, uint32_t* keys, float4* rec, float4* erec, cudaStream_t st) {
+  const bool grouped = b.ngroups < b.nviews;
+#define GS_PROJECT(F, G) \
+  k_project<F, G, FAST_SH><<<b.total_blocks, kBlock, 0, st>>>(b, o, mean, conic, color, counts, keys, rec, erec)
+  if (o.proj_fp64) {
+    if (grouped) GS_PROJECT(true, true); else GS_PROJECT(true, false);
+  } else {
+    if (grouped) GS_PROJECT(false, true); else GS_PROJECT(false, false);
+  }
+#undef GS_PROJECT
+}
+
+// The fast raster forms (rec != null) take the fused-multiply-add SH colour;
+// EXACT keeps the reference's order.
 void launch_project(const BatchView& b, const PassOptions& o, float4* mean, float4* conic, float4* color,
                     uint32_t* counts, uint32_t* keys, float4* rec, float4* erec, cudaStream_t st) {
   if (b.total_blocks == 0) return;  // projection blocks over the view groups
-  const bool grouped = b.ngroups < b.nviews;
-  if (o.proj_fp64) {
-    if (grouped)
-      k_project<true, true><<<b.total_blocks, kBlock, 0, st>>>(b, o, mean, conic, color, counts, keys, rec,
-                                                                      erec);
-    else
-      k_project<true, false><<<b.total_blocks, kBlock, 0, st>>>(b, o, mean, conic, color, counts, keys, rec,
-                                                                      erec);
-  } else {
-    if (grouped)
-      k_project<false, true><<<b.total_blocks, kBlock, 0, st>>>(b, o, mean, conic, color, counts, keys, rec,
-                                                                      erec);
-    else
-      k_project<false, false><<<b.total_blocks, kBlock, 0, st>>>(b, o, mean, conic, color, counts, keys, rec,
-                                                                      erec);
-  }
+  if (rec) launch_project_t<true>(b, o, mean, conic, color, counts, keys, rec, erec, st);
+  else launch_project_t<false>(b, o, mean, conic, color, counts, keys, rec, erec, st);
 }
 
 // ---------------------------------------------------------------------------

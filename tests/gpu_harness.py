@@ -80,14 +80,25 @@ class GpuRun:
         self.pipe.dispose()
 
 
-def assert_bit_exact(g: dict, o: dict, image: bool = True) -> None:
-    """Every buffer the reference exposes through getResources() is identical."""
+# The fast raster forms evaluate the SH colour with fused multiply-adds (the
+# colour feeds only their image): projected colours within this of the
+# oracle's, the slot tag in the fourth component still exact.
+FAST_COLOR_TOL = 1e-5
+
+
+def assert_bit_exact(g: dict, o: dict, image: bool = True, color_tol: float = 0.0) -> None:
+    """Every buffer the reference exposes through getResources() is identical
+    (the projected colour within color_tol when it is nonzero)."""
     assert np.array_equal(g["visible_state"], o["visible_state"]), (g["visible_state"], o["visible_state"])
     assert np.array_equal(g["tile_counts"], o["tile_counts"])
     assert np.array_equal(g["proj_mean"].view(np.uint32), o["proj_mean"].view(np.uint32))
     vis = o["tile_counts"] > 0
     assert np.array_equal(g["proj_conic"][vis].view(np.uint32), o["proj_conic"][vis].view(np.uint32))
-    assert np.array_equal(g["proj_color"][vis].view(np.uint32), o["proj_color"][vis].view(np.uint32))
+    if color_tol:
+        assert np.abs(g["proj_color"][vis][:, :3] - o["proj_color"][vis][:, :3]).max(initial=0.0) <= color_tol
+        assert np.array_equal(g["proj_color"][vis][:, 3].view(np.uint32), o["proj_color"][vis][:, 3].view(np.uint32))
+    else:
+        assert np.array_equal(g["proj_color"][vis].view(np.uint32), o["proj_color"][vis].view(np.uint32))
     assert np.array_equal(g["visible_offsets"], o["visible_offsets"])
     assert np.array_equal(g["depth_sorted"], o["depth_sorted"])
     assert np.array_equal(g["ordered_counts"], o["ordered_counts"])

@@ -3,7 +3,8 @@
 Integer stages (tile counts, visible offsets, depth keys and stable order,
 intersection offsets, sorted (tile, ordinal) records, tile ranges, dispatch
 and output state) are bit-exact. The EXACT raster form is bit-exact too; the
-FP32 raster form (hardware exp/log, fused multiply-add) is held to
+fast forms' projected colour (SH by fused multiply-adds) is held to 1e-5 and
+the FP32 raster form (hardware exp/log, fused multiply-add) to
 max |err| <= 4e-3 against the oracle's FP32 image and >= 50 dB PSNR against
 the FP64 twin.
 """
@@ -14,7 +15,7 @@ import pytest
 
 import oracle
 from conftest import scenes
-from gpu_harness import GpuRun, assert_bit_exact, psnr
+from gpu_harness import FAST_COLOR_TOL, GpuRun, assert_bit_exact, psnr
 
 pytestmark = pytest.mark.gpu
 
@@ -122,7 +123,7 @@ def test_fp32_raster_tolerance(name):
     run = GpuRun(scene, frame, "fp32", capacity=max(int(o["state"][1]), 1))
     g = run.render(frame)
     run.close()
-    assert_bit_exact(g, o, image=False)
+    assert_bit_exact(g, o, image=False, color_tol=FAST_COLOR_TOL)
     assert np.abs(g["rgba"] - o["rgba"]).max() <= FP32_MAX_ABS
     assert psnr(g["rgba"][..., :3], o64["rgba"][..., :3]) >= MIN_PSNR_DB
 
@@ -137,7 +138,7 @@ def test_half2_raster_tolerance(name):
     run = GpuRun(scene, frame, "half2", capacity=max(int(o["state"][1]), 1))
     g = run.render(frame)
     run.close()
-    assert_bit_exact(g, o, image=False)
+    assert_bit_exact(g, o, image=False, color_tol=FAST_COLOR_TOL)
     assert np.abs(g["rgba"] - o["rgba"]).max() <= HALF2_MAX_ABS
     assert psnr(g["rgba"][..., :3], o64["rgba"][..., :3]) >= MIN_PSNR_DB
 
