@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shape for the batched form")
     ap.add_argument("--views-per-launch", type=int, default=None,
                     help="fixed launch shape for the batched form instead of the autotuner's")
+    ap.add_argument("--tile-size", type=int, default=None, choices=[8, 16, 32],
+                    help="fixed tile size for the batched form instead of the autotuner's")
     ap.add_argument("--forms", default="all", choices=["all", "batched"],
                     help="'batched' skips the timed plain (one view per launch) form")
     ap.add_argument("--serve", action="store_true", help="serving-loop measurement (configuration 4)")
@@ -543,6 +545,8 @@ def main() -> None:
         batched.set_tuning({"views_per_launch": args.views_per_launch})
     elif not args.no_autotune:
         _, tune_ms = batched.autotune(views, trials=3)
+    if args.tile_size is not None:
+        batched.set_tuning({"tile_size": args.tile_size})
     tuning = batched.get_tuning()
     batched.render_batch(views)  # size the workspaces, then capture the pass as a graph
     torch.cuda.synchronize()
