@@ -214,3 +214,30 @@ def test_tile_sort_bits(L):
     assert L.gso_tile_sort_bits(80 * 45) == 13
     assert L.gso_tile_sort_bits(120 * 68) == 14
     assert L.gso_tile_sort_bits(240 * 135) == 16
+
+
+def test_oracle_chunked_raster_composites_to_the_whole_stream():
+    # The same rule through the oracle's own rasterizer: with chunks of 256
+    # samples (TileRasterizer.ts:807-902, rasterChunks.ts:3-99) every tile
+    # of more than 256 records is blended as ordered chunk partials and
+    # composited; with chunking off it is one stream. In the FP64 twin, and
+    # with a transmittance threshold too small to stop any pixel early (the
+    # early stop is the one place the two differ by design), the images agree
+    # to rounding.
+    from conftest import scenes
+    sc = scenes()
+    scene = sc.uniform_cloud(8000, seed=17, log_scale=(-1.6, 0.4), opacity_logit=(-2.0, 0.5))
+    base = sc.make_frame(sc.look_at((0.5, 1.0, 11.0), (0, 0, 0)), 64, 48, 55.0, 0.1, 100.0,
+                         transmittance_threshold=1e-30)
+    whole = oracle.render(scene, dict(base, raster_chunk_size=0), 1)
+    chunked = oracle.render(scene, dict(base, raster_chunk_size=256), 1)
+    loads = np.diff(whole["tile_offsets"].astype(np.int64))
+    assert loads.max() > 2 * 256  # some tiles split into three or more chunks
+    assert np.array_equal(whole["sorted_records"], chunked["sorted_records"])
+    assert np.abs(whole["rgba"] - chunked["rgba"]).max() <= 1e-9
+    # In FP32 the two orders of the same sums round differently: the chunked
+    # path did run, and stays within rounding of the whole stream.
+    whole32 = oracle.render(scene, dict(base, raster_chunk_size=0), 0)
+    chunked32 = oracle.render(scene, dict(base, raster_chunk_size=256), 0)
+    diff = np.abs(whole32["rgba"] - chunked32["rgba"]).max()
+    assert 0.0 < diff <= 1e-5
