@@ -518,13 +518,15 @@ def main() -> None:
         ck = clocks.stop()
         barrier()
         ms = e0.elapsed_time(e1)
-        pipe_for_stages.set_profiling(True)
-        pipe_for_stages.stage_times()
-        for _ in range(args.steps):
-            step()
-        torch.cuda.synchronize()
-        sm, prof = pipe_for_stages.stage_times()
-        pipe_for_stages.set_profiling(False)
+        sm, prof = {}, 0
+        if pipe_for_stages is not None:
+            pipe_for_stages.set_profiling(True)
+            pipe_for_stages.stage_times()
+            for _ in range(args.steps):
+                step()
+            torch.cuda.synchronize()
+            sm, prof = pipe_for_stages.stage_times()
+            pipe_for_stages.set_profiling(False)
         ms = max_over_ranks(ms, world)
         return ms, sm, prof, nl, ck
 
@@ -561,22 +563,18 @@ def main() -> None:
             batched.launch_graph(cams, stream=gstream.cuda_stream)
         return batched.last_launch_count()
 
-    ms_total, stage_ms, profiled, launches, clock_info = timed(step_batched, batched)
+    # Direct batches (one render_batch call per step), then the per-stage
+    # breakdown from a profiled run of as many steps.
+    ms_direct, stage_ms, profiled, launches_direct, clock_direct = timed(step_batched, batched)
     # Stage times are means per launch sequence; a batch may run as several.
     seq_per_batch = profiled / args.steps if profiled else 1.0
     stage_ms = {k: v * seq_per_batch for k, v in stage_ms.items()}
-    # Same batches replayed from the captured graph (no per-stage events).
-    for _ in range(3):
-        step_graph()
-    torch.cuda.synchronize()
-    g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    g0.record(gstream)
-    for _ in range(args.steps):
-        step_graph()
-    g1.record(gstream)
-    torch.cuda.synchronize()
-    fps_graph = job_frames_per_s(args.steps, ncam, world, max_over_ranks(g0.elapsed_time(g1), world) / 1000.0)
+    fps_direct = job_frames_per_s(args.steps, ncam, world, ms_direct / 1000.0)
+    # The headline: the same batches replayed from the captured graph (one
+    # graph launch per step; each replay restages the cameras).
+    ms_total, _, _, launches, clock_info = timed(step_graph, None, gstream)
     fps = job_frames_per_s(args.steps, ncam, world, ms_total / 1000.0)
+    fps_graph = fps
     bstats = batched.read_stats()
 
     # Latency distributions: one frame (plain) and one 16-camera batch, each
@@ -745,8 +743,8 @@ def main() -> None:
         "warmup": args.warmup, "ms_per_step": ms_total / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f16" if args.precision == "half2" else "f32", "data": "synthetic",
         "config": {"workload": f"{args.splats} clustered Gaussians (64-cluster mixture, SH3 rgb8e8, compact), "
-                               f"{W}x{H}, {len(cams)} orbit cameras per step rendered as one batch, "
-                               f"{args.precision} raster",
+                               f"{W}x{H}, {len(cams)} orbit cameras per step rendered as one batch "
+                               f"replayed from a captured CUDA graph, {args.precision} raster",
                    "splats": args.splats, "width": W, "height": H, "cameras": len(cams),
                    "frames_per_step": len(cams), "parallelism": f"replicas x{world}",
                    "launch_shape": tuning,
@@ -757,6 +755,8 @@ def main() -> None:
         "forms": {"batched": {"precision": args.precision, "frames_per_s": fps, "views_per_batch": ncam,
                               "tuning": tuning, "autotune_ms_per_batch": tune_ms,
                               "graph_replay_frames_per_s": fps_graph,
+                              "direct_frames_per_s": fps_direct, "direct_clocks": clock_direct,
+                              "direct_gpu_launches": launches_direct,
                               "p50_batch_ms": p50, "p99_batch_ms": p99, "psnr_db": psnr_db,
                               "stats": bstats},
                   "plain": {"precision": args.plain_precision, "frames_per_s": fps_plain,
