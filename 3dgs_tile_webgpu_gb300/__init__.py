@@ -213,7 +213,8 @@ class TiledGaussianPipeline:
         ``tile_digit_bits`` (4..8), ``work_order`` (1 = heaviest tiles first)
         change nothing the batch produces; ``tile_size`` (8, 16 or 32; 0 =
         16) sets the tiles of batched renders, which leaves the EXACT image
-        unchanged but not the per-tile buffers."""
+        unchanged but not the per-tile buffers; ``raster_pixels_per_lane``
+        (2 or 4) sets the fast rasterizers' block shape."""
         t = Tuning()
         self._lib.gs3d_pipeline_get_tuning(self._p, C.byref(t))
         for k, v in tuning.items():
@@ -224,7 +225,8 @@ class TiledGaussianPipeline:
         t = Tuning()
         _raise(self._lib, self._lib.gs3d_pipeline_get_tuning(self._p, C.byref(t)), self._p)
         return {"views_per_launch": t.views_per_launch, "tile_digit_bits": t.tile_digit_bits,
-                "work_order": t.work_order, "tile_size": t.tile_size or 16}
+                "work_order": t.work_order, "tile_size": t.tile_size or 16,
+                "raster_pixels_per_lane": t.raster_pixels_per_lane or 2}
 
     def autotune(self, views: list, trials: int = 3, stream: int = 0) -> tuple[dict, float]:
         """Time candidate tunings on this batch (same tuple layout as

@@ -3,7 +3,7 @@ from __future__ import annotations
 
 import ctypes as C
 
-GS3D_ABI_VERSION = 3
+GS3D_ABI_VERSION = 4
 GS3D_OK = 0
 GS3D_ERROR_INVALID_ARGUMENT = 1
 GS3D_ERROR_RANGE = 2
@@ -55,7 +55,7 @@ class View(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("views_per_launch", C.c_uint32), ("tile_digit_bits", C.c_uint32), ("work_order", C.c_uint32),
-                ("tile_size", C.c_uint32)]
+                ("tile_size", C.c_uint32), ("raster_pixels_per_lane", C.c_uint32), ("reserved", C.c_uint32 * 3)]
 
 
 class SplatSource(C.Structure):

@@ -51,6 +51,7 @@ struct PassOptions {
   uint32_t tile;           // pixels per tile side: 16 (the reference's), or 8 / 32 in tuned batches
   float tile_px;           // the same as a float
   float tile_inv;          // its reciprocal (exact: a power of two)
+  uint32_t pixels_per_lane;  // fast raster forms: 2 (a warp per 8x8 patch) or 4 (per 8x16)
 };
 
 // The batch table in device memory: the per-frame parameters (attempt,

@@ -139,7 +139,7 @@ struct gs3d_pipeline {
   uint32_t graph_tile = kTileSize;
   // Tuning (gs3d_pipeline_set_tuning / autotune) and the device summary of a
   // batch rendered as several launch sequences.
-  gs3d_tuning tuning{0u, 8u, 1u, 0u};  // tile_size 0: the reference's 16
+  gs3d_tuning tuning{0u, 8u, 1u, 0u, 0u, {0u, 0u, 0u}};  // tile_size 0: the reference's 16; 2 pixels per lane
   BatchSummary* summary = nullptr;
   uint32_t last_chunks = 1;
   BatchView last_bv{};  // batch table of the last launch sequence (device pointers)
@@ -774,6 +774,7 @@ void record_batch(gs3d_pipeline* p, const Plan& pl, unsigned char* dev, cudaStre
   o.tile = pl.tile;
   o.tile_px = (float)pl.tile;
   o.tile_inv = 1.0f / (float)pl.tile;
+  o.pixels_per_lane = p->tuning.raster_pixels_per_lane == 4u ? 4u : 2u;
   memcpy(o.background, p->desc.background, sizeof(o.background));
   o.t_threshold = p->desc.raster_transmittance_threshold;
   o.depth_alpha_threshold = p->desc.depth_alpha_threshold;
@@ -1070,6 +1071,8 @@ gs3d_status gs3d_pipeline_set_tuning(gs3d_pipeline* p, const gs3d_tuning* t) {
   if (t->work_order > 1) return fail(p, GS3D_ERROR_INVALID_ARGUMENT, "work_order must be 0 or 1");
   if (t->tile_size != 0 && t->tile_size != 8 && t->tile_size != 16 && t->tile_size != 32)
     return fail(p, GS3D_ERROR_RANGE, "tile_size must be 8, 16 or 32 (0: 16)");
+  if (t->raster_pixels_per_lane != 0 && t->raster_pixels_per_lane != 2 && t->raster_pixels_per_lane != 4)
+    return fail(p, GS3D_ERROR_RANGE, "raster_pixels_per_lane must be 2 or 4 (0: 2)");
   if (p->last_stream) cudaStreamSynchronize(p->last_stream);
   release_graphs(p);  // captured graphs follow the tuning they were captured with
   p->tuning = *t;
@@ -1118,16 +1121,23 @@ gs3d_status gs3d_pipeline_autotune(gs3d_pipeline* p, const gs3d_view* views, uin
     *ms = (double)f / trials;
     return GS3D_OK;
   };
-  gs3d_tuning cur{0u, 8u, 1u, 0u};
+  gs3d_tuning cur{0u, 8u, 1u, 0u, 0u, {0u, 0u, 0u}};
   double cur_ms = 0.0;
   gs3d_status s = measure(cur, &cur_ms);
   // Coordinate descent: tile size (8 and 32 against the reference's 16; the
-  // raster block follows the tile, one warp per 8x8 patch), views per launch
-  // (halving), widest tile-sort digit, then the raster work order.
+  // raster block follows the tile), the fast rasterizers' pixels per lane
+  // (the block shape), views per launch (halving), widest tile-sort digit,
+  // then the raster work order.
   for (uint32_t ts : {8u, 32u}) {
     if (s != GS3D_OK) break;
     gs3d_tuning t = cur;
     t.tile_size = ts;
+    double ms = 0.0;
+    if ((s = measure(t, &ms)) == GS3D_OK && ms < cur_ms) { cur = t; cur_ms = ms; }
+  }
+  if (s == GS3D_OK && p->desc.raster_precision != GS3D_RASTER_EXACT) {
+    gs3d_tuning t = cur;
+    t.raster_pixels_per_lane = 4u;
     double ms = 0.0;
     if ((s = measure(t, &ms)) == GS3D_OK && ms < cur_ms) { cur = t; cur_ms = ms; }
   }

@@ -209,6 +209,169 @@ __device__ __forceinline__ void blend_range_h2(uint32_t begin, uint32_t source_c
   if (count1) c1n.checked += stop1 - s0;
 }
 
+// The same blend for K pixels per lane (pixels (x, y + 4 i), i < K, in pairs):
+// the block shape of a warp per 8 x 4K patch. Warp-level: needs no other warp
+// of the block.
+template <bool HALF, bool PERIODIC, bool STATS, bool DEPTH, int K>
+__device__ __forceinline__ void blend_range_hk(uint32_t begin, uint32_t source_count, uint32_t raster_count,
+                                               uint32_t s0, uint32_t s1, bool capped,
+                                               const uint32_t* __restrict__ ids, const float4* __restrict__ mean,
+                                               const float4* __restrict__ color,
+                                               const float4* __restrict__ rec, bool need_depth,
+                                               const RasterFrame& f, float patch_x0, float patch_y0, float pxc,
+                                               float pyc0, bool (&done)[K], PixelAcc (&acc)[K], WarpStage& ws,
+                                               RasterCounters (&cnt)[K]) {
+  static_assert(K % 2 == 0, "pixels are evaluated in pairs");
+  const uint32_t lane = threadIdx.x & 31u;
+  bool counting[K];
+  uint32_t stop[K];
+  float pyc[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    counting[k] = STATS && !done[k];
+    stop[k] = s1;
+    pyc[k] = pyc0 + 4.0f * (float)k;
+  }
+  const uint32_t lt = (1u << lane) - 1u;
+  auto load_id = [&](uint32_t i) -> uint32_t {
+    if (i >= s1) return 0u;
+    uint32_t src = i;
+    if (capped) src = (uint32_t)floorf((((float)i + 0.5f) * (float)source_count) / (float)raster_count);
+    return __ldg(ids + begin + src);
+  };
+  auto all_done = [&]() {
+    bool d = true;
+#pragma unroll
+    for (int k = 0; k < K; ++k) d = d && done[k];
+    return d;
+  };
+  // The FP32 form loads the next group's record ids one group ahead (the
+  // half2 form, at its register limit for 9 blocks per SM, is faster without).
+  uint32_t next_id = HALF ? 0u : load_id(s0 + lane);
+  for (uint32_t b = s0; b < s1; b += 32) {
+    if (__all_sync(0xffffffffu, all_done())) break;
+    const uint32_t i = b + lane;
+    bool reach = false;
+    float4 r0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), r1 = r0, col32 = r0;
+    float depth = 0.0f;
+    uint32_t cur_id = 0;
+    if (!HALF) {
+      cur_id = next_id;
+      next_id = load_id(b + 32u + lane);
+    }
+    if (i < s1) {
+      const uint32_t g = HALF ? load_id(i) : cur_id;
+      r0 = __ldg(rec + 2 * (size_t)g);  // one 32-byte record
+      r1 = __ldg(rec + 2 * (size_t)g + 1);
+      if (!HALF) col32 = __ldg(color + g);
+      if (DEPTH && need_depth) depth = __ldg(&mean[g].z);
+      reach = PERIODIC || patch_reach(r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, patch_x0 + 0.5f, patch_y0 + 0.5f,
+                                          7.0f, 4.0f * (float)K - 1.0f);
+    }
+    const uint32_t bal = __ballot_sync(0xffffffffu, reach);
+    if (reach) {
+      const uint32_t q = __popc(bal & lt);
+      ws.geo[q] = r0;
+      if (HALF) {
+        const uint32_t rg_bits = __float_as_uint(r1.z), bl_bits = __float_as_uint(r1.w);
+        const float2 rg = __half22float2(*reinterpret_cast<const __half2*>(&rg_bits));
+        const __half2 bl = *reinterpret_cast<const __half2*>(&bl_bits);
+        const __half2 lim = __half2half2(__high2half(bl));
+        ws.con[q] = make_float4(r1.x, r1.y, __uint_as_float(*reinterpret_cast<const uint32_t*>(&lim)), depth);
+        ws.col[q] = make_float4(rg.x, rg.y, __low2float(bl), 0.0f);
+      } else {
+        ws.con[q] = make_float4(r1.x, r1.y, fminf(r1.y, kLog2MaxAlpha), depth);
+        ws.col[q] = col32;
+      }
+      if (PERIODIC) ws.raw[q] = raw_conic(r0, r1);
+      if (STATS) ws.idx[q] = (uint8_t)lane;
+    }
+    __syncwarp();
+    const uint32_t n = __popc(bal);
+    float th[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) th[k] = done[k] ? __int_as_float(0x7f800000) : kLog2MinAlpha;
+    for (uint32_t j = 0; j < n; ++j) {
+      const float4 g = ws.geo[j];
+      const float4 c = ws.con[j];
+      float pv[K];
+      if (PERIODIC) {
+        const float4 r = ws.raw[j];
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+          float dx, dy;
+          boundary_delta<true>(pxc, pyc[k], g.x, g.y, r.x, r.y, r.z, f, &dx, &dy);
+          pv[k] = fmaf(g.z * dx, dx, fmaf(g.w * dx, dy, fmaf(c.x * dy, dy, c.y)));
+        }
+      } else {
+        // The lane's pixels share dx and the x-only terms of the quadratic.
+        const float dx = pxc - g.x;
+        const float bdx = g.w * dx, xx = fmaf(g.z * dx, dx, c.y);
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+          const float dy = pyc[k] - g.y;
+          pv[k] = fmaf(fmaf(c.x, dy, bdx), dy, xx);
+        }
+      }
+      if (!STATS) {
+        // Branch-free: a pixel below the threshold (or done) blends alpha
+        // 2^-inf = +0, which leaves its colour, depth and transmittance
+        // exactly unchanged (t * 0 = 0, x + c * 0 = x for finite c).
+        const float4 col = ws.col[j];
+#pragma unroll
+        for (int k = 0; k < K; k += 2) {
+          const float q0 = pv[k] >= th[k] ? pv[k] : -__int_as_float(0x7f800000);
+          const float q1 = pv[k + 1] >= th[k + 1] ? pv[k + 1] : -__int_as_float(0x7f800000);
+          float2 al;
+          if (HALF) {
+            const uint32_t lim_bits = __float_as_uint(c.z);
+            al = __half22float2(
+                h2ex2_approx(__hmin2(__floats2half2_rn(q0, q1), *reinterpret_cast<const __half2*>(&lim_bits))));
+          } else {
+            al.x = ex2_approx(fminf(q0, c.z));
+            al.y = ex2_approx(fminf(q1, c.z));
+          }
+          blend_pixel<DEPTH>(al.x, col, c.w, acc[k]);
+          blend_pixel<DEPTH>(al.y, col, c.w, acc[k + 1]);
+        }
+        continue;
+      }
+      const float4 col = ws.col[j];
+#pragma unroll
+      for (int k = 0; k < K; k += 2) {
+        const bool use0 = pv[k] >= th[k];
+        const bool use1 = pv[k + 1] >= th[k + 1];
+        if (!(use0 || use1)) continue;
+        float2 al;
+        if (HALF) {
+          const uint32_t lim_bits = __float_as_uint(c.z);
+          al = __half22float2(h2ex2_approx(
+              __hmin2(__floats2half2_rn(pv[k], pv[k + 1]), *reinterpret_cast<const __half2*>(&lim_bits))));
+        } else {
+          al.x = ex2_approx(fminf(pv[k], c.z));
+          al.y = ex2_approx(fminf(pv[k + 1], c.z));
+        }
+        if (use0) {
+          blend_pixel<DEPTH>(al.x, col, c.w, acc[k]);
+          ++cnt[k].blended;
+          if (acc[k].t < f.t_threshold && stop[k] == s1) stop[k] = b + ws.idx[j] + 1;
+        }
+        if (use1) {
+          blend_pixel<DEPTH>(al.y, col, c.w, acc[k + 1]);
+          ++cnt[k + 1].blended;
+          if (acc[k + 1].t < f.t_threshold && stop[k + 1] == s1) stop[k + 1] = b + ws.idx[j] + 1;
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < K; ++k) done[k] = done[k] || acc[k].t < f.t_threshold;
+    __syncwarp();  // the staging area is rewritten by the next group
+  }
+#pragma unroll
+  for (int k = 0; k < K; ++k)
+    if (counting[k]) cnt[k].checked += stop[k] - s0;
+}
+
 __device__ __forceinline__ void store_pixel(const ViewDesc& v, const PassOptions& o, uint32_t px, uint32_t py,
                                             const PixelAcc& a) {
   const uint32_t W = (uint32_t)v.vw;
@@ -331,6 +494,122 @@ __global__ void __launch_bounds__(h2_threads<TILE>(), h2_min_blocks<HALF, TILE>(
   if (active1) store_pixel(v, o, px, py1, a1);
 }
 
+// The rasterizer with K pixels per lane (the other block shape of the fast
+// forms): threads of the block for a TILE x TILE tile, one warp per 8 x 4K
+// patch.
+template <int TILE, int K>
+constexpr int hk_threads() {
+  return 32 * (TILE / 8) * (TILE / (4 * K));
+}
+// Resident blocks per SM the register budget is set for: 768 threads per SM
+// (the K accumulators need more registers than k_raster_h2's pair).
+template <bool HALF, int TILE, int K>
+constexpr int hk_threads_per_sm() {
+  return 768;
+}
+template <bool HALF, int TILE, int K>
+constexpr int hk_min_blocks() {
+  return hk_threads_per_sm<HALF, TILE, K>() / hk_threads<TILE, K>() > 32
+             ? 32
+             : hk_threads_per_sm<HALF, TILE, K>() / hk_threads<TILE, K>();
+}
+
+template <bool HALF, bool PERIODIC, bool STATS, bool DEPTH, int TILE, int K>
+__global__ void __launch_bounds__(hk_threads<TILE, K>(), hk_min_blocks<HALF, TILE, K>())
+    k_raster_hk(const uint32_t* __restrict__ tile_offsets, const uint32_t* __restrict__ order,
+                const uint32_t* __restrict__ ids, const float4* __restrict__ mean, const float4* __restrict__ color,
+                const float4* __restrict__ rec, BatchView bv, PassOptions o, Control* __restrict__ ctl) {
+  if (ctl->state[3] != 0u) return;  // overflow: nothing is published
+  constexpr uint32_t PW = TILE / 8;             // patches per tile row
+  constexpr uint32_t PH = TILE / (4 * K);       // patch rows per tile
+  __shared__ WarpStage s_stage[PW * PH];
+  __shared__ uint32_t s_view;
+  __shared__ unsigned long long s_stats[4];
+  const uint32_t tile = order ? order[blockIdx.x] : blockIdx.x;
+  if (threadIdx.x == 0) s_view = find_view(bv.tile_base, bv.nviews, tile);
+  if (STATS && threadIdx.x < 4) s_stats[threadIdx.x] = 0ull;
+  __syncthreads();
+  const ViewDesc& v = bv.views[s_view];
+  const RasterFrame f = {v.vw, v.vh, o.t_threshold, o.axis};
+  const uint32_t local = tile - v.tile_base;
+  const uint32_t tx = local % v.tiles_x, ty = local / v.tiles_x;
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+  WarpStage& ws = s_stage[warp];
+  const uint32_t patch_x = tx * TILE + 8u * (warp % PW), patch_y = ty * TILE + 4u * K * (warp / PW);
+  const uint32_t px = patch_x + morton_compact(lane);
+  const uint32_t py0 = patch_y + morton_compact(lane >> 1);
+  const uint32_t W = (uint32_t)v.vw, H = (uint32_t)v.vh;
+  bool active[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) active[k] = px < W && py0 + 4u * k < H;
+  const uint32_t begin = tile_offsets[tile], end = tile_offsets[tile + 1];
+  const uint32_t source_count = end - begin;
+  const bool capped = o.max_per_tile != 0u;
+  const uint32_t raster_count = capped ? min(source_count, o.max_per_tile) : source_count;
+  const uint32_t chunk = o.chunk;
+  const bool chunked = chunk != 0u && raster_count > chunk;
+  const bool need_depth = v.depth != nullptr;
+  const float pxc = (float)px + 0.5f, pyc0 = (float)py0 + 0.5f;
+  PixelAcc a[K];
+  RasterCounters n[K];
+  bool fin[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    a[k] = {0.0f, 0.0f, 0.0f, 1.0f, 0.0f};
+    n[k] = {0u, 0u};
+    fin[k] = !active[k];
+  }
+  if (!chunked) {
+    blend_range_hk<HALF, PERIODIC, STATS, DEPTH, K>(begin, source_count, raster_count, 0, raster_count, capped, ids,
+                                                    mean, color, rec, need_depth, f, (float)patch_x, (float)patch_y,
+                                                    pxc, pyc0, fin, a, ws, n);
+  } else {
+    const uint32_t nchunk = (raster_count + chunk - 1) / chunk;
+    for (uint32_t ch = 0; ch < nchunk; ++ch) {
+      bool all = true;
+#pragma unroll
+      for (int k = 0; k < K; ++k) all = all && fin[k];
+      if (__all_sync(0xffffffffu, all)) break;
+      const uint32_t s0 = ch * chunk, s1 = min(s0 + chunk, raster_count);
+      PixelAcc p[K];
+      bool pfin[K];
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        p[k] = {0.0f, 0.0f, 0.0f, 1.0f, 0.0f};
+        pfin[k] = fin[k];
+      }
+      blend_range_hk<HALF, PERIODIC, STATS, DEPTH, K>(begin, source_count, raster_count, s0, s1, capped, ids, mean,
+                                                      color, rec, need_depth, f, (float)patch_x, (float)patch_y, pxc,
+                                                      pyc0, pfin, p, ws, n);
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        if (fin[k]) continue;
+        a[k].r = a[k].r + p[k].r * a[k].t; a[k].g = a[k].g + p[k].g * a[k].t; a[k].b = a[k].b + p[k].b * a[k].t;
+        a[k].d = a[k].d + p[k].d * a[k].t; a[k].t = a[k].t * p[k].t;
+        if (a[k].t < f.t_threshold) fin[k] = true;
+      }
+    }
+  }
+  if (STATS) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      if (active[k]) {
+        atomicAdd(&s_stats[0], (unsigned long long)n[k].checked);
+        atomicAdd(&s_stats[1], (unsigned long long)n[k].blended);
+        if (raster_count > 0) {
+          atomicAdd(&s_stats[2], 1ull);
+          if (a[k].t < f.t_threshold) atomicAdd(&s_stats[3], 1ull);
+        }
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x < 4 && s_stats[threadIdx.x]) atomicAdd(&ctl->raster_stats[threadIdx.x], s_stats[threadIdx.x]);
+  }
+#pragma unroll
+  for (int k = 0; k < K; ++k)
+    if (active[k]) store_pixel(v, o, px, py0 + 4u * k, a[k]);
+}
+
 // half = true: packed half2 form; false: FP32 form. o.any_depth: some view
 // of the launch has a depth target.
 template <bool HALF, bool PERIODIC, int TILE>
@@ -349,14 +628,37 @@ inline void launch_raster_pairs_tile(const uint32_t* tile_offsets, const uint32_
 #undef GS_RASTER_H2
 }
 
+template <bool HALF, bool PERIODIC, int TILE, int K>
+inline void launch_raster_k_tile(const uint32_t* tile_offsets, const uint32_t* order, const uint32_t* ids,
+                                 const float4* mean, const float4* color, const float4* rec, const BatchView& b,
+                                 const PassOptions& o, Control* ctl, bool stats, cudaStream_t st) {
+#define GS_RASTER_HK(S, D)                                                                          \
+  k_raster_hk<HALF, PERIODIC, S, D, TILE, K><<<b.total_tiles, hk_threads<TILE, K>(), 0, st>>>(      \
+      tile_offsets, order, ids, mean, color, rec, b, o, ctl)
+  const bool depth = o.any_depth != 0u;
+  if (stats) {
+    if (depth) GS_RASTER_HK(true, true); else GS_RASTER_HK(true, false);
+  } else {
+    if (depth) GS_RASTER_HK(false, true); else GS_RASTER_HK(false, false);
+  }
+#undef GS_RASTER_HK
+}
+
 template <bool HALF, bool PERIODIC>
 inline void launch_raster_pairs_t(const uint32_t* tile_offsets, const uint32_t* order, const uint32_t* ids,
                                   const float4* mean, const float4* color, const float4* rec, const BatchView& b,
                                   const PassOptions& o, Control* ctl, bool stats, cudaStream_t st) {
+  // Four pixels per lane (one warp per 8x16 patch) where the tile holds such
+  // patches; otherwise two (one warp per 8x8 patch).
+  const bool four = o.pixels_per_lane == 4u && o.tile >= 16u;
   if (o.tile == 8u)
     launch_raster_pairs_tile<HALF, PERIODIC, 8>(tile_offsets, order, ids, mean, color, rec, b, o, ctl, stats, st);
+  else if (o.tile == 32u && four)
+    launch_raster_k_tile<HALF, PERIODIC, 32, 4>(tile_offsets, order, ids, mean, color, rec, b, o, ctl, stats, st);
   else if (o.tile == 32u)
     launch_raster_pairs_tile<HALF, PERIODIC, 32>(tile_offsets, order, ids, mean, color, rec, b, o, ctl, stats, st);
+  else if (four)
+    launch_raster_k_tile<HALF, PERIODIC, 16, 4>(tile_offsets, order, ids, mean, color, rec, b, o, ctl, stats, st);
   else
     launch_raster_pairs_tile<HALF, PERIODIC, 16>(tile_offsets, order, ids, mean, color, rec, b, o, ctl, stats, st);
 }

@@ -50,6 +50,8 @@ def parse():
                     help="fixed launch shape for the batched form instead of the autotuner's")
     ap.add_argument("--tile-size", type=int, default=None, choices=[8, 16, 32],
                     help="fixed tile size for the batched form instead of the autotuner's")
+    ap.add_argument("--pixels-per-lane", type=int, default=None, choices=[2, 4],
+                    help="fixed raster block shape for the batched form instead of the autotuner's")
     ap.add_argument("--forms", default="all", choices=["all", "batched"],
                     help="'batched' skips the timed plain (one view per launch) form")
     ap.add_argument("--serve", action="store_true", help="serving-loop measurement (configuration 4)")
@@ -549,6 +551,8 @@ def main() -> None:
         _, tune_ms = batched.autotune(views, trials=3)
     if args.tile_size is not None:
         batched.set_tuning({"tile_size": args.tile_size})
+    if args.pixels_per_lane is not None:
+        batched.set_tuning({"raster_pixels_per_lane": args.pixels_per_lane})
     tuning = batched.get_tuning()
     batched.render_batch(views)  # size the workspaces, then capture the pass as a graph
     torch.cuda.synchronize()

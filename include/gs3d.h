@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define GS3D_ABI_VERSION 3u
+#define GS3D_ABI_VERSION 4u
 
 typedef enum gs3d_status {
   GS3D_OK = 0,
@@ -251,20 +251,28 @@ typedef struct gs3d_view {
  * tile, and the visible set, by splats that reach a tile only where it
  * extends past the image edge (they cover no pixel). Single-view
  * gs3d_pipeline_render always uses 16.
+ * raster_pixels_per_lane: the FP32 and half2 rasterizers' block shape, 2 (a
+ * warp per 8x8 patch of the tile, each lane two pixels of one column) or 4
+ * (a warp per 8x16 patch, half the warps per tile; 8-pixel tiles keep 2);
+ * 0 = 2. The EXACT form has one thread per pixel. The image of the fast
+ * forms stays within their tolerance (their transmittance test runs per
+ * group of 32 records of a warp's walk, which the patch regroups).
  * Setting a tuning releases captured graphs. */
 typedef struct gs3d_tuning {
-  uint32_t views_per_launch; /* default 0 */
-  uint32_t tile_digit_bits;  /* default 8 */
-  uint32_t work_order;       /* default 1 */
-  uint32_t tile_size;        /* default 0 (16) */
+  uint32_t views_per_launch;       /* default 0 */
+  uint32_t tile_digit_bits;        /* default 8 */
+  uint32_t work_order;             /* default 1 */
+  uint32_t tile_size;              /* default 0 (16) */
+  uint32_t raster_pixels_per_lane; /* default 0 (2) */
+  uint32_t reserved[3];
 } gs3d_tuning;
 
 gs3d_status gs3d_pipeline_set_tuning(gs3d_pipeline* pipeline, const gs3d_tuning* tuning);
 gs3d_status gs3d_pipeline_get_tuning(gs3d_pipeline* pipeline, gs3d_tuning* tuning);
 
 /* Times the batch under candidate tunings (coordinate descent: tile size 8
- * and 32 against 16, views per launch halving from the batch size, tile
- * digit width 7..4, then the work order; `trials` timed batches each after
+ * and 32 against 16, four pixels per lane against two, views per launch
+ * halving from the batch size, tile digit width 7..4, then the work order; `trials` timed batches each after
  * one untimed one), keeps the fastest and returns it with its milliseconds
  * per batch. The views' targets receive the renders. GS3D_ERROR_RANGE if the
  * intersection capacity cannot hold the batch at 16-pixel tiles; a tile size

@@ -149,3 +149,63 @@ def test_invalid_tile_size_is_rejected():
     pipe.set_tuning({"tile_size": 0})
     assert pipe.get_tuning()["tile_size"] == 16
     pipe.dispose()
+
+
+@pytest.mark.parametrize("precision", ["half2", "fp32"])
+@pytest.mark.parametrize("name", ["default", "repeat_y", "chunked", "capped", "background_depth_raw"])
+def test_four_pixels_per_lane(precision, name):
+    # The fast rasterizers' other block shape (a warp per 8x16 patch, four
+    # pixels per lane): the image stays within the fast forms' tolerance of
+    # the two-pixel shape and of the oracle, at 16- and 32-pixel tiles (16
+    # only where a per-tile cap applies).
+    pairs = batch_of(name)
+    ref, _ = render_batch(pairs, precision, share_scenes=True)
+    # maxRasterizedSplatsPerTile acts per tile: the capped case keeps 16.
+    for tile in ((16,) if name == "capped" else (16, 32)):
+        got, _ = render_batch(pairs, precision, share_scenes=True,
+                              tuning={"tile_size": tile, "raster_pixels_per_lane": 4})
+        for (scene, frame), g, r in zip(pairs, got, ref):
+            o = oracle.render(scene, frame, 0)
+            o64 = oracle.render(scene, frame, 1)
+            assert np.abs(g["rgba"] - r["rgba"]).max() <= 2e-2, tile
+            assert np.abs(g["rgba"] - o["rgba"]).max() <= 2e-2, tile
+            assert psnr(g["rgba"][..., :3], o64["rgba"][..., :3]) >= 50.0, tile
+            if name == "background_depth_raw":
+                finite = np.isfinite(r["depth"]) & np.isfinite(g["depth"])
+                assert np.abs(g["depth"][finite] - r["depth"][finite]).max() <= 2e-2 * max(1.0, np.abs(r["depth"][finite]).max())
+
+
+def test_four_pixels_per_lane_counts_the_same_work():
+    # rasterStats with the other block shape: the same pixels, and the
+    # checked / blended samples within the regrouping of the transmittance
+    # test (at most 31 records per pixel past the exact stop).
+    import torch
+    dev = importlib.import_module(PKG_NAME + ".device")
+    scene, frame = CASES["default"]()
+    ds = dev.DeviceScene(scene)
+    W, H = int(frame["width"]), int(frame["height"])
+    out = {}
+    for ppl in (2, 4):
+        pipe = P.TiledGaussianPipeline(ds.data(), {"raster_precision": "half2", "raster_stats": True,
+                                                   "intersection_capacity": 1 << 20})
+        pipe.set_tuning({"raster_pixels_per_lane": ppl})
+        color = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+        pipe.render_batch([(ds.data(), P.make_camera(frame), W, H, color.data_ptr(), 0, "rgba32f")])
+        out[ppl] = pipe.read_stats()["rasterWork"]
+        pipe.dispose()
+    assert out[4]["pixels"] == out[2]["pixels"] > 0
+    for k in ("checked", "blended"):
+        assert abs(out[4][k] - out[2][k]) <= 31 * out[2]["pixels"], k
+        assert out[4][k] > 0
+
+
+def test_invalid_pixels_per_lane_is_rejected():
+    dev = importlib.import_module(PKG_NAME + ".device")
+    ds = dev.DeviceScene(sc.uniform_cloud(1000, seed=84))
+    pipe = P.TiledGaussianPipeline(ds.data(), {"intersection_capacity": 1 << 16})
+    for bad in (1, 3, 8):
+        with pytest.raises(ValueError):
+            pipe.set_tuning({"raster_pixels_per_lane": bad})
+    pipe.set_tuning({"raster_pixels_per_lane": 0})
+    assert pipe.get_tuning()["raster_pixels_per_lane"] == 2
+    pipe.dispose()
