@@ -23,11 +23,14 @@
 // so alpha = min(opacity e^power, 0.99) = 2^min(p', L), L = min(log2 opacity,
 // log2 0.99), and the reference's alpha >= 1/255 test is p' >= log2(1/255).
 // Per record and pixel pair:
-//   FP32   dx, dy0, dy1, p'0, p'1 and the two threshold compares
-//   half2 form: min(p', L) and its exp2 in one ex2.approx.f16x2, colour from
-//               the record's f16 values
-//   FP32 form:  min(p', L) and exp2 per pixel (ex2.approx.f32), FP32 colour
-//   FP32   transmittance and colour/depth accumulation
+//   half2 form: p'0 and p'1 in packed half2 from the record's Cholesky
+//               factor (cholesky_record below: five HFMA2), the threshold
+//               compare, min(p', log2 0.99) and exp2 in packed half2 too
+//               (ex2.approx.f16x2), colour from the record's f16 values;
+//               the periodic-boundary variant evaluates p' in FP32
+//   FP32 form:  dx, dy0, dy1, p'0, p'1, the compares, min(p', L) and exp2
+//               per pixel (ex2.approx.f32), FP32 colour
+//   both:       FP32 transmittance and colour/depth accumulation
 // A pixel's transmittance is tested against the threshold once per group of
 // 32 records; a pixel found done stops blending from there on (its threshold
 // becomes +inf), so it may blend up to 31 records more than the reference,
@@ -47,11 +50,64 @@ __device__ __forceinline__ __half2 h2ex2_approx(__half2 x) {
   return *reinterpret_cast<__half2*>(&out);
 }
 
+__device__ __forceinline__ __half2 u2h2(uint32_t u) { return *reinterpret_cast<const __half2*>(&u); }
+__device__ __forceinline__ uint32_t h22u(__half2 h) { return *reinterpret_cast<const uint32_t*>(&h); }
+
+// The half2 form's per-pixel evaluation. With M = [[a, b], [b, c]] log2(e)/2
+// (the record's conic, positive definite) and its Cholesky factor
+// M = L L^T, L = [[l11, 0], [l21, l22]], the exponent of a pixel at offset
+// d from the splat centre is
+//   p' = log2(opacity) - d^T M d = log2(opacity) - w1^2 - w2^2,
+//   w1 = l11 dx + l21 dy,  w2 = l22 dy.
+// Per record and warp patch the FP32 staging step evaluates w at the
+// patch centre e (offset d_e); a pixel at e + u then has
+//   w1 = w1(e) + l11 ux + l21 uy,  w2 = w2(e) + l22 uy
+// with |ux|, |uy| <= 3.5 (exact in f16), so the per-pixel work is five
+// packed half2 FMAs for two pixels. In this form no intermediate cancels:
+// |w| stays near the square root of the exponent, where the expanded
+// quadratic (a dx^2 + 2 b dx dy + c dy^2) would round its large, opposite
+// terms for a long, tilted splat. And p' <= log2(opacity) after rounding too
+// (subtracting squares), so alpha = 2^min(p', log2 0.99) needs no per-record
+// limit.
+// Words: (l11, l21), (w1(e), w2(e)), (l22, log2 opacity), unused. The factor
+// is stored in f16, so approximate reciprocal square roots (2 ulp in FP32)
+// suffice. A degenerate record (m00 or the Schur complement not positive,
+// which a valid projection does not produce) gets a tiny floor instead; its
+// exponent may then overflow to -inf or NaN, and either blends nothing.
+__device__ __forceinline__ uint4 cholesky_record(const float4& r0, const float4& r1, float ex, float ey) {
+  const float m00 = fmaxf(-r0.z, 1e-30f), m01 = -0.5f * r0.w, m11 = -r1.x;
+  const float r = rsqrtf(m00);
+  const float l11 = m00 * r, l21 = m01 * r;
+  const float s = fmaxf(fmaf(-l21, l21, m11), 1e-30f);
+  const float l22 = s * rsqrtf(s);
+  const float dx = ex - r0.x, dy = ey - r0.y;
+  const float w1 = fmaf(l11, dx, l21 * dy), w2 = l22 * dy;
+  return make_uint4(h22u(__floats2half2_rn(l11, l21)), h22u(__floats2half2_rn(w1, w2)),
+                    h22u(__floats2half2_rn(l22, r1.y)), 0u);
+}
+
+// Alpha of the lane's two pixels from the Cholesky record: 2^min(p', L) where
+// p' >= the pixel's threshold (log2(1/255), or +inf once the pixel is done),
+// else +0 (a NaN exponent fails the compare and blends +0 too).
+__device__ __forceinline__ float2 cholesky_alpha(const uint4& h, __half2 ux, __half2 uy, __half2 th,
+                                                 uint32_t* use_mask) {
+  const __half2 h0 = u2h2(h.x), h1 = u2h2(h.y), h2 = u2h2(h.z);
+  const __half2 t = __hfma2(__low2half2(h0), ux, __low2half2(h1));
+  const __half2 w1 = __hfma2(__high2half2(h0), uy, t);
+  const __half2 w2 = __hfma2(__low2half2(h2), uy, __high2half2(h1));
+  __half2 p = __hfma2(__hneg2(w1), w1, __high2half2(h2));
+  p = __hfma2(__hneg2(w2), w2, p);
+  const uint32_t m = __hge2_mask(p, th);
+  *use_mask = m;
+  const uint32_t q = (h22u(p) & m) | (0xFC00FC00u & ~m);  // -inf where unused
+  return __half22float2(h2ex2_approx(__hmin2(u2h2(q), __float2half2_rn(kLog2MaxAlpha))));
+}
+
 // One warp's staged records (up to 32, compacted in record order).
 struct WarpStage {
-  float4 geo[32];  // cx, cy, -a/2 log2 e, -b log2 e
+  float4 geo[32];  // cx, cy, -a/2 log2 e, -b log2 e (the half2 form: its Cholesky record)
   float4 con[32];  // -c/2 log2 e, log2 opacity, L as half2 bits, depth
-  float4 col[32];
+  float4 col[32];  // r, g, b (the half2 form: and depth)
   float4 raw[32];  // conic (a, b, c) for periodic boundaries
   uint8_t idx[32]; // lane (record offset within the group) of each staged record
 };
@@ -84,6 +140,11 @@ __device__ __forceinline__ void blend_range_h2(uint32_t begin, uint32_t source_c
   uint32_t stop0 = s1, stop1 = s1;
   const float pyc1 = pyc0 + 4.0f;
   const uint32_t lt = (1u << lane) - 1u;
+  // The half2 form's Cholesky evaluation: the pixels' offsets from the patch
+  // centre (multiples of 0.5 within +-3.5, exact in f16).
+  constexpr bool kChol = HALF && !PERIODIC;
+  const float ecx = patch_x0 + 4.0f, ecy = patch_y0 + 4.0f;
+  const __half2 ux2 = __float2half2_rn(pxc - ecx), uy2 = __floats2half2_rn(pyc0 - ecy, pyc1 - ecy);
   auto load_id = [&](uint32_t i) -> uint32_t {
     if (i >= s1) return 0u;
     uint32_t src = i;
@@ -91,7 +152,7 @@ __device__ __forceinline__ void blend_range_h2(uint32_t begin, uint32_t source_c
     return __ldg(ids + begin + src);
   };
   // The FP32 form loads the next group's record ids one group ahead (the
-  // half2 form, at its register limit for 9 blocks per SM, is faster without).
+  // half2 form, at its register limit for 10 blocks per SM, is faster without).
   uint32_t next_id = HALF ? 0u : load_id(s0 + lane);
   for (uint32_t b = s0; b < s1; b += 32) {
     if (__all_sync(0xffffffffu, done0 && done1)) break;
@@ -116,17 +177,23 @@ __device__ __forceinline__ void blend_range_h2(uint32_t begin, uint32_t source_c
     const uint32_t bal = __ballot_sync(0xffffffffu, reach);
     if (reach) {
       const uint32_t q = __popc(bal & lt);
-      ws.geo[q] = r0;
-      if (HALF) {
-        const uint32_t rg_bits = __float_as_uint(r1.z), bl_bits = __float_as_uint(r1.w);
-        const float2 rg = __half22float2(*reinterpret_cast<const __half2*>(&rg_bits));
-        const __half2 bl = *reinterpret_cast<const __half2*>(&bl_bits);
-        const __half2 lim = __half2half2(__high2half(bl));
-        ws.con[q] = make_float4(r1.x, r1.y, __uint_as_float(*reinterpret_cast<const uint32_t*>(&lim)), depth);
-        ws.col[q] = make_float4(rg.x, rg.y, __low2float(bl), 0.0f);
+      if (kChol) {
+        *reinterpret_cast<uint4*>(&ws.geo[q]) = cholesky_record(r0, r1, ecx, ecy);
+        const float2 rg = __half22float2(u2h2(__float_as_uint(r1.z)));
+        ws.col[q] = make_float4(rg.x, rg.y, __low2float(u2h2(__float_as_uint(r1.w))), depth);
       } else {
-        ws.con[q] = make_float4(r1.x, r1.y, fminf(r1.y, kLog2MaxAlpha), depth);
-        ws.col[q] = col32;
+        ws.geo[q] = r0;
+        if (HALF) {
+          const uint32_t rg_bits = __float_as_uint(r1.z), bl_bits = __float_as_uint(r1.w);
+          const float2 rg = __half22float2(*reinterpret_cast<const __half2*>(&rg_bits));
+          const __half2 bl = *reinterpret_cast<const __half2*>(&bl_bits);
+          const __half2 lim = __half2half2(__high2half(bl));
+          ws.con[q] = make_float4(r1.x, r1.y, __uint_as_float(*reinterpret_cast<const uint32_t*>(&lim)), depth);
+          ws.col[q] = make_float4(rg.x, rg.y, __low2float(bl), 0.0f);
+        } else {
+          ws.con[q] = make_float4(r1.x, r1.y, fminf(r1.y, kLog2MaxAlpha), depth);
+          ws.col[q] = col32;
+        }
       }
       if (PERIODIC) ws.raw[q] = raw_conic(r0, r1);
       if (STATS) ws.idx[q] = (uint8_t)lane;
@@ -135,6 +202,34 @@ __device__ __forceinline__ void blend_range_h2(uint32_t begin, uint32_t source_c
     const uint32_t n = __popc(bal);
     const float th0 = done0 ? __int_as_float(0x7f800000) : kLog2MinAlpha;
     const float th1 = done1 ? __int_as_float(0x7f800000) : kLog2MinAlpha;
+    if (kChol) {
+      const __half2 th2 = __floats2half2_rn(th0, th1);
+      for (uint32_t j = 0; j < n; ++j) {
+        uint32_t m;
+        const float2 al = cholesky_alpha(*reinterpret_cast<const uint4*>(&ws.geo[j]), ux2, uy2, th2, &m);
+        const float4 col = ws.col[j];  // r, g, b, depth
+        if (!STATS) {
+          // Unused pixels blend alpha +0, which changes nothing.
+          blend_pixel<DEPTH>(al.x, col, col.w, a0);
+          blend_pixel<DEPTH>(al.y, col, col.w, a1);
+          continue;
+        }
+        if (m & 0xFFFFu) {
+          blend_pixel<DEPTH>(al.x, col, col.w, a0);
+          ++c0n.blended;
+          if (a0.t < f.t_threshold && stop0 == s1) stop0 = b + ws.idx[j] + 1;
+        }
+        if (m >> 16) {
+          blend_pixel<DEPTH>(al.y, col, col.w, a1);
+          ++c1n.blended;
+          if (a1.t < f.t_threshold && stop1 == s1) stop1 = b + ws.idx[j] + 1;
+        }
+      }
+      done0 = done0 || a0.t < f.t_threshold;
+      done1 = done1 || a1.t < f.t_threshold;
+      __syncwarp();  // the staging area is rewritten by the next group
+      continue;
+    }
     for (uint32_t j = 0; j < n; ++j) {
       const float4 g = ws.geo[j];
       const float4 c = ws.con[j];
@@ -233,6 +328,14 @@ __device__ __forceinline__ void blend_range_hk(uint32_t begin, uint32_t source_c
     pyc[k] = pyc0 + 4.0f * (float)k;
   }
   const uint32_t lt = (1u << lane) - 1u;
+  // The half2 form's Cholesky evaluation about the 8 x 4K patch's centre
+  // (offsets within +-3.5 in x and +-(2K - 0.5) in y, exact in f16).
+  constexpr bool kChol = HALF && !PERIODIC;
+  const float ecx = patch_x0 + 4.0f, ecy = patch_y0 + 2.0f * (float)K;
+  const __half2 ux2 = __float2half2_rn(pxc - ecx);
+  __half2 uy2[K / 2];
+#pragma unroll
+  for (int k = 0; k < K; k += 2) uy2[k / 2] = __floats2half2_rn(pyc[k] - ecy, pyc[k + 1] - ecy);
   auto load_id = [&](uint32_t i) -> uint32_t {
     if (i >= s1) return 0u;
     uint32_t src = i;
@@ -246,7 +349,7 @@ __device__ __forceinline__ void blend_range_hk(uint32_t begin, uint32_t source_c
     return d;
   };
   // The FP32 form loads the next group's record ids one group ahead (the
-  // half2 form, at its register limit for 9 blocks per SM, is faster without).
+  // half2 form, at its register limit, is faster without).
   uint32_t next_id = HALF ? 0u : load_id(s0 + lane);
   for (uint32_t b = s0; b < s1; b += 32) {
     if (__all_sync(0xffffffffu, all_done())) break;
@@ -271,17 +374,23 @@ __device__ __forceinline__ void blend_range_hk(uint32_t begin, uint32_t source_c
     const uint32_t bal = __ballot_sync(0xffffffffu, reach);
     if (reach) {
       const uint32_t q = __popc(bal & lt);
-      ws.geo[q] = r0;
-      if (HALF) {
-        const uint32_t rg_bits = __float_as_uint(r1.z), bl_bits = __float_as_uint(r1.w);
-        const float2 rg = __half22float2(*reinterpret_cast<const __half2*>(&rg_bits));
-        const __half2 bl = *reinterpret_cast<const __half2*>(&bl_bits);
-        const __half2 lim = __half2half2(__high2half(bl));
-        ws.con[q] = make_float4(r1.x, r1.y, __uint_as_float(*reinterpret_cast<const uint32_t*>(&lim)), depth);
-        ws.col[q] = make_float4(rg.x, rg.y, __low2float(bl), 0.0f);
+      if (kChol) {
+        *reinterpret_cast<uint4*>(&ws.geo[q]) = cholesky_record(r0, r1, ecx, ecy);
+        const float2 rg = __half22float2(u2h2(__float_as_uint(r1.z)));
+        ws.col[q] = make_float4(rg.x, rg.y, __low2float(u2h2(__float_as_uint(r1.w))), depth);
       } else {
-        ws.con[q] = make_float4(r1.x, r1.y, fminf(r1.y, kLog2MaxAlpha), depth);
-        ws.col[q] = col32;
+        ws.geo[q] = r0;
+        if (HALF) {
+          const uint32_t rg_bits = __float_as_uint(r1.z), bl_bits = __float_as_uint(r1.w);
+          const float2 rg = __half22float2(*reinterpret_cast<const __half2*>(&rg_bits));
+          const __half2 bl = *reinterpret_cast<const __half2*>(&bl_bits);
+          const __half2 lim = __half2half2(__high2half(bl));
+          ws.con[q] = make_float4(r1.x, r1.y, __uint_as_float(*reinterpret_cast<const uint32_t*>(&lim)), depth);
+          ws.col[q] = make_float4(rg.x, rg.y, __low2float(bl), 0.0f);
+        } else {
+          ws.con[q] = make_float4(r1.x, r1.y, fminf(r1.y, kLog2MaxAlpha), depth);
+          ws.col[q] = col32;
+        }
       }
       if (PERIODIC) ws.raw[q] = raw_conic(r0, r1);
       if (STATS) ws.idx[q] = (uint8_t)lane;
@@ -291,6 +400,40 @@ __device__ __forceinline__ void blend_range_hk(uint32_t begin, uint32_t source_c
     float th[K];
 #pragma unroll
     for (int k = 0; k < K; ++k) th[k] = done[k] ? __int_as_float(0x7f800000) : kLog2MinAlpha;
+    if (kChol) {
+      __half2 th2[K / 2];
+#pragma unroll
+      for (int k = 0; k < K; k += 2) th2[k / 2] = __floats2half2_rn(th[k], th[k + 1]);
+      for (uint32_t j = 0; j < n; ++j) {
+        const uint4 h = *reinterpret_cast<const uint4*>(&ws.geo[j]);
+        const float4 col = ws.col[j];  // r, g, b, depth
+#pragma unroll
+        for (int k = 0; k < K; k += 2) {
+          uint32_t m;
+          const float2 al = cholesky_alpha(h, ux2, uy2[k / 2], th2[k / 2], &m);
+          if (!STATS) {
+            // Unused pixels blend alpha +0, which changes nothing.
+            blend_pixel<DEPTH>(al.x, col, col.w, acc[k]);
+            blend_pixel<DEPTH>(al.y, col, col.w, acc[k + 1]);
+            continue;
+          }
+          if (m & 0xFFFFu) {
+            blend_pixel<DEPTH>(al.x, col, col.w, acc[k]);
+            ++cnt[k].blended;
+            if (acc[k].t < f.t_threshold && stop[k] == s1) stop[k] = b + ws.idx[j] + 1;
+          }
+          if (m >> 16) {
+            blend_pixel<DEPTH>(al.y, col, col.w, acc[k + 1]);
+            ++cnt[k + 1].blended;
+            if (acc[k + 1].t < f.t_threshold && stop[k + 1] == s1) stop[k + 1] = b + ws.idx[j] + 1;
+          }
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < K; ++k) done[k] = done[k] || acc[k].t < f.t_threshold;
+      __syncwarp();  // the staging area is rewritten by the next group
+      continue;
+    }
     for (uint32_t j = 0; j < n; ++j) {
       const float4 g = ws.geo[j];
       const float4 c = ws.con[j];
@@ -399,12 +542,13 @@ template <int TILE>
 constexpr int h2_threads() {
   return 32 * (TILE / 8) * (TILE / 8);
 }
-// Resident blocks per SM the register budget is set for: 9 blocks of 128
-// threads (half2) / 8 (FP32) at the reference's 16-pixel tiles, the same
-// threads per SM at other tile sizes (at most 32 blocks).
+// Resident blocks per SM the register budget is set for: 10 blocks of 128
+// threads (half2: 48 registers; 9 and 12 blocks measured slower) / 8 (FP32)
+// at the reference's 16-pixel tiles, the same threads per SM at other tile
+// sizes (at most 32 blocks).
 template <bool HALF, int TILE>
 constexpr int h2_min_blocks() {
-  return (HALF ? 1152 : 1024) / h2_threads<TILE>() > 32 ? 32 : (HALF ? 1152 : 1024) / h2_threads<TILE>();
+  return (HALF ? 1280 : 1024) / h2_threads<TILE>() > 32 ? 32 : (HALF ? 1280 : 1024) / h2_threads<TILE>();
 }
 
 template <bool HALF, bool PERIODIC, bool STATS, bool DEPTH, int TILE>
