@@ -63,10 +63,11 @@ typedef enum gs3d_boundary_policy {
 } gs3d_boundary_policy;
 /* Rasterizer arithmetic. FP32 is the reference's form. EXACT is FP32 with the
  * deterministic math library and no FMA contraction (bit-identical to the CPU
- * restatement). HALF2 keeps each pixel's quadratic and threshold test in FP32
- * and takes the alpha clamp and exp2 of a lane's two pixels in one packed
- * half2 instruction, with the colour stored in half; transmittance and colour
- * accumulation stay FP32. */
+ * restatement). HALF2 evaluates each pixel's Gaussian exponent in packed
+ * half2 (from the splat's Cholesky factor about the patch centre, two pixels
+ * per instruction), with its threshold test, alpha clamp and exp2, the colour
+ * stored in half; transmittance and colour accumulation stay FP32 (the
+ * periodic-boundary variant keeps the exponent in FP32). */
 /* Projection arithmetic. FP32 is the reference's (ProjectionStage.ts, bit-exact
  * with the CPU restatement). FP64 has no counterpart in the reference: it
  * evaluates the model-view mean transform in double (far-origin scenes) and
