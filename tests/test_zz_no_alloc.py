@@ -1,9 +1,9 @@
 """The allocation-free compaction entry point against the pipeline's own compaction.
 
 gs3d_compact_visible_static keeps its scratch in a static device array so that
-callers who cannot allocate device memory where they enqueue work (CUDA graph
-capture, hosts with their own memory arena, real-time loops) can still run the
-visibility compaction. Its outputs must equal what gs3d_pipeline_render's
+callers who cannot allocate device memory where they enqueue work (hosts with
+their own memory arena, real-time loops that must not stall on the allocator)
+can still run the visibility compaction. Its outputs must equal what gs3d_pipeline_render's
 compaction stage produced for the same frame, on two calls in a row (the
 second call finds the previous call's contents in the shared array).
 """
