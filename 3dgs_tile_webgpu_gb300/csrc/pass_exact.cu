@@ -68,15 +68,17 @@ __device__ __forceinline__ uint32_t bit_range(uint32_t s, uint32_t e) {
 // parameters of the tile test, the box, and the inclusive box-tile counts.
 struct CountShared {
   float f[8][kBlock / 32][32];     // cx, cy, conic a, b, c, threshold, rx, ry
-  uint32_t u[3][kBlock / 32][32];  // tminx, tminy, box width
+  uint32_t u[4][kBlock / 32][32];  // tminx, tminy, box width, box index of the centre tile (or ~0)
   uint32_t incl[kBlock / 32][32];
   uint32_t cnt[kBlock / 32][32];
 };
 
 // Counts the tiles of every lane's box that pass the reference's tile test,
 // with the warp's lanes spread over the union of the 32 boxes (32 box tiles
-// per round) instead of each lane walking its own box. Must be called by all
-// 32 lanes; a lane with nbox == 0 contributes nothing. Returns the lane's count.
+// per round) instead of each lane walking its own box. A lane walks nbox
+// tiles of its box in row-major order, skipping the box index u[3] (the
+// centre's tile, counted by the caller). Must be called by all 32 lanes; a
+// lane with nbox == 0 contributes nothing. Returns the lane's count.
 __device__ __forceinline__ uint32_t count_tiles_warp(CountShared& sm, uint32_t nbox, float vw, float vh,
                                                      uint32_t axis, float ts) {
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
@@ -100,7 +102,8 @@ __device__ __forceinline__ uint32_t count_tiles_warp(CountShared& sm, uint32_t n
     bool hit = false;
     if (valid) {
       const uint32_t bw = sm.u[2][warp][owner];
-      const uint32_t k = j - (owner ? sm.incl[warp][owner - 1] : 0u);
+      uint32_t k = j - (owner ? sm.incl[warp][owner - 1] : 0u);
+      k += k >= sm.u[3][warp][owner] ? 1u : 0u;
       const uint32_t by = k / bw, bx = k - by * bw;
       hit = boundary_tile_hit(sm.f[0][warp][owner], sm.f[1][warp][owner], sm.f[2][warp][owner],
                               sm.f[3][warp][owner], sm.f[4][warp][owner], sm.f[5][warp][owner],
@@ -164,7 +167,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_project(BatchView b, PassOptions 
     const float vw = v.vw, vh = v.vh;
     float4 mo4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     uint32_t cnt = 0, key = kInvisibleKey, nbox = 0;
-    bool single = false;
+    bool centre = false;
     Projected pr = {};
     float op = 0.0f, rx = 0.0f, ry = 0.0f, thr = 0.0f;
     f3 vdir = {0.0f, 0.0f, 0.0f};
@@ -252,12 +255,14 @@ __global__ void __launch_bounds__(kBlock, 4) k_project(BatchView b, PassOptions 
       if (o.axis == 2u) { tminy = 0; tmaxy = tiles_y - 1; }
       const uint32_t bw = (uint32_t)(tmaxx - tminx + 1);
       nbox = bw * (uint32_t)(tmaxy - tminy + 1);
-      // A box of one on-screen tile that no clamp touched holds the centre
-      // strictly inside that tile (rx, ry >= 1 and the floors of c - r and
-      // c + r agree), so the reference's tile test takes its centre-inside
-      // path and passes: the count is 1 without the walk.
-      single = o.axis == 0u && fx0 == fx1 && fy0 == fy1 && fx0 >= 0.0f && fx0 <= mtx && fy0 >= 0.0f &&
-               fy0 <= mty;
+      // The tile holding the centre, when it is on screen, lies in the box
+      // (the floors are monotone and rx, ry >= 1) and passes the reference's
+      // tile test by its centre-inside path (tileContribution.ts:16-59): it
+      // counts 1 without a test, and the warp walks the box's other tiles.
+      const float fcx = floorf(pr.cx * o.tile_inv), fcy = floorf(pr.cy * o.tile_inv);
+      centre = o.axis == 0u && fcx >= 0.0f && fcx <= mtx && fcy >= 0.0f && fcy <= mty;
+      s_count.u[3][warp][lane] =
+          centre ? ((uint32_t)fcy - (uint32_t)tminy) * bw + ((uint32_t)fcx - (uint32_t)tminx) : 0xffffffffu;
       s_count.f[0][warp][lane] = pr.cx; s_count.f[1][warp][lane] = pr.cy;
       s_count.f[2][warp][lane] = pr.conic_x; s_count.f[3][warp][lane] = pr.conic_y;
       s_count.f[4][warp][lane] = pr.conic_z; s_count.f[5][warp][lane] = thr;
@@ -266,8 +271,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_project(BatchView b, PassOptions 
       s_count.u[2][warp][lane] = bw;
     } while (false);
     // Tiles passing the tile test (projectionHelpers.ts:223-236), counted by the whole warp.
-    cnt = count_tiles_warp(s_count, single ? 0u : nbox, vw, vh, o.axis, o.tile_px);
-    if (single) cnt = 1u;
+    cnt = count_tiles_warp(s_count, centre ? nbox - 1u : nbox, vw, vh, o.axis, o.tile_px) + (centre ? 1u : 0u);
     if (cnt > 0) {
       uint32_t co[16];
       load_sh(v.sh + (size_t)slot * v.C, v.degree, co);
