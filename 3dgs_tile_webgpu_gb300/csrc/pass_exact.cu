@@ -45,10 +45,10 @@ template <bool FAST>
 __device__ __forceinline__ f3 eval_sh_any(uint32_t degree, const uint32_t* co, f3 d, const float* snorm) {
   if (FAST) {
     switch (degree) {
-      case 0: return eval_sh_fast<0>(co, d, snorm);
-      case 1: return eval_sh_fast<1>(co, d, snorm);
-      case 2: return eval_sh_fast<2>(co, d, snorm);
-      default: return eval_sh_fast<3>(co, d, snorm);
+      case 0: return eval_sh_fast<0>(co, d);
+      case 1: return eval_sh_fast<1>(co, d);
+      case 2: return eval_sh_fast<2>(co, d);
+      default: return eval_sh_fast<3>(co, d);
     }
   }
   switch (degree) {

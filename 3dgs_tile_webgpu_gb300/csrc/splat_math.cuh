@@ -342,46 +342,51 @@ __device__ __forceinline__ f3 eval_sh(const uint32_t* co, f3 d, const float* sno
 
 // The same SH colour for the fast raster forms, whose colour feeds only the
 // image (the EXACT form and the integer stages keep eval_sh): each
-// coefficient's rgb8e8 scale 2^e is folded into its basis weight once and the
-// sum runs as fused multiply-adds from the +0.5 offset. The result differs
-// from eval_sh by the rounding of the reordered sum (a few ulps of the
-// colour), and is clamped to [0, 1] the same way.
+// coefficient's rgb8e8 scale 2^(e - 127) is the float whose exponent field is
+// e (e = 0, a scale of 2^-127, becomes 0: far below a colour's resolution;
+// e = 255 is +inf either way), each signed byte converts directly, and the
+// 1/127 of snorm(b) = max(b, -127) / 127 is folded into the basis weights, so
+// the decode needs no table. The sum runs as fused multiply-adds from the
+// +0.5 offset. The result differs from eval_sh by the rounding of the
+// reordered products and sum (a few ulps of the colour), and is clamped to
+// [0, 1] the same way.
 template <int DEG>
-__device__ __forceinline__ f3 eval_sh_fast(const uint32_t* co, f3 d, const float* snorm) {
+__device__ __forceinline__ f3 eval_sh_fast(const uint32_t* co, f3 d) {
   const float x = d.x, y = d.y, z = d.z;
+  constexpr float S = 1.0f / 127.0f;
   float w[16];
-  w[0] = 0.28209479177387814f;
+  w[0] = 0.28209479177387814f * S;
   if (DEG >= 1) {
-    w[1] = -0.4886025119029199f * y;
-    w[2] = 0.4886025119029199f * z;
-    w[3] = -0.4886025119029199f * x;
+    w[1] = (-0.4886025119029199f * S) * y;
+    w[2] = (0.4886025119029199f * S) * z;
+    w[3] = (-0.4886025119029199f * S) * x;
   }
   if (DEG >= 2) {
     const float xx = x * x, yy = y * y, zz = z * z;
-    w[4] = (1.0925484305920792f * x) * y;
-    w[5] = (-1.0925484305920792f * y) * z;
-    w[6] = 0.31539156525252005f * ((2.0f * zz - xx) - yy);
-    w[7] = (-1.0925484305920792f * x) * z;
-    w[8] = 0.5462742152960396f * (xx - yy);
+    w[4] = ((1.0925484305920792f * S) * x) * y;
+    w[5] = ((-1.0925484305920792f * S) * y) * z;
+    w[6] = (0.31539156525252005f * S) * ((2.0f * zz - xx) - yy);
+    w[7] = ((-1.0925484305920792f * S) * x) * z;
+    w[8] = (0.5462742152960396f * S) * (xx - yy);
   }
   if (DEG >= 3) {
     const float xx = x * x, yy = y * y, zz = z * z;
-    w[9] = (-0.5900435899266435f * y) * (3.0f * xx - yy);
-    w[10] = ((2.890611442640554f * x) * y) * z;
-    w[11] = (-0.4570457994644658f * y) * ((4.0f * zz - xx) - yy);
-    w[12] = (0.3731763325901154f * z) * ((2.0f * zz - 3.0f * xx) - 3.0f * yy);
-    w[13] = (-0.4570457994644658f * x) * ((4.0f * zz - xx) - yy);
-    w[14] = (1.445305721320277f * z) * (xx - yy);
-    w[15] = (-0.5900435899266435f * x) * (xx - 3.0f * yy);
+    w[9] = ((-0.5900435899266435f * S) * y) * (3.0f * xx - yy);
+    w[10] = (((2.890611442640554f * S) * x) * y) * z;
+    w[11] = ((-0.4570457994644658f * S) * y) * ((4.0f * zz - xx) - yy);
+    w[12] = ((0.3731763325901154f * S) * z) * ((2.0f * zz - 3.0f * xx) - 3.0f * yy);
+    w[13] = ((-0.4570457994644658f * S) * x) * ((4.0f * zz - xx) - yy);
+    w[14] = ((1.445305721320277f * S) * z) * (xx - yy);
+    w[15] = ((-0.5900435899266435f * S) * x) * (xx - 3.0f * yy);
   }
   f3 col = {0.5f, 0.5f, 0.5f};
 #pragma unroll
   for (int k = 0; k < (DEG + 1) * (DEG + 1); ++k) {
     const uint32_t p = co[k];
-    const float ws = w[k] * gsdm::pow2i((int)((p >> 24) & 255u) - 127);
-    col.x = __fmaf_rn(ws, snorm[p & 255u], col.x);
-    col.y = __fmaf_rn(ws, snorm[(p >> 8) & 255u], col.y);
-    col.z = __fmaf_rn(ws, snorm[(p >> 16) & 255u], col.z);
+    const float ws = w[k] * __uint_as_float((p >> 1) & 0x7f800000u);
+    col.x = __fmaf_rn(ws, fmaxf((float)(int8_t)(uint8_t)p, -127.0f), col.x);
+    col.y = __fmaf_rn(ws, fmaxf((float)(int8_t)(uint8_t)(p >> 8), -127.0f), col.y);
+    col.z = __fmaf_rn(ws, fmaxf((float)(int8_t)(uint8_t)(p >> 16), -127.0f), col.z);
   }
   return {clampf(col.x, 0.0f, 1.0f), clampf(col.y, 0.0f, 1.0f), clampf(col.z, 0.0f, 1.0f)};
 }
