@@ -170,7 +170,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_project(BatchView b, PassOptions 
     bool centre = false;
     Projected pr = {};
     float op = 0.0f, rx = 0.0f, ry = 0.0f, thr = 0.0f;
-    f3 vdir = {0.0f, 0.0f, 0.0f};
+    float ddx = 0.0f, ddy = 0.0f, ddz = 0.0f;  // positionLocal - cameraLocal
     // Project and cull; a splat that survives gets its tile box.
     do {
       if (!live) break;
@@ -186,10 +186,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_project(BatchView b, PassOptions 
 #pragma unroll
       for (int i = 0; i < 16; ++i) mv[i] = __ldg(ot + 16 + i);
       const float camx = __ldg(ot + 32), camy = __ldg(ot + 33), camz = __ldg(ot + 34);
-      // viewDirection = normalize(positionLocal - cameraLocal) (:469)
-      const float ddx = mo.x - camx, ddy = mo.y - camy, ddz = mo.z - camz;
-      const float dlen = sqrtf((ddx * ddx + ddy * ddy) + ddz * ddz);
-      vdir = {ddx / dlen, ddy / dlen, ddz / dlen};
+      ddx = mo.x - camx; ddy = mo.y - camy; ddz = mo.z - camz;
       // view = modelView * (p, 1) (:479-482); the FP64 form evaluates it in
       // double so far-origin coordinates do not cancel against the translation.
       double vxd = 0.0, vyd = 0.0, vzd = 0.0;
@@ -275,6 +272,18 @@ __global__ void __launch_bounds__(kBlock, 4) k_project(BatchView b, PassOptions 
     if (cnt > 0) {
       uint32_t co[16];
       load_sh(v.sh + (size_t)slot * v.C, v.degree, co);
+      // viewDirection = normalize(positionLocal - cameraLocal) (:469), which
+      // feeds only the colour: the reference's quotients for the EXACT form,
+      // a reciprocal square root (2 ulp) for the fast forms' colour.
+      const float dd2 = (ddx * ddx + ddy * ddy) + ddz * ddz;
+      f3 vdir;
+      if (FAST_SH) {
+        const float r = rsqrtf(dd2);
+        vdir = {ddx * r, ddy * r, ddz * r};
+      } else {
+        const float dlen = sqrtf(dd2);
+        vdir = {ddx / dlen, ddy / dlen, ddz / dlen};
+      }
       const f3 col = eval_sh_any<FAST_SH>(v.degree, co, vdir, s_snorm);
       mo4 = make_float4(pr.cx, pr.cy, pr.depth, op);
       conic_out[item] = make_float4(pr.conic_x, pr.conic_y, pr.conic_z, rx + ry * 512.0f);
