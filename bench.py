@@ -300,7 +300,8 @@ def run_serving(args) -> None:
         "value": best["frames_per_s"], "unit": "frames/s", "n_gpus": 1, "higher_is_better": True,
         "dtype": "f16", "data": "synthetic",
         "config": {"workload": "4 resident scenes (0.5M/1.5M/3M/6M), 720p/1080p/1440p, orbit cameras, "
-                               "40 GB workspace budget, 3 lanes, <= 8 views per batch",
+                               f"40 GB workspace budget, {args.serve_lanes} lanes, "
+                               f"<= {args.serve_max_views} views per batch",
                    "scene_scale": args.serve_scale, "requests_per_rate": args.serve_requests,
                    "lanes": args.serve_lanes, "max_views": args.serve_max_views},
         "rates": results,
