@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--forms", default="all", choices=["all", "batched"],
                     help="'batched' skips the timed plain (one view per launch) form")
     ap.add_argument("--serve", action="store_true", help="serving-loop measurement (configuration 4)")
+    ap.add_argument("--no-other-configs", action="store_true",
+                    help="skip configurations 3, 5 and 4 after the headline workload")
     ap.add_argument("--config3", action="store_true",
                     help="multi-cloud, multi-view batch (configuration 3): 8 clouds, 32 mixed-resolution cameras")
     ap.add_argument("--config5", action="store_true",
@@ -242,6 +244,10 @@ def run_reference(args) -> None:
 
 
 def run_serving(args) -> None:
+    print(json.dumps(serving_result(args)))
+
+
+def serving_result(args) -> dict:
     """Configuration 4: four resident scenes (0.5M, 1.5M, 3M, 6M Gaussians,
     configuration-1 distributions), Poisson arrivals, a random orbit camera
     and a size from {720p, 1080p, 1440p} per request, 40 GB workspace budget,
@@ -295,7 +301,7 @@ def run_serving(args) -> None:
         results[str(int(rate))] = server.run(reqs)
     server.close()
     best = max(list(results.values()) + ([closed] if closed else []), key=lambda r: r["frames_per_s"])
-    print(json.dumps({
+    return {
         "metric": "serving: p50/p99 ms and frames/s at Poisson request rates (configuration 4)",
         "value": best["frames_per_s"], "unit": "frames/s", "n_gpus": 1, "higher_is_better": True,
         "dtype": "f16", "data": "synthetic",
@@ -306,10 +312,14 @@ def run_serving(args) -> None:
                    "lanes": args.serve_lanes, "max_views": args.serve_max_views},
         "rates": results,
         "closed_loop": closed,
-    }))
+    }
 
 
 def run_config3(args) -> None:
+    print(json.dumps(config3_result(args)))
+
+
+def config3_result(args) -> dict:
     """Configuration 3: one store of 8 transformed clouds (50k..2M splats),
     32 cameras at 640x480..3840x2160, all views in one graph-captured batch
     with the autotuned launch shape; half2 raster."""
@@ -366,7 +376,8 @@ def run_config3(args) -> None:
         mse = float(np.mean((img[..., :3].astype(np.float64) - o64["rgba"][..., :3]) ** 2))
         psnr_db = float("inf") if mse == 0 else 10 * np.log10(1.0 / mse)
     pixels = sum(f["width"] * f["height"] for f in frames)
-    print(json.dumps({
+    pipe.dispose()
+    return {
         "metric": "frames/s, configuration 3 (8 clouds, 32 mixed-resolution cameras, one graph-captured batch)",
         "value": len(frames) / (ms / 1000.0), "unit": "frames/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "dtype": "f16", "data": "synthetic",
@@ -376,11 +387,14 @@ def run_config3(args) -> None:
         "stats": {"visible": stats["visibleGaussianCount"], "intersections": stats["intersectionCount"]},
         "megapixels_per_s": pixels / 1e6 / (ms / 1000.0),
         "psnr_db_vs_fp64_smallest_view": psnr_db, "clocks": ck,
-    }))
-    pipe.dispose()
+    }
 
 
 def run_config5(args) -> None:
+    print(json.dumps(config5_result(args)))
+
+
+def config5_result(args) -> dict:
     """Configuration 5: 12M splats in clusters centred at (1e5, 1e5, 0) with 5%
     near-degenerate axes, one 3840x2160 view, FP64 projection form (far-origin
     mean transform and near-singular conic in double) and the half2 raster;
@@ -422,7 +436,8 @@ def run_config5(args) -> None:
     ck = clocks.stop()
     ms = e0.elapsed_time(e1) / args.steps
     st = pipe.read_stats()
-    print(json.dumps({
+    pipe.dispose()
+    return {
         "metric": "frames/s, configuration 5 (12M far-origin splats, 3840x2160, FP64 projection form)",
         "value": 1000.0 / ms, "unit": "frames/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms, "higher_is_better": True, "dtype": "f16" if args.precision == "half2" else "f32",
@@ -431,8 +446,7 @@ def run_config5(args) -> None:
                                "5% near-degenerate axes, 3840x2160, FP64 projection form"},
         "stats": {"visible": st["visibleGaussianCount"], "intersections": st["intersectionCount"]},
         "intersections_per_s": st["intersectionCount"] / (ms / 1000.0), "clocks": ck,
-    }))
-    pipe.dispose()
+    }
 
 
 def main() -> None:
@@ -776,6 +790,19 @@ def main() -> None:
         "clocks": clock_info,
         "cpu_baseline": cpu,
     }
+    if world == 1 and args.forms == "all" and not args.no_other_configs:
+        # The other benchmark configurations, measured in the same run (each
+        # with its own resident scene and pipeline, after this workload's
+        # pipelines are released): configuration 3 (batching), 5 (FP64
+        # projection form) and 4 (serving).
+        out["other_configs"] = {}
+        for name, fn in (("config3", config3_result), ("config5", config5_result), ("serving", serving_result)):
+            try:
+                out["other_configs"][name] = fn(args)
+            except Exception as exc:  # reported in the line; the headline stands
+                out["other_configs"][name] = {"error": f"{type(exc).__name__}: {exc}"[:300]}
+            torch.cuda.synchronize()
+            torch.cuda.empty_cache()
     print(json.dumps(out))
 
 
