@@ -807,11 +807,23 @@ inline void launch_raster_pairs_t(const uint32_t* tile_offsets, const uint32_t* 
     launch_raster_pairs_tile<HALF, PERIODIC, 16>(tile_offsets, order, ids, mean, color, rec, b, o, ctl, stats, st);
 }
 
+// The half2 form's Cholesky evaluation needs the screen-space low-pass
+// filter: it bounds the conic's eigenvalues by 1 / filterVariance, and with
+// that the magnitudes of the f16 factor and of w at the patch centre. Below
+// this variance (the filter switched off or nearly: splats may be far thinner
+// than a pixel, and w at the patch centre reaches hundreds, past f16's
+// resolution) the half2 form renders with the FP32 form's evaluation. A CPU
+// model of the f16 arithmetic over random conics (sigma 0.001-300 px,
+// anisotropy up to 200) bounds the per-splat alpha error by 0.005 from a
+// variance of 0.05 up; with none it reaches 0.25.
+constexpr float kHalf2MinFilterVariance = 0.05f;
+
 inline void launch_raster_pairs(bool half, const uint32_t* tile_offsets, const uint32_t* order, const uint32_t* ids,
                                 const float4* mean, const float4* color, const float4* rec, const BatchView& b,
                                 const PassOptions& o, Control* ctl, bool stats, cudaStream_t st) {
   if (b.total_tiles == 0) return;
   const bool periodic = o.axis != 0u;
+  if (half && !periodic && !(o.filter >= kHalf2MinFilterVariance)) half = false;
   if (half) {
     if (periodic) launch_raster_pairs_t<true, true>(tile_offsets, order, ids, mean, color, rec, b, o, ctl, stats, st);
     else launch_raster_pairs_t<true, false>(tile_offsets, order, ids, mean, color, rec, b, o, ctl, stats, st);

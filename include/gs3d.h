@@ -67,7 +67,9 @@ typedef enum gs3d_boundary_policy {
  * half2 (from the splat's Cholesky factor about the patch centre, two pixels
  * per instruction), with its threshold test, alpha clamp and exp2, the colour
  * stored in half; transmittance and colour accumulation stay FP32 (the
- * periodic-boundary variant keeps the exponent in FP32). */
+ * periodic-boundary variant keeps the exponent in FP32). The f16 exponent
+ * relies on the screen-space low-pass filter: with filter_variance below
+ * 0.05 a HALF2 render evaluates as FP32. */
 /* Projection arithmetic. FP32 is the reference's (ProjectionStage.ts, bit-exact
  * with the CPU restatement). FP64 has no counterpart in the reference: it
  * evaluates the model-view mean transform in double (far-origin scenes) and
