@@ -64,6 +64,11 @@ __device__ __forceinline__ uint32_t bit_range(uint32_t s, uint32_t e) {
   return (e >= 32u ? 0xffffffffu : ((1u << e) - 1u)) & ~((1u << s) - 1u);
 }
 
+// Boxes of at least this many tiles are walked by the whole warp, one box at
+// a time, instead of in the shared rounds of the tile count and the emission
+// (the owner's parameters read once per box instead of once per round).
+constexpr uint32_t kWideBox = 64;
+
 // Per-warp tables of the projection's cooperative tile count: the splat
 // parameters of the tile test, the box, and the inclusive box-tile counts.
 struct CountShared {
@@ -82,7 +87,10 @@ struct CountShared {
 __device__ __forceinline__ uint32_t count_tiles_warp(CountShared& sm, uint32_t nbox, float vw, float vh,
                                                      uint32_t axis, float ts) {
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-  uint32_t incl = nbox;
+  // Wide boxes (kWideBox tiles or more) are left out of the shared rounds and
+  // walked by the whole warp afterwards, one box at a time.
+  const bool wide = nbox >= kWideBox;
+  uint32_t incl = wide ? 0u : nbox;
 #pragma unroll
   for (int d = 1; d < 32; d <<= 1) {
     const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
@@ -115,7 +123,34 @@ __device__ __forceinline__ uint32_t count_tiles_warp(CountShared& sm, uint32_t n
     if (valid && lane == 31u - (uint32_t)__clz(same)) sm.cnt[warp][owner] += __popc(hits & same);
   }
   __syncwarp();
-  return sm.cnt[warp][lane];
+  uint32_t cnt = sm.cnt[warp][lane];
+  // Wide boxes: the owner's parameters read once (broadcast), 32 tiles a step.
+  uint32_t wide_lanes = __ballot_sync(0xffffffffu, wide);
+  while (wide_lanes) {
+    const uint32_t w = (uint32_t)__ffs(wide_lanes) - 1u;
+    wide_lanes &= wide_lanes - 1u;
+    // The owner's parameters are read from the warp's table at each step
+    // (broadcast loads) rather than held in registers across the walk.
+    const volatile float(*vf)[kBlock / 32][32] = sm.f;
+    const volatile uint32_t(*vu)[kBlock / 32][32] = sm.u;
+    const uint32_t n = __shfl_sync(0xffffffffu, nbox, w);
+    uint32_t sum = 0;
+    for (uint32_t j0 = 0; j0 < n; j0 += 32) {
+      uint32_t k = j0 + lane;
+      bool hit = false;
+      if (k < n) {
+        k += k >= vu[3][warp][w] ? 1u : 0u;
+        const uint32_t bw = vu[2][warp][w];
+        const uint32_t by = k / bw, bx = k - by * bw;
+        hit = boundary_tile_hit(vf[0][warp][w], vf[1][warp][w], vf[2][warp][w], vf[3][warp][w], vf[4][warp][w],
+                                vf[5][warp][w], vf[6][warp][w], vf[7][warp][w], (int)(vu[0][warp][w] + bx),
+                                (int)(vu[1][warp][w] + by), vw, vh, axis, ts);
+      }
+      sum += __popc(__ballot_sync(0xffffffffu, hit));
+    }
+    if (lane == w) cnt = sum;
+  }
+  return cnt;
 }
 
 // GROUPED: some group holds several views (decode once, before the view
@@ -662,11 +697,13 @@ __device__ __forceinline__ void emit_group(EmitShared& sm, bool live, uint32_t g
   // A splat whose every box tile passed the projection's count (reserved ==
   // nbox) emits its whole box: those boxes are walked first without the tile
   // test, the others after it with the test. Each splat is walked once, so
-  // its records keep row-major box order.
+  // its records keep row-major box order. Wide boxes (kWideBox tiles or more)
+  // are walked afterwards by the whole warp, one box at a time.
   const bool full = reserved == nbox;
+  const bool wide = nbox >= kWideBox;
 #pragma unroll 1
   for (int pass = 0; pass < 2; ++pass) {
-    const uint32_t nb = (pass == 0) == full ? nbox : 0u;
+    const uint32_t nb = !wide && (pass == 0) == full ? nbox : 0u;
     uint32_t incl = nb;
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
@@ -726,6 +763,48 @@ __device__ __forceinline__ void emit_group(EmitShared& sm, bool live, uint32_t g
       }
     }
     __syncwarp();
+  }
+
+  // Wide boxes: the warp walks one box 32 tiles at a time with the owner's
+  // parameters read once (broadcast) instead of per round, in row-major box
+  // order, each hit after the box's earlier hits.
+  uint32_t wide_lanes = __ballot_sync(0xffffffffu, wide);
+  while (wide_lanes) {
+    const uint32_t w = (uint32_t)__ffs(wide_lanes) - 1u;
+    wide_lanes &= wide_lanes - 1u;
+    // The owner's parameters are read from the warp's table at each step
+    // (broadcast loads) rather than held in registers across the walk.
+    const volatile float(*vf)[kEmitWarps][32] = sm.f;
+    const volatile uint32_t(*vu)[kEmitWarps][32] = sm.u;
+    const uint32_t wn = __shfl_sync(0xffffffffu, nbox, w);
+    const uint32_t wres = vu[6][warp][w];
+    const bool wfull = wres == wn;
+    uint32_t wfilled = 0;
+    for (uint32_t k0 = 0; k0 < wn; k0 += 32) {
+      const uint32_t k = k0 + lane;
+      bool hit = false;
+      uint32_t t = 0;
+      if (k < wn) {
+        const uint32_t wbw = vu[2][warp][w];
+        const uint32_t by = k / wbw, bx = k - by * wbw;
+        const int tx = (int)(vu[0][warp][w] + bx), ty = (int)(vu[1][warp][w] + by);
+        hit = wfull || boundary_tile_hit(vf[0][warp][w], vf[1][warp][w], vf[2][warp][w], vf[3][warp][w],
+                                         vf[4][warp][w], vf[5][warp][w], vf[6][warp][w], vf[7][warp][w], tx, ty,
+                                         vf[8][warp][w], vf[9][warp][w], o.axis, o.tile_px);
+        t = vu[4][warp][w] + (uint32_t)ty * vu[3][warp][w] + (uint32_t)tx;
+      }
+      const uint32_t hits = __ballot_sync(0xffffffffu, hit);
+      if (hit) {
+        const uint32_t local = wfilled + __popc(hits & lt);
+        const uint32_t wbase = vu[5][warp][w];
+        if (local < wres && wbase + local < capacity) {
+          tile_keys[wbase + local] = t;
+          tile_vals[wbase + local] = vu[7][warp][w];
+        }
+      }
+      wfilled += __popc(hits);
+    }
+    if (lane == w) filled = wfilled;
   }
 
   // Sentinel padding for reserved slots without a hit.
