@@ -252,7 +252,9 @@ __global__ void __launch_bounds__(kBlock, 4) k_project(BatchView b, PassOptions 
         const float cond_num = (pr.cov_x + pr.cov_z) * (pr.cov_x + pr.cov_z);
         const bool redo = !pr.ok ? (-vz > v.vnear && -vz < v.vfar)
                                  : (pr.orig_det < 1e-2f * pr.det || !(cond_num <= 4e3f * pr.det));
-        if (redo) pr = project_fp64(vxd, vyd, vzd, so, q, mv, P, vw, vh, v.vnear, v.vfar, o.filter);
+        // The redo reads the model-view and projection rows from global memory
+        // (the same values as mv and P), so neither array needs a stack copy.
+        if (redo) pr = project_fp64(vxd, vyd, vzd, so, q, ot + 16, v.P, vw, vh, v.vnear, v.vfar, o.filter);
       }
       if (!pr.ok) break;
       op = clampf(so.w, 0.0f, 1.0f);
