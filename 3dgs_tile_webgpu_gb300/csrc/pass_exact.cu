@@ -65,8 +65,8 @@ __device__ __forceinline__ uint32_t bit_range(uint32_t s, uint32_t e) {
 }
 
 // Boxes of at least this many tiles are walked by the whole warp, one box at
-// a time, instead of in the shared rounds of the tile count and the emission
-// (the owner's parameters read once per box instead of once per round).
+// a time, instead of in the shared rounds of the tile count and the emission:
+// no per-tile owner lookup, the owner's parameters broadcast to every lane.
 constexpr uint32_t kWideBox = 64;
 
 // Per-warp tables of the projection's cooperative tile count: the splat
@@ -82,8 +82,10 @@ struct CountShared {
 // with the warp's lanes spread over the union of the 32 boxes (32 box tiles
 // per round) instead of each lane walking its own box. A lane walks nbox
 // tiles of its box in row-major order, skipping the box index u[3] (the
-// centre's tile, counted by the caller). Must be called by all 32 lanes; a
-// lane with nbox == 0 contributes nothing. Returns the lane's count.
+// centre's tile, counted by the caller); boxes of kWideBox tiles or more are
+// walked afterwards by the whole warp, one at a time. Must be called by all
+// 32 lanes; a lane with nbox == 0 contributes nothing. Returns the lane's
+// count.
 __device__ __forceinline__ uint32_t count_tiles_warp(CountShared& sm, uint32_t nbox, float vw, float vh,
                                                      uint32_t axis, float ts) {
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
@@ -124,7 +126,7 @@ __device__ __forceinline__ uint32_t count_tiles_warp(CountShared& sm, uint32_t n
   }
   __syncwarp();
   uint32_t cnt = sm.cnt[warp][lane];
-  // Wide boxes: the owner's parameters read once (broadcast), 32 tiles a step.
+  // Wide boxes: the whole warp walks one box, 32 tiles a step.
   uint32_t wide_lanes = __ballot_sync(0xffffffffu, wide);
   while (wide_lanes) {
     const uint32_t w = (uint32_t)__ffs(wide_lanes) - 1u;
@@ -767,9 +769,8 @@ __device__ __forceinline__ void emit_group(EmitShared& sm, bool live, uint32_t g
     __syncwarp();
   }
 
-  // Wide boxes: the warp walks one box 32 tiles at a time with the owner's
-  // parameters read once (broadcast) instead of per round, in row-major box
-  // order, each hit after the box's earlier hits.
+  // Wide boxes: the warp walks one box 32 tiles at a time, in row-major box
+  // order, each hit after the box's earlier hits (no per-tile owner lookup).
   uint32_t wide_lanes = __ballot_sync(0xffffffffu, wide);
   while (wide_lanes) {
     const uint32_t w = (uint32_t)__ffs(wide_lanes) - 1u;
